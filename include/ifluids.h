@@ -1,0 +1,184 @@
+/*
+ * ifluids.h - C ABI of the GB300 (sm_103a) incremental-fluids solver.
+ *
+ * One handle = one FluidSolver of the reference (tunabrain/incremental-fluids),
+ * with its state resident in device memory.  The handle owns every device
+ * buffer; the caller owns host buffers.  All calls on one handle must come from
+ * one host thread at a time; distinct handles may be driven from distinct
+ * threads.  Work is enqueued on the handle's CUDA stream; calls that return
+ * data to the host synchronise that stream.  No exception crosses this ABI:
+ * every entry point returns an ifl_status.
+ *
+ * Reference surface replaced (paths inside the reference project):
+ *   FluidSolver(int w, int h, double density)            3-conjugate-gradients/Fluid.cpp:401
+ *   FluidSolver(w, h, density, bodies)                   4-solid-boundaries/Fluid.cpp:836,
+ *                                                        5-curved-boundaries/Fluid.cpp:894
+ *   FluidSolver(w, h, rhoAir, rhoSoot, diffusion, bodies) 6-heat/Fluid.cpp:921,
+ *                                                        7-variable-density/Fluid.cpp:945
+ *   void addInflow(x, y, w, h, d, u, v)                  3-conjugate-gradients/Fluid.cpp:449
+ *   void addInflow(x, y, w, h, d, t, u, v)               7-variable-density/Fluid.cpp:1036
+ *   void update(double timestep)                         3-conjugate-gradients/Fluid.cpp:433,
+ *                                                        7-variable-density/Fluid.cpp:995
+ *   double ambientT()                                    7-variable-density/Fluid.cpp:1043
+ *   SolidBox / SolidSphere / SolidBody::update           4-solid-boundaries/Fluid.cpp:79-241
+ * The reference has no field readback (only toImage -> PNG); ifl_read_field
+ * is the replacement for that.
+ */
+#ifndef IFLUIDS_H
+#define IFLUIDS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ifl_solver ifl_solver;
+
+/* Status codes. */
+enum {
+    IFL_OK = 0,
+    IFL_ERR_ARG = -1,        /* invalid argument                                  */
+    IFL_ERR_CUDA = -2,       /* CUDA runtime error (see ifl_last_error)           */
+    IFL_ERR_NOMEM = -3,      /* device allocation failed                          */
+    IFL_ERR_TIMEOUT = -4,    /* a bounded device-side wait gave up (status word)  */
+    IFL_ERR_UNSUPPORTED = -5 /* configuration outside the supported envelope      */
+};
+
+/* Variant = tutorial step of the reference whose update() is reproduced. */
+enum {
+    IFL_PLAIN = 3,    /* 3-conjugate-gradients: MIC(0)-PCG, no solids          */
+    IFL_SOLID = 4,    /* 4-solid-boundaries: binary solid cells               */
+    IFL_CURVED = 5,   /* 5-curved-boundaries: fractional cell volumes         */
+    IFL_HEAT = 6,     /* 6-heat: + temperature, heat diffusion, buoyancy       */
+    IFL_VARDENS = 7   /* 7-variable-density: + per-face density               */
+};
+
+/* Storage / arithmetic form. */
+enum {
+    IFL_FP64 = 0,  /* drop-in: FP64 everywhere, bit-exact advection/assembly   */
+    IFL_FP32 = 1   /* FP32 fields, matrix, advection, matvec, MIC(0) apply;
+                      FP64 dot products, max-norm, alpha/beta, MIC(0) factor */
+};
+
+/* Element types for field transfer. */
+enum { IFL_DT_F64 = 0, IFL_DT_F32 = 1, IFL_DT_U8 = 2 };
+
+/* Quantities. */
+enum { IFL_Q_D = 0, IFL_Q_T = 1, IFL_Q_U = 2, IFL_Q_V = 3 };
+
+/* Per-quantity arrays; a field id is IFL_FIELD(quantity, array). */
+enum {
+    IFL_A_SRC = 0,      /* the quantity itself (FluidQuantity::_src)            */
+    IFL_A_DST = 1,      /* advection target buffer (FluidQuantity::_dst)        */
+    IFL_A_PHI = 2,      /* distance samples at cell corners, (w+1) x (h+1)      */
+    IFL_A_VOLUME = 3,   /* fluid volume fraction                                 */
+    IFL_A_NORMALX = 4,
+    IFL_A_NORMALY = 5,
+    IFL_A_CELL = 8,     /* u8: 0 fluid, 1 solid                                  */
+    IFL_A_BODY = 9      /* u8: index of the nearest body                         */
+};
+#define IFL_FIELD(q, a) (((q) << 8) | (a))
+/* Solver-level arrays (w x h unless noted). */
+enum {
+    IFL_F_R = 16, IFL_F_P = 17, IFL_F_Z = 18, IFL_F_S = 19, IFL_F_PRECON = 20,
+    IFL_F_ADIAG = 21, IFL_F_APLUSX = 22, IFL_F_APLUSY = 23,
+    IFL_F_UDENS = 24,   /* (w+1) x h */
+    IFL_F_VDENS = 25    /* w x (h+1) */
+};
+
+/* Phases of one update(), for per-phase parity runs (ifl_run_phase). */
+enum {
+    IFL_PH_FILL_SOLID = 0, IFL_PH_HEAT = 1, IFL_PH_EXTRAP_T = 2, IFL_PH_BUOYANCY = 3,
+    IFL_PH_BC = 4, IFL_PH_RHS = 5, IFL_PH_DENSITIES = 6, IFL_PH_MATRIX = 7,
+    IFL_PH_PRECON = 8, IFL_PH_PROJECT = 9, IFL_PH_APPLY_P = 10,
+    IFL_PH_EXTRAP_DUV = 11, IFL_PH_ADVECT = 12
+};
+
+/* PCG outcome. */
+enum { IFL_PCG_CONVERGED = 0, IFL_PCG_INITIAL = 1, IFL_PCG_CAP = 2 };
+
+typedef struct {
+    int32_t variant;           /* IFL_PLAIN .. IFL_VARDENS                       */
+    int32_t w, h;              /* pressure grid size (>= 2 each)                 */
+    int32_t precision;         /* IFL_FP64 or IFL_FP32                           */
+    double density_air;        /* `density` of steps 3-5, rhoAir of 6-7 (0.1)    */
+    double density_soot;       /* rhoSoot (1.0)                                  */
+    double diffusion;          /* heat diffusion (0.01)                          */
+    int32_t max_iter_pressure; /* 600 in step 3, 2000 in steps 4-7               */
+    int32_t max_iter_heat;     /* 2000                                           */
+    void *stream;              /* cudaStream_t to use; NULL = handle-owned stream */
+} ifl_params;
+
+/* Solid body; same parameters as SolidBox(x, y, sx, sy, t, vx, vy, vt) and
+ * SolidSphere(x, y, s, t, vx, vy, vt) (scale_y is ignored for spheres). */
+typedef struct {
+    int32_t type;  /* 0 = box, 1 = sphere */
+    int32_t pad_;
+    double pos_x, pos_y, scale_x, scale_y, theta, vel_x, vel_y, vel_theta;
+} ifl_body;
+
+typedef struct {
+    int32_t iterations;  /* matrix-vector products performed by the last solve */
+    int32_t status;      /* IFL_PCG_*                                          */
+    double max_error;    /* last infinity norm of the residual                 */
+} ifl_pcg_stats;
+
+typedef struct {
+    ifl_pcg_stats pressure;
+    ifl_pcg_stats heat;
+    uint32_t device_flags;  /* bit 0: bounded wait timed out; bit 1: solid cell on
+                               the outer ring (outside the parity envelope) */
+    uint32_t steps;         /* update() calls completed                         */
+} ifl_step_stats;
+
+/* Fill *p with the reference's defaults for a variant and grid size. */
+void ifl_default_params(ifl_params *p, int variant, int w, int h);
+
+/* FluidSolver constructors (all steps). */
+int ifl_create(const ifl_params *p, ifl_solver **out);
+int ifl_destroy(ifl_solver *s);
+
+/* Bodies (steps 4-7).  The reference keeps references to caller-owned bodies
+ * and the caller moves them between steps (SolidBody::update); here the caller
+ * passes the current body table before update() (it is copied), or lets the
+ * handle advance its own copy with ifl_advance_bodies. */
+int ifl_set_bodies(ifl_solver *s, const ifl_body *bodies, int n);
+int ifl_get_bodies(ifl_solver *s, ifl_body *bodies, int capacity, int *n);
+int ifl_advance_bodies(ifl_solver *s, double dt);
+
+/* FluidSolver::addInflow; `t` is ignored below step 6. */
+int ifl_add_inflow(ifl_solver *s, double x, double y, double w, double h,
+                   double d, double t, double u, double v);
+/* FluidSolver::update; asynchronous on the handle's stream. */
+int ifl_update(ifl_solver *s, double dt);
+/* Run one phase of update() (tests; same semantics as inside update). */
+int ifl_run_phase(ifl_solver *s, int phase, double dt);
+/* FluidSolver::ambientT (294 K). */
+double ifl_ambient_t(const ifl_solver *s);
+
+/* Field transfer between the device state and a dense row-major host array
+ * (idx = x + y*w).  `dtype` converts on the fly.  Both synchronise. */
+int ifl_field_shape(const ifl_solver *s, int field, int *w, int *h);
+int ifl_read_field(ifl_solver *s, int field, void *host, size_t bytes, int dtype);
+int ifl_write_field(ifl_solver *s, int field, const void *host, size_t bytes, int dtype);
+/* FluidQuantity::flip for one quantity (tests). */
+int ifl_flip(ifl_solver *s, int quantity);
+
+/* PCG outcome of the last update (synchronises). */
+int ifl_get_stats(ifl_solver *s, ifl_step_stats *out);
+/* -1: stop on the residual test (default); k >= 0: run exactly k iterations. */
+int ifl_set_pinned_iterations(ifl_solver *s, int k);
+
+int ifl_synchronize(ifl_solver *s);
+void *ifl_stream(ifl_solver *s);
+/* Kernel launches of this library issued by the handle since creation. */
+int64_t ifl_launch_count(const ifl_solver *s);
+const char *ifl_last_error(const ifl_solver *s);
+const char *ifl_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,114 @@
+// ifl_internal.h - device data layout and kernel launchers of the GB300 solver.
+//
+// HBM layout of one scene (w x h pressure cells):
+//   every 2-D array is row-major with one shared row pitch P (elements),
+//   P = round_up(w + 2, 32), and h + 2 rows, so that the largest grid of the
+//   scene (the (w+2) x (h+1) / (w+1) x (h+2) corner grids of the distance
+//   field) fits, every row starts 128-byte aligned for both element sizes and a
+//   cell (x, y) of any grid lives at x + y*P.
+// Field storage type F is double (IFL_FP64) or float (IFL_FP32); solid
+// geometry (distance, normals, volumes) and the MIC(0) factor stay FP64.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace ifl {
+
+enum : uint8_t { CELL_FLUID = 0, CELL_SOLID = 1 };
+
+// Neighbour bits consumed by the PCG kernel (one byte per cell).
+enum : uint8_t {
+    NB_SELF = 1,   // cell takes part in masked MIC(0) work (fluid, or unmasked variant)
+    NB_LEFT = 2,   // x-1 term present in MIC(0) factor / forward solve
+    NB_DOWN = 4,   // y-1 term present
+    NB_RIGHT = 8,  // x+1 term present in backward solve
+    NB_UP = 16,    // y+1 term present
+    NB_RED = 32    // cell takes part in dot products / max-norm / AXPY
+};
+
+// Rigid body with host-computed trigonometry (cos/sin of +theta and -theta are
+// evaluated once per update by the host C library, exactly the values the
+// reference's rotate() obtains on every call).
+struct DevBody {
+    int type;  // 0 box, 1 sphere
+    int pad_;
+    double px, py, sx, sy, vx, vy, vth;
+    double cpos, spos, cneg, sneg;
+};
+
+template <typename F>
+struct Quant {
+    F *src, *dst;
+    double *phi, *vol, *nx, *ny;
+    uint8_t *cell, *body, *ready;
+    int *list;  // extrapolation work lists (2 x P*(h+2) ints)
+    int w, h;
+    double ox, oy;
+};
+
+template <typename F>
+struct Scene {
+    int variant, w, h, P;
+    int nq;  // 3 or 4 quantities
+    double hx;
+    double rho_air, rho_soot, diffusion, t_amb, g;
+    Quant<F> q[4];  // d, t, u, v
+    F *r, *p, *z, *sa, *sb, *as;
+    F *adiag, *ax, *ay;
+    F *lx, *ly, *pcf;  // MIC(0) apply operands in storage precision
+    double *pc;        // MIC(0) factor, FP64
+    uint8_t *nb;
+    F *udens, *vdens;
+    const DevBody *bodies;
+    int nbodies;
+    unsigned *flags;  // device status word
+};
+
+struct PcgOut {
+    int iterations;
+    int status;
+    double max_error;
+};
+
+// Scratch for the persistent PCG kernel.
+struct PcgScratch {
+    double *partials;    // 4 * max_blocks
+    unsigned *barrier;   // 2 words
+    unsigned *progress;  // one word per 32-row strip
+    PcgOut *out;
+    int max_blocks;
+};
+
+enum { PCG_FACTOR = 1, PCG_SOLVE = 2 };
+
+struct PcgConfig {
+    int mode;
+    int limit;
+    int pinned;
+    int heat;  // 1: writes to the heat PcgOut slot
+};
+
+// Launchers (stream-ordered, no host synchronisation).
+template <typename F> void launch_inflow(const Scene<F> &S, int qi, double x0, double y0, double x1,
+                                         double y1, double val, cudaStream_t st);
+template <typename F> void launch_fill_solid(const Scene<F> &S, cudaStream_t st);
+template <typename F> void launch_bc(const Scene<F> &S, cudaStream_t st);
+template <typename F> void launch_buoyancy(const Scene<F> &S, double dt, cudaStream_t st);
+template <typename F> void launch_assemble(const Scene<F> &S, double dt, int what, cudaStream_t st);
+template <typename F> void launch_heat_assemble(const Scene<F> &S, double dt, cudaStream_t st);
+template <typename F> void launch_apply_pressure(const Scene<F> &S, double dt, cudaStream_t st);
+template <typename F> void launch_extrapolate(const Scene<F> &S, unsigned qmask, cudaStream_t st);
+template <typename F> void launch_advect(const Scene<F> &S, double dt, cudaStream_t st);
+template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
+                                             cudaStream_t st, int *blocks_used);
+template <typename F> int pcg_max_blocks();
+
+// what-bits for launch_assemble
+enum { ASM_RHS = 1, ASM_MATRIX = 2, ASM_DENS = 4 };
+
+// Device flag bits (Scene::flags[0]).
+enum : unsigned { FLAG_TIMEOUT = 1u, FLAG_RING_SOLID = 2u };
+
+}  // namespace ifl

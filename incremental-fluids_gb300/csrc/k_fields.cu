@@ -1,0 +1,660 @@
+// k_fields.cu - per-cell / per-face kernels of one solver step (sm_103a).
+//
+// Each kernel is a gather: one thread owns one output cell or face and
+// reproduces, in the same floating-point order, every update the reference's
+// row-major loops apply to that location (scatters such as applyPressure and
+// setBoundaryCondition become "earlier cell first" gathers).  FP64 storage
+// gives results identical to the reference; FP32 storage runs the same
+// formulas (advection in FP32, cheap per-cell bookkeeping in FP64 then
+// rounded).
+#include "ifl_device.cuh"
+
+namespace ifl {
+
+namespace {
+
+__device__ __forceinline__ int qid_of(int nq, int z) { return nq == 4 ? z : (z == 0 ? 0 : z + 1); }
+
+template <typename F> __device__ __forceinline__ F ldv(const F *p) { return *(const volatile F *)p; }
+template <typename F> __device__ __forceinline__ void stv(F *p, F v) { *(volatile F *)p = v; }
+
+// ----------------------------------------------------------------- inflow
+// FluidQuantity::addInflow (3-conjugate-gradients/Fluid.cpp:167-184).  The x
+// bound is the quantity's height (as in the reference) and cells are
+// addressed by the flat index x + y*w.  When that index can wrap into the next
+// row two rectangle cells may hit one location, so the rectangle is then
+// walked by one thread in the reference's order.
+template <typename F>
+__global__ void inflow_kernel(Quant<F> Q, int P, double hx, double x0, double y0, double x1, double y1,
+                              double val) {
+    int ix0 = (int)(x0 / hx - Q.ox);
+    int iy0 = (int)(y0 / hx - Q.oy);
+    int ix1 = (int)(x1 / hx - Q.ox);
+    int iy1 = (int)(y1 / hx - Q.oy);
+    int ylo = max(iy0, 0), yhi = min(iy1, Q.h);
+    int xlo = max(ix0, 0), xhi = min(ix1, Q.h);
+    if (ylo >= yhi || xlo >= xhi) return;
+    long n = (long)Q.w * Q.h;
+    int nx = xhi - xlo, ncell = nx * (yhi - ylo);
+    bool serial = xhi > Q.w;
+    int start = serial ? 0 : threadIdx.x;
+    int step = serial ? 1 : blockDim.x;
+    if (serial && threadIdx.x != 0) return;
+    for (int i = start; i < ncell; i += step) {
+        int x = xlo + i % nx, y = ylo + i / nx;
+        double l = length2((2.0 * (x + 0.5) * hx - (x0 + x1)) / (x1 - x0),
+                           (2.0 * (y + 0.5) * hx - (y0 + y1)) / (y1 - y0));
+        double vi = cubic_pulse(l) * val;
+        long flat = (long)x + (long)y * Q.w;
+        if (flat >= n) continue;
+        int fx = (int)(flat % Q.w), fy = (int)(flat / Q.w);
+        F *c = Q.src + fx + (size_t)fy * P;
+        if (fabs((double)*c) < fabs(vi)) *c = (F)vi;
+    }
+}
+
+// ------------------------------------------------------------ solid fields
+// fillSolidFields, distance grid part (7-variable-density/Fluid.cpp:479-488)
+template <typename F>
+__global__ void phi_kernel(Scene<F> S) {
+    Quant<F> Q = S.q[qid_of(S.nq, blockIdx.z)];
+    int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix > Q.w || iy > Q.h) return;
+    double x = (ix + Q.ox - 0.5) * S.hx;
+    double y = (iy + Q.oy - 0.5) * S.hx;
+    double phi = body_distance(S.bodies[0], x, y);
+    for (int i = 1; i < S.nbodies; i++) phi = smin(phi, body_distance(S.bodies[i], x, y));
+    Q.phi[ix + (size_t)iy * S.P] = phi;
+}
+
+// fillSolidFields, per-cell part (4-solid-boundaries/Fluid.cpp:453-479,
+// 7-variable-density/Fluid.cpp:490-521)
+template <typename F>
+__global__ void cell_kernel(Scene<F> S) {
+    Quant<F> Q = S.q[qid_of(S.nq, blockIdx.z)];
+    int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= Q.w || iy >= Q.h) return;
+    size_t idx = ix + (size_t)iy * S.P;
+    double x = (ix + Q.ox) * S.hx;
+    double y = (iy + Q.oy) * S.hx;
+    int body = 0;
+    double d = body_distance(S.bodies[0], x, y);
+    for (int i = 1; i < S.nbodies; i++) {
+        double id = body_distance(S.bodies[i], x, y);
+        if (id < d) {
+            body = i;
+            d = id;
+        }
+    }
+    Q.body[idx] = (uint8_t)body;
+    uint8_t cell;
+    double nx, ny;
+    if (S.variant >= 5) {
+        double vol = 1.0 - occupancy(Q.phi[idx], Q.phi[idx + 1], Q.phi[idx + S.P], Q.phi[idx + S.P + 1]);
+        if (vol < 0.01) vol = 0.0;
+        Q.vol[idx] = vol;
+        body_normal(S.bodies[body], nx, ny, x, y);
+        cell = (vol == 0.0) ? CELL_SOLID : CELL_FLUID;
+    } else {
+        cell = (d < 0.0) ? CELL_SOLID : CELL_FLUID;
+        body_normal(S.bodies[body], nx, ny, x, y);
+    }
+    Q.cell[idx] = cell;
+    Q.nx[idx] = nx;
+    Q.ny[idx] = ny;
+    if (cell != CELL_FLUID && (ix == 0 || iy == 0 || ix == Q.w - 1 || iy == Q.h - 1))
+        atomicOr(S.flags, FLAG_RING_SOLID);
+}
+
+// ------------------------------------------------------ boundary condition
+// setBoundaryCondition (4-solid-boundaries/Fluid.cpp:812-833): the later
+// (right / upper) solid cell's write wins, then the domain walls are zeroed.
+template <typename F>
+__global__ void bc_kernel(Scene<F> S) {
+    const int w = S.w, h = S.h, P = S.P;
+    const uint8_t *cell = S.q[0].cell, *body = S.q[0].body;
+    int fx = blockIdx.x * blockDim.x + threadIdx.x, fy = blockIdx.y * blockDim.y + threadIdx.y;
+    const double hx = S.hx;
+    if (blockIdx.z == 0) {  // u faces (w+1) x h
+        if (fx > w || fy >= h) return;
+        F *u = S.q[2].src + fx + (size_t)fy * P;
+        if (fx == 0 || fx == w) {
+            *u = (F)0.0;
+            return;
+        }
+        size_t c = fx + (size_t)fy * P;
+        if (cell[c] == CELL_SOLID)
+            *u = (F)body_vel_x(S.bodies[body[c]], fx * hx, (fy + 0.5) * hx);
+        else if (cell[c - 1] == CELL_SOLID)
+            *u = (F)body_vel_x(S.bodies[body[c - 1]], ((fx - 1) + 1.0) * hx, (fy + 0.5) * hx);
+    } else {  // v faces w x (h+1)
+        if (fx >= w || fy > h) return;
+        F *v = S.q[3].src + fx + (size_t)fy * P;
+        if (fy == 0 || fy == h) {
+            *v = (F)0.0;
+            return;
+        }
+        size_t c = fx + (size_t)fy * P;
+        if (cell[c] == CELL_SOLID)
+            *v = (F)body_vel_y(S.bodies[body[c]], (fx + 0.5) * hx, fy * hx);
+        else if (cell[c - P] == CELL_SOLID)
+            *v = (F)body_vel_y(S.bodies[body[c - P]], (fx + 0.5) * hx, ((fy - 1) + 1.0) * hx);
+    }
+}
+
+// ---------------------------------------------------------------- buoyancy
+// addBuoyancy (7-variable-density/Fluid.cpp:908-919), gathered per v face.
+template <typename F>
+__global__ void buoyancy_kernel(Scene<F> S, double dt) {
+    int fx = blockIdx.x * blockDim.x + threadIdx.x, fy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (fx >= S.w || fy > S.h) return;
+    const int P = S.P;
+    const double alpha = (S.rho_soot - S.rho_air) / S.rho_air;
+    const F *d = S.q[0].src, *t = S.q[1].src;
+    F *v = S.q[3].src + fx + (size_t)fy * P;
+    double val = (double)*v;
+    if (fy > 0) {
+        size_t c = fx + (size_t)(fy - 1) * P;
+        double b = dt * S.g * (alpha * (double)d[c] - ((double)t[c] - S.t_amb) / S.t_amb);
+        val += b * 0.5;
+    }
+    if (fy < S.h) {
+        size_t c = fx + (size_t)fy * P;
+        double b = dt * S.g * (alpha * (double)d[c] - ((double)t[c] - S.t_amb) / S.t_amb);
+        val += b * 0.5;
+    }
+    *v = (F)val;
+}
+
+// ------------------------------------------------------------- assembly
+// Cell density of computeDensities (7-variable-density/Fluid.cpp:666-667).
+template <typename F>
+__device__ __forceinline__ double cell_density(const Scene<F> &S, double alpha, size_t c) {
+    double dens = S.rho_air * S.t_amb / (double)S.q[1].src[c] * (1.0 + alpha * (double)S.q[0].src[c]);
+    return smax(dens, 0.05 * S.rho_air);
+}
+// u-face density (x, y), 0 <= x <= w: 0.5*left cell + 0.5*right cell.
+template <typename F>
+__device__ __forceinline__ double udens_at(const Scene<F> &S, double alpha, int x, int y) {
+    double acc = 0.0;
+    if (x > 0) acc += 0.5 * cell_density(S, alpha, (x - 1) + (size_t)y * S.P);
+    if (x < S.w) acc += 0.5 * cell_density(S, alpha, x + (size_t)y * S.P);
+    return acc;
+}
+// v-face density (x, y), 0 <= y <= h.
+template <typename F>
+__device__ __forceinline__ double vdens_at(const Scene<F> &S, double alpha, int x, int y) {
+    double acc = 0.0;
+    if (y > 0) acc += 0.5 * cell_density(S, alpha, x + (size_t)(y - 1) * S.P);
+    if (y < S.h) acc += 0.5 * cell_density(S, alpha, x + (size_t)y * S.P);
+    return acc;
+}
+
+// Pressure-matrix coefficient of the x-face between cells (x-1, y) and (x, y).
+template <typename F>
+__device__ __forceinline__ double xface_factor(const Scene<F> &S, double scale, double alpha, int x, int y) {
+    if (S.variant <= 4) return scale;
+    double vol = S.q[2].vol[x + (size_t)y * S.P];
+    if (S.variant == 7) return scale * vol / udens_at(S, alpha, x, y);
+    return scale * vol;
+}
+// y-face between (x, y-1) and (x, y).  Step 7 reads the face density at the
+// u-grid flat index x + y*(w+1) of the w-wide v-density array; *present is
+// cleared when that index leaves the array.
+template <typename F>
+__device__ __forceinline__ double yface_factor(const Scene<F> &S, double scale, double alpha, int x, int y,
+                                               bool *present) {
+    if (S.variant <= 4) return scale;
+    double vol = S.q[3].vol[x + (size_t)y * S.P];
+    if (S.variant == 7) {
+        long flat = (long)x + (long)y * (S.w + 1);
+        if (flat >= (long)S.w * (S.h + 1)) {
+            *present = false;
+            return 0.0;
+        }
+        int fx = (int)(flat % S.w), fy = (int)(flat / S.w);
+        return scale * vol / vdens_at(S, alpha, fx, fy);
+    }
+    return scale * vol;
+}
+
+// buildRhs + computeDensities + buildPressureMatrix (+ neighbour bits), one
+// thread per cell.  References: buildRhs 3-conjugate-gradients/Fluid.cpp:208-217,
+// 4-solid-boundaries/Fluid.cpp:614-627, 7-variable-density/Fluid.cpp:624-653;
+// buildPressureMatrix 3-conjugate-gradients/Fluid.cpp:222-244,
+// 4-solid-boundaries/Fluid.cpp:629-654, 5-curved-boundaries/Fluid.cpp:686-713,
+// 7-variable-density/Fluid.cpp:680-707.  The diagonal accumulates its faces
+// in the reference's visiting order: lower face, left face, right face, upper
+// face.
+template <typename F>
+__global__ void assemble_kernel(Scene<F> S, double dt, int what) {
+    const int w = S.w, h = S.h, P = S.P;
+    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const size_t c = x + (size_t)y * P;
+    const int var = S.variant;
+    const uint8_t *cell = S.q[0].cell;
+    const bool plain = var == 3;
+    const bool fl = plain || cell[c] == CELL_FLUID;
+    const double alpha = (S.rho_soot - S.rho_air) / S.rho_air;
+    const F *U = S.q[2].src, *V = S.q[3].src;
+
+    if (what & ASM_RHS) {
+        double scale = 1.0 / S.hx;
+        double r;
+        if (var <= 4) {
+            r = fl ? -scale * ((double)U[c + 1] - (double)U[c] + (double)V[c + P] - (double)V[c]) : 0.0;
+        } else if (!fl) {
+            r = 0.0;
+        } else {
+            const double *uv = S.q[2].vol, *vv = S.q[3].vol;
+            double uv0 = uv[c], uv1 = uv[c + 1], vv0 = vv[c], vv1 = vv[c + P];
+            r = -scale * (uv1 * (double)U[c + 1] - uv0 * (double)U[c] + vv1 * (double)V[c + P] -
+                          vv0 * (double)V[c]);
+            if (S.nbodies > 0) {
+                double vol = S.q[0].vol[c];
+                const uint8_t *body = S.q[0].body;
+                const double hx = S.hx;
+                if (x > 0) r -= (uv0 - vol) * body_vel_x(S.bodies[body[c - 1]], x * hx, (y + 0.5) * hx);
+                if (y > 0) r -= (vv0 - vol) * body_vel_y(S.bodies[body[c - P]], (x + 0.5) * hx, y * hx);
+                if (x < w - 1)
+                    r += (uv1 - vol) * body_vel_x(S.bodies[body[c + 1]], (x + 1.0) * hx, (y + 0.5) * hx);
+                if (y < h - 1)
+                    r += (vv1 - vol) * body_vel_y(S.bodies[body[c + P]], (x + 0.5) * hx, (y + 1.0) * hx);
+            }
+        }
+        S.r[c] = (F)r;
+    }
+
+    if (what & ASM_DENS) {  // face densities for applyPressure (step 7)
+        S.udens[c] = (F)udens_at(S, alpha, x, y);
+        if (x == w - 1) S.udens[c + 1] = (F)udens_at(S, alpha, w, y);
+        S.vdens[c] = (F)vdens_at(S, alpha, x, y);
+        if (y == h - 1) S.vdens[c + P] = (F)vdens_at(S, alpha, x, h);
+    }
+
+    if (what & ASM_MATRIX) {
+        double scale = (var == 7) ? dt / (S.hx * S.hx) : dt / (S.rho_air * S.hx * S.hx);
+        bool fL = x > 0 && (plain || (fl && cell[c - 1] == CELL_FLUID));
+        bool fR = x < w - 1 && (plain || (fl && cell[c + 1] == CELL_FLUID));
+        bool fD = y > 0 && (plain || (fl && cell[c - P] == CELL_FLUID));
+        bool fU = y < h - 1 && (plain || (fl && cell[c + P] == CELL_FLUID));
+        double diag = 0.0, ax = 0.0, ay = 0.0;
+        if (fD) {
+            double f = yface_factor(S, scale, alpha, x, y, &fD);
+            if (fD) diag += f;
+        }
+        if (fL) diag += xface_factor(S, scale, alpha, x, y);
+        if (fR) {
+            double f = xface_factor(S, scale, alpha, x + 1, y);
+            diag += f;
+            ax = -f;
+        }
+        if (fU) {
+            double f = yface_factor(S, scale, alpha, x, y + 1, &fU);
+            if (fU) {
+                diag += f;
+                ay = -f;
+            }
+        }
+        S.adiag[c] = (F)diag;
+        S.ax[c] = (F)ax;
+        S.ay[c] = (F)ay;
+        uint8_t nb = (fl ? NB_SELF : 0) | (fL ? NB_LEFT : 0) | (fD ? NB_DOWN : 0) | (fR ? NB_RIGHT : 0) |
+                     (fU ? NB_UP : 0) | ((var < 6 || cell[c] == CELL_FLUID) ? NB_RED : 0);
+        // The MIC(0) sweeps use the fluid test of each neighbour, independent
+        // of whether the face carries a matrix entry.
+        if (!plain) {
+            nb = (fl ? NB_SELF : 0) | ((var < 6 || fl) ? NB_RED : 0);
+            if (x > 0 && cell[c - 1] == CELL_FLUID) nb |= NB_LEFT;
+            if (y > 0 && cell[c - P] == CELL_FLUID) nb |= NB_DOWN;
+            if (x < w - 1 && cell[c + 1] == CELL_FLUID) nb |= NB_RIGHT;
+            if (y < h - 1 && cell[c + P] == CELL_FLUID) nb |= NB_UP;
+        }
+        S.nb[c] = nb;
+    }
+}
+
+// r = T, buildHeatDiffusionMatrix (7-variable-density/Fluid.cpp:709-737,
+// 1001) and the neighbour bits.
+template <typename F>
+__global__ void heat_assemble_kernel(Scene<F> S, double dt) {
+    const int w = S.w, h = S.h, P = S.P;
+    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const size_t c = x + (size_t)y * P;
+    const uint8_t *cell = S.q[0].cell;
+    const bool fl = cell[c] == CELL_FLUID;
+    S.r[c] = S.q[1].src[c];
+    double scale = S.diffusion * dt * 1.0 / (S.hx * S.hx);
+    bool fL = x > 0 && fl && cell[c - 1] == CELL_FLUID;
+    bool fR = x < w - 1 && fl && cell[c + 1] == CELL_FLUID;
+    bool fD = y > 0 && fl && cell[c - P] == CELL_FLUID;
+    bool fU = y < h - 1 && fl && cell[c + P] == CELL_FLUID;
+    double diag = 1.0;
+    if (fD) diag += scale;
+    if (fL) diag += scale;
+    if (fR) diag += scale;
+    if (fU) diag += scale;
+    S.adiag[c] = (F)diag;
+    S.ax[c] = (F)(fR ? -scale : 0.0);
+    S.ay[c] = (F)(fU ? -scale : 0.0);
+    uint8_t nb = (fl ? NB_SELF : 0) | (fl ? NB_RED : 0);
+    if (x > 0 && cell[c - 1] == CELL_FLUID) nb |= NB_LEFT;
+    if (y > 0 && cell[c - P] == CELL_FLUID) nb |= NB_DOWN;
+    if (x < w - 1 && cell[c + 1] == CELL_FLUID) nb |= NB_RIGHT;
+    if (y < h - 1 && cell[c + P] == CELL_FLUID) nb |= NB_UP;
+    S.nb[c] = nb;
+}
+
+// ---------------------------------------------------------- applyPressure
+// 3-conjugate-gradients/Fluid.cpp:382-398, 4-solid-boundaries/Fluid.cpp:794-809,
+// 7-variable-density/Fluid.cpp:891-906, gathered per face: first the
+// contribution of the lower/left cell (visited first), then the cell itself.
+template <typename F>
+__global__ void apply_pressure_kernel(Scene<F> S, double dt) {
+    const int w = S.w, h = S.h, P = S.P, var = S.variant;
+    int fx = blockIdx.x * blockDim.x + threadIdx.x, fy = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint8_t *cell = S.q[0].cell;
+    const double scale = (var == 7) ? dt / S.hx : dt / (S.rho_air * S.hx);
+    if (blockIdx.z == 0) {  // u faces
+        if (fx > w || fy >= h) return;
+        size_t f = fx + (size_t)fy * P;
+        F *u = S.q[2].src + f;
+        if (var == 3 && (fx == 0 || fx == w)) {
+            *u = (F)0.0;
+            return;
+        }
+        double val = (double)*u;
+        if (fx > 0 && (var == 3 || cell[f - 1] == CELL_FLUID)) {
+            double pv = (double)S.p[f - 1];
+            val += (var == 7) ? scale * pv / (double)S.udens[f] : scale * pv;
+        }
+        if (fx < w && (var == 3 || cell[f] == CELL_FLUID)) {
+            double pv = (double)S.p[f];
+            val -= (var == 7) ? scale * pv / (double)S.udens[f] : scale * pv;
+        }
+        *u = (F)val;
+    } else {  // v faces
+        if (fx >= w || fy > h) return;
+        size_t f = fx + (size_t)fy * P;
+        F *v = S.q[3].src + f;
+        if (var == 3 && (fy == 0 || fy == h)) {
+            *v = (F)0.0;
+            return;
+        }
+        double val = (double)*v;
+        if (fy > 0 && (var == 3 || cell[f - P] == CELL_FLUID)) {
+            double pv = (double)S.p[f - P];
+            val += (var == 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
+        }
+        if (fy < h && (var == 3 || cell[f] == CELL_FLUID)) {
+            double pv = (double)S.p[f];
+            val -= (var == 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
+        }
+        *v = (F)val;
+    }
+}
+
+// ------------------------------------------------------------ extrapolate
+// extrapolate / fillSolidMask / extrapolateNormal (4-solid-boundaries/Fluid.cpp:508-587).
+// The reference solves the upwind DAG with a LIFO stack; every interior solid
+// cell is computed exactly once, from upstream neighbours that are final, so
+// a level-synchronous relaxation over the same DAG gives the same values.
+// Pass 1 (grid-wide): mask bits and the list of interior solid cells.
+template <typename F>
+__global__ void extrap_mask_kernel(Scene<F> S, unsigned qmask, int *counters) {
+    int qi = blockIdx.z;
+    if (!((qmask >> qi) & 1u)) return;
+    Quant<F> Q = S.q[qi];
+    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= Q.w || y >= Q.h) return;
+    const int P = S.P;
+    size_t idx = x + (size_t)y * P;
+    if (Q.cell[idx] == CELL_FLUID) return;
+    Q.ready[idx] = 0;
+    if (x < 1 || y < 1 || x >= Q.w - 1 || y >= Q.h - 1) return;
+    double nx = Q.nx[idx], ny = Q.ny[idx];
+    int m = 0;
+    if (nx != 0.0 && Q.cell[idx + sgn(nx)] != CELL_FLUID) m |= 1;
+    if (ny != 0.0 && Q.cell[idx + (long)sgn(ny) * P] != CELL_FLUID) m |= 2;
+    int slot = atomicAdd(&counters[qi], 1);
+    Q.list[slot] = (int)(idx * 4 + m);
+}
+
+// Pass 2: one CTA per quantity relaxes its list until nothing changes.
+template <typename F>
+__global__ void __launch_bounds__(1024) extrap_solve_kernel(Scene<F> S, unsigned qmask, const int *counters) {
+    int qi = blockIdx.x;
+    if (!((qmask >> qi) & 1u)) return;
+    Quant<F> Q = S.q[qi];
+    const long P = S.P;
+    const size_t cap = (size_t)P * (S.h + 2);
+    int *cur = Q.list, *nxt = Q.list + cap;
+    int cnt = counters[qi];
+    __shared__ int s_next;
+    const int max_rounds = Q.w + Q.h + 16;
+    for (int round = 0; round < max_rounds && cnt > 0; round++) {
+        if (threadIdx.x == 0) s_next = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            int e = cur[i];
+            long idx = e >> 2;
+            int m = e & 3;
+            double nx = Q.nx[idx], ny = Q.ny[idx];
+            long ix = idx + sgn(nx), iy = idx + (long)sgn(ny) * P;
+            bool ok = (!(m & 1) || ldv(Q.ready + ix)) && (!(m & 2) || ldv(Q.ready + iy));
+            if (ok) {
+                double sx = (double)ldv(Q.src + ix), sy = (double)ldv(Q.src + iy);
+                double val = (fabs(nx) * sx + fabs(ny) * sy) / (fabs(nx) + fabs(ny));
+                stv(Q.src + idx, (F)val);
+                __threadfence_block();
+                stv(Q.ready + idx, (uint8_t)1);
+            } else {
+                nxt[atomicAdd(&s_next, 1)] = e;
+            }
+        }
+        __syncthreads();
+        int n2 = s_next;
+        __syncthreads();
+        if (n2 == cnt) break;  // upwind cycle: the reference never solves these cells either
+        int *t = cur;
+        cur = nxt;
+        nxt = t;
+        cnt = n2;
+    }
+}
+
+// -------------------------------------------------------------- advection
+template <typename F> __device__ __forceinline__ F lerp1(F a, F b, F x) { return a * (F(1.0) - x) + b * x; }
+
+// FluidQuantity::lerp (3-conjugate-gradients/Fluid.cpp:121-133)
+template <typename F>
+__device__ __forceinline__ F q_lerp(const F *__restrict__ src, int P, int w, int h, F ox, F oy, F x, F y) {
+    x = smin(smax(x - ox, F(0.0)), F(w) - F(1.001));
+    y = smin(smax(y - oy, F(0.0)), F(h) - F(1.001));
+    int ix = (int)x, iy = (int)y;
+    x -= F(ix);
+    y -= F(iy);
+    const F *r0 = src + ix + (size_t)iy * P;
+    F x00 = __ldg(r0), x10 = __ldg(r0 + 1);
+    F x01 = __ldg(r0 + P), x11 = __ldg(r0 + P + 1);
+    return lerp1(lerp1(x00, x10, x), lerp1(x01, x11, x), y);
+}
+
+// Catmull-Rom weights of 3-conjugate-gradients/Fluid.cpp:55-69 (computed once
+// per fractional offset; the same expressions as the reference).
+template <typename F>
+struct CerpW {
+    F w0, w1, w2, w3;
+    __device__ __forceinline__ explicit CerpW(F x) {
+        F xsq = x * x;
+        F xcu = xsq * x;
+        w0 = F(0.0) - F(0.5) * x + F(1.0) * xsq - F(0.5) * xcu;
+        w1 = F(1.0) + F(0.0) * x - F(2.5) * xsq + F(1.5) * xcu;
+        w2 = F(0.0) + F(0.5) * x + F(2.0) * xsq - F(1.5) * xcu;
+        w3 = F(0.0) + F(0.0) * x - F(0.5) * xsq + F(0.5) * xcu;
+    }
+    __device__ __forceinline__ F apply(F a, F b, F c, F d) const {
+        F minV = smin(a, smin(b, smin(c, d)));
+        F maxV = smax(a, smax(b, smax(c, d)));
+        F t = a * w0 + b * w1 + c * w2 + d * w3;
+        return smin(smax(t, minV), maxV);
+    }
+};
+
+// FluidQuantity::cerp (3-conjugate-gradients/Fluid.cpp:135-152)
+template <typename F>
+__device__ __forceinline__ F q_cerp(const F *__restrict__ src, int P, int w, int h, F ox, F oy, F x, F y) {
+    x = smin(smax(x - ox, F(0.0)), F(w) - F(1.001));
+    y = smin(smax(y - oy, F(0.0)), F(h) - F(1.001));
+    int ix = (int)x, iy = (int)y;
+    x -= F(ix);
+    y -= F(iy);
+    int x0 = max(ix - 1, 0), x1 = ix, x2 = ix + 1, x3 = min(ix + 2, w - 1);
+    int y0 = max(iy - 1, 0), y1 = iy, y2 = iy + 1, y3 = min(iy + 2, h - 1);
+    CerpW<F> wx(x), wy(y);
+    const F *r0 = src + (size_t)y0 * P, *r1 = src + (size_t)y1 * P;
+    const F *r2 = src + (size_t)y2 * P, *r3 = src + (size_t)y3 * P;
+    F q0 = wx.apply(__ldg(r0 + x0), __ldg(r0 + x1), __ldg(r0 + x2), __ldg(r0 + x3));
+    F q1 = wx.apply(__ldg(r1 + x0), __ldg(r1 + x1), __ldg(r1 + x2), __ldg(r1 + x3));
+    F q2 = wx.apply(__ldg(r2 + x0), __ldg(r2 + x1), __ldg(r2 + x2), __ldg(r2 + x3));
+    F q3 = wx.apply(__ldg(r3 + x0), __ldg(r3 + x1), __ldg(r3 + x2), __ldg(r3 + x3));
+    return wy.apply(q0, q1, q2, q3);
+}
+
+// FluidQuantity::advect with rungeKutta3 and backProject
+// (3-conjugate-gradients/Fluid.cpp:71-89, 154-165; 4-solid-boundaries/Fluid.cpp:393-427).
+// blockIdx.z: 0 = density (and temperature, which shares its grid, cells and
+// backtrace), 1 = u, 2 = v.  Every quantity reads the u, v sources and writes
+// its own destination, so all of them advect in one launch.
+template <typename F>
+__global__ void advect_kernel(Scene<F> S, F dt) {
+    const int z = blockIdx.z;
+    const int qi = z == 0 ? 0 : z + 1;
+    const Quant<F> &Q = S.q[qi];
+    int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ix >= Q.w || iy >= Q.h) return;
+    const int P = S.P;
+    const size_t idx = ix + (size_t)iy * P;
+    const bool solid = S.variant >= 4;
+    if (solid && Q.cell[idx] != CELL_FLUID) return;
+    const Quant<F> &U = S.q[2], &V = S.q[3];
+    const F hx = F(S.hx);
+    const F uox = F(U.ox), uoy = F(U.oy), vox = F(V.ox), voy = F(V.oy);
+    F x = F(ix) + F(Q.ox);
+    F y = F(iy) + F(Q.oy);
+    {
+        F firstU = q_lerp(U.src, P, U.w, U.h, uox, uoy, x, y) / hx;
+        F firstV = q_lerp(V.src, P, V.w, V.h, vox, voy, x, y) / hx;
+        F midX = x - F(0.5) * dt * firstU;
+        F midY = y - F(0.5) * dt * firstV;
+        F midU = q_lerp(U.src, P, U.w, U.h, uox, uoy, midX, midY) / hx;
+        F midV = q_lerp(V.src, P, V.w, V.h, vox, voy, midX, midY) / hx;
+        F lastX = x - F(0.75) * dt * midU;
+        F lastY = y - F(0.75) * dt * midV;
+        F lastU = q_lerp(U.src, P, U.w, U.h, uox, uoy, lastX, lastY);
+        F lastV = q_lerp(V.src, P, V.w, V.h, vox, voy, lastX, lastY);
+        x -= dt * (F(2.0 / 9.0) * firstU + F(3.0 / 9.0) * midU + F(4.0 / 9.0) * lastU);
+        y -= dt * (F(2.0 / 9.0) * firstV + F(3.0 / 9.0) * midV + F(4.0 / 9.0) * lastV);
+    }
+    if (solid) {
+        int rx = min(max((int)(x - F(Q.ox)), 0), Q.w - 1);
+        int ry = min(max((int)(y - F(Q.oy)), 0), Q.h - 1);
+        size_t r = rx + (size_t)ry * P;
+        if (Q.cell[r] != CELL_FLUID) {
+            double bx = ((double)x - Q.ox) * S.hx;
+            double by = ((double)y - Q.oy) * S.hx;
+            body_closest(S.bodies[Q.body[r]], bx, by);
+            x = F(bx / S.hx + Q.ox);
+            y = F(by / S.hx + Q.oy);
+        }
+    }
+    Q.dst[idx] = q_cerp(Q.src, P, Q.w, Q.h, F(Q.ox), F(Q.oy), x, y);
+    if (z == 0 && S.nq == 4) {
+        const Quant<F> &T = S.q[1];
+        T.dst[idx] = q_cerp(T.src, P, T.w, T.h, F(T.ox), F(T.oy), x, y);
+    }
+}
+
+inline dim3 grid2(int nx, int ny, int nz, dim3 b) {
+    return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y, nz);
+}
+
+}  // namespace
+
+// -------------------------------------------------------------- launchers
+template <typename F>
+void launch_inflow(const Scene<F> &S, int qi, double x0, double y0, double x1, double y1, double val,
+                   cudaStream_t st) {
+    inflow_kernel<F><<<1, 256, 0, st>>>(S.q[qi], S.P, S.hx, x0, y0, x1, y1, val);
+}
+
+template <typename F>
+void launch_fill_solid(const Scene<F> &S, cudaStream_t st) {
+    dim3 b(32, 8);
+    if (S.variant >= 5) phi_kernel<F><<<grid2(S.w + 2, S.h + 2, S.nq, b), b, 0, st>>>(S);
+    cell_kernel<F><<<grid2(S.w + 1, S.h + 1, S.nq, b), b, 0, st>>>(S);
+}
+
+template <typename F>
+void launch_bc(const Scene<F> &S, cudaStream_t st) {
+    dim3 b(32, 8);
+    bc_kernel<F><<<grid2(S.w + 1, S.h + 1, 2, b), b, 0, st>>>(S);
+}
+
+template <typename F>
+void launch_buoyancy(const Scene<F> &S, double dt, cudaStream_t st) {
+    dim3 b(32, 8);
+    buoyancy_kernel<F><<<grid2(S.w, S.h + 1, 1, b), b, 0, st>>>(S, dt);
+}
+
+template <typename F>
+void launch_assemble(const Scene<F> &S, double dt, int what, cudaStream_t st) {
+    dim3 b(32, 8);
+    assemble_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S, dt, what);
+}
+
+template <typename F>
+void launch_heat_assemble(const Scene<F> &S, double dt, cudaStream_t st) {
+    dim3 b(32, 8);
+    heat_assemble_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S, dt);
+}
+
+template <typename F>
+void launch_apply_pressure(const Scene<F> &S, double dt, cudaStream_t st) {
+    dim3 b(32, 8);
+    apply_pressure_kernel<F><<<grid2(S.w + 1, S.h + 1, 2, b), b, 0, st>>>(S, dt);
+}
+
+template <typename F>
+void launch_extrapolate(const Scene<F> &S, unsigned qmask, cudaStream_t st) {
+    // counters live right after the status word
+    int *counters = (int *)(S.flags + 4);
+    cudaMemsetAsync(counters, 0, 4 * sizeof(int), st);
+    dim3 b(32, 8);
+    extrap_mask_kernel<F><<<grid2(S.w + 1, S.h + 1, 4, b), b, 0, st>>>(S, qmask, counters);
+    extrap_solve_kernel<F><<<4, 1024, 0, st>>>(S, qmask, counters);
+}
+
+template <typename F>
+void launch_advect(const Scene<F> &S, double dt, cudaStream_t st) {
+    dim3 b(32, 8);
+    advect_kernel<F><<<grid2(S.w + 1, S.h + 1, 3, b), b, 0, st>>>(S, (F)dt);
+}
+
+#define IFL_INST(F)                                                                                        \
+    template void launch_inflow<F>(const Scene<F> &, int, double, double, double, double, double,           \
+                                   cudaStream_t);                                                          \
+    template void launch_fill_solid<F>(const Scene<F> &, cudaStream_t);                                     \
+    template void launch_bc<F>(const Scene<F> &, cudaStream_t);                                             \
+    template void launch_buoyancy<F>(const Scene<F> &, double, cudaStream_t);                               \
+    template void launch_assemble<F>(const Scene<F> &, double, int, cudaStream_t);                          \
+    template void launch_heat_assemble<F>(const Scene<F> &, double, cudaStream_t);                          \
+    template void launch_apply_pressure<F>(const Scene<F> &, double, cudaStream_t);                         \
+    template void launch_extrapolate<F>(const Scene<F> &, unsigned, cudaStream_t);                          \
+    template void launch_advect<F>(const Scene<F> &, double, cudaStream_t);
+IFL_INST(double)
+IFL_INST(float)
+
+}  // namespace ifl

@@ -1,0 +1,495 @@
+// solver.cu - host-side FluidSolver: device arena, phase orchestration and
+// field transfer behind the C ABI (include/ifluids.h).  No kernels live here.
+//
+// update() follows FluidSolver::update of the reference step selected by the
+// variant (3-conjugate-gradients/Fluid.cpp:433-447, 4-solid-boundaries/Fluid.cpp:869-895,
+// 5-curved-boundaries/Fluid.cpp:927-953, 6-heat/Fluid.cpp:966-1006,
+// 7-variable-density/Fluid.cpp:995-1034); buildRhs/computeDensities/
+// buildPressureMatrix run as one assembly launch and buildPreconditioner +
+// project as one persistent PCG launch.
+#include "solver.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace ifl {
+
+namespace {
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct Carver {
+    size_t off = 0;
+    template <typename T>
+    T *take(char *base, size_t count) {
+        off = align_up(off, 256);
+        T *p = base ? (T *)(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+}  // namespace
+
+template <typename F>
+class SolverImpl final : public SolverBase {
+  public:
+    explicit SolverImpl(const ifl_params &prm) : SolverBase(prm) {}
+    ~SolverImpl() override { release(); }
+
+    int init() override {
+        const int w = prm_.w, h = prm_.h;
+        P_ = (int)align_up((size_t)w + 2, 32);
+        rows_ = h + 2;
+        nq_ = prm_.variant >= IFL_HEAT ? 4 : 3;
+        if (prm_.stream) {
+            stream_ = (cudaStream_t)prm_.stream;
+        } else {
+            if (check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream")) return IFL_ERR_CUDA;
+            own_stream_ = true;
+        }
+        max_blocks_ = pcg_max_blocks<F>();
+        Carver c;
+        carve(nullptr, c);
+        arena_bytes_ = c.off;
+        cudaError_t e = cudaMalloc(&arena_, arena_bytes_);
+        if (e != cudaSuccess) {
+            arena_ = nullptr;
+            cudaGetLastError();
+            err_ = "device allocation of " + std::to_string(arena_bytes_) + " bytes failed";
+            return IFL_ERR_NOMEM;
+        }
+        Carver c2;
+        carve((char *)arena_, c2);
+        if (check(cudaMemsetAsync(arena_, 0, arena_bytes_, stream_), "memset")) return IFL_ERR_CUDA;
+        // FluidQuantity ctor: volume = 1 (5-curved-boundaries and later),
+        // temperature = ambient (6-heat/Fluid.cpp:935-938).
+        if (prm_.variant >= IFL_CURVED) {
+            std::vector<double> ones((size_t)P_ * rows_, 1.0);
+            for (int q = 0; q < 4; q++)
+                if (present(q) && S_.q[q].vol)
+                    if (check(cudaMemcpy(S_.q[q].vol, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice),
+                              "init volume"))
+                        return IFL_ERR_CUDA;
+        }
+        if (prm_.variant >= IFL_HEAT) {
+            std::vector<F> tamb((size_t)P_ * rows_, (F)294.0);
+            if (check(cudaMemcpy(S_.q[1].src, tamb.data(), tamb.size() * sizeof(F), cudaMemcpyHostToDevice),
+                      "init T"))
+                return IFL_ERR_CUDA;
+        }
+        if (check(cudaStreamSynchronize(stream_), "init sync")) return IFL_ERR_CUDA;
+        return IFL_OK;
+    }
+
+    // ----------------------------------------------------------- phases
+    int add_inflow(double x, double y, double w, double h, double d, double t, double u, double v) override {
+        const double val[4] = {d, t, u, v};
+        for (int q = 0; q < 4; q++) {
+            if (!present(q)) continue;
+            launch_inflow<F>(S_, q, x, y, x + w, y + h, val[q], stream_);
+            launches_++;
+        }
+        return launch_check("inflow");
+    }
+
+    int run_phase(int ph, double dt) override {
+        const int var = prm_.variant;
+        switch (ph) {
+        case IFL_PH_FILL_SOLID:
+            if (var >= IFL_SOLID && !bodies_.empty()) {
+                if (int e = upload_bodies()) return e;
+                launch_fill_solid<F>(S_, stream_);
+                launches_ += var >= IFL_CURVED ? 2 : 1;
+            }
+            break;
+        case IFL_PH_HEAT:
+            if (var >= IFL_HEAT) return heat_solve(dt);
+            break;
+        case IFL_PH_EXTRAP_T:
+            if (var >= IFL_HEAT) extrapolate(1u << 1);
+            break;
+        case IFL_PH_BUOYANCY:
+            if (var >= IFL_HEAT) {
+                launch_buoyancy<F>(S_, dt, stream_);
+                launches_++;
+            }
+            break;
+        case IFL_PH_BC:
+            if (var >= IFL_SOLID) {
+                launch_bc<F>(S_, stream_);
+                launches_++;
+            }
+            break;
+        case IFL_PH_RHS: assemble(dt, ASM_RHS); break;
+        case IFL_PH_DENSITIES:
+            if (var == IFL_VARDENS) assemble(dt, ASM_DENS);
+            break;
+        case IFL_PH_MATRIX: assemble(dt, ASM_MATRIX); break;
+        case IFL_PH_PRECON: return pcg(PCG_FACTOR, false);
+        case IFL_PH_PROJECT: return pcg(PCG_SOLVE, false);
+        case IFL_PH_APPLY_P:
+            launch_apply_pressure<F>(S_, dt, stream_);
+            launches_++;
+            break;
+        case IFL_PH_EXTRAP_DUV:
+            if (var >= IFL_SOLID) extrapolate((1u << 0) | (1u << 2) | (1u << 3));
+            break;
+        case IFL_PH_ADVECT:
+            launch_advect<F>(S_, dt, stream_);
+            launches_++;
+            for (int q = 0; q < 4; q++)
+                if (present(q)) std::swap(S_.q[q].src, S_.q[q].dst);
+            break;
+        default: return IFL_ERR_ARG;
+        }
+        return launch_check("phase");
+    }
+
+    int update(double dt) override {
+        const int var = prm_.variant;
+        int e;
+        if (var == IFL_PLAIN) {
+            assemble(dt, ASM_RHS | ASM_MATRIX);
+            if ((e = pcg(PCG_FACTOR | PCG_SOLVE, false))) return e;
+            if ((e = run_phase(IFL_PH_APPLY_P, dt))) return e;
+            if ((e = run_phase(IFL_PH_ADVECT, dt))) return e;
+        } else {
+            if ((e = run_phase(IFL_PH_FILL_SOLID, dt))) return e;
+            if (var >= IFL_HEAT) {
+                if ((e = heat_solve(dt))) return e;
+                extrapolate(1u << 1);
+                if ((e = run_phase(IFL_PH_BUOYANCY, dt))) return e;
+            }
+            if ((e = run_phase(IFL_PH_BC, dt))) return e;
+            assemble(dt, ASM_RHS | ASM_MATRIX | (var == IFL_VARDENS ? ASM_DENS : 0));
+            if ((e = pcg(PCG_FACTOR | PCG_SOLVE, false))) return e;
+            if ((e = run_phase(IFL_PH_APPLY_P, dt))) return e;
+            extrapolate((1u << 0) | (1u << 2) | (1u << 3));
+            if ((e = run_phase(IFL_PH_BC, dt))) return e;
+            if ((e = run_phase(IFL_PH_ADVECT, dt))) return e;
+        }
+        steps_++;
+        return launch_check("update");
+    }
+
+    // ------------------------------------------------------ field access
+    int field_info(int field, void **ptr, int *elem, int *w, int *h) const override {
+        const int W = prm_.w, H = prm_.h;
+        *w = W;
+        *h = H;
+        const int fe = sizeof(F) == 8 ? IFL_DT_F64 : IFL_DT_F32;
+        if (field >= IFL_F_R && field <= IFL_F_VDENS) {
+            *elem = fe;
+            switch (field) {
+            case IFL_F_R: *ptr = S_.r; return 0;
+            case IFL_F_P: *ptr = S_.p; return 0;
+            case IFL_F_Z: *ptr = S_.z; return 0;
+            case IFL_F_S: *ptr = S_.sa; return 0;
+            case IFL_F_PRECON: *ptr = S_.pc; *elem = IFL_DT_F64; return 0;
+            case IFL_F_ADIAG: *ptr = S_.adiag; return 0;
+            case IFL_F_APLUSX: *ptr = S_.ax; return 0;
+            case IFL_F_APLUSY: *ptr = S_.ay; return 0;
+            case IFL_F_UDENS: *ptr = S_.udens; *w = W + 1; return 0;
+            case IFL_F_VDENS: *ptr = S_.vdens; *h = H + 1; return 0;
+            }
+        }
+        int q = field >> 8, a = field & 0xff;
+        if (q < 0 || q > 3 || !present(q)) return IFL_ERR_ARG;
+        const Quant<F> &Q = S_.q[q];
+        *w = Q.w;
+        *h = Q.h;
+        switch (a) {
+        case IFL_A_SRC: *ptr = Q.src; *elem = fe; return 0;
+        case IFL_A_DST: *ptr = Q.dst; *elem = fe; return 0;
+        case IFL_A_PHI: *ptr = Q.phi; *elem = IFL_DT_F64; *w = Q.w + 1; *h = Q.h + 1; break;
+        case IFL_A_VOLUME: *ptr = Q.vol; *elem = IFL_DT_F64; break;
+        case IFL_A_NORMALX: *ptr = Q.nx; *elem = IFL_DT_F64; break;
+        case IFL_A_NORMALY: *ptr = Q.ny; *elem = IFL_DT_F64; break;
+        case IFL_A_CELL: *ptr = Q.cell; *elem = IFL_DT_U8; break;
+        case IFL_A_BODY: *ptr = Q.body; *elem = IFL_DT_U8; break;
+        default: return IFL_ERR_ARG;
+        }
+        return *ptr ? 0 : IFL_ERR_ARG;
+    }
+
+    int flip(int q) override {
+        if (q < 0 || q > 3 || !present(q)) return IFL_ERR_ARG;
+        std::swap(S_.q[q].src, S_.q[q].dst);
+        return IFL_OK;
+    }
+
+    int read_pcg(ifl_step_stats *st) override {
+        PcgOut o[2];
+        unsigned fl = 0;
+        if (check(cudaMemcpyAsync(o, scratch_.out, sizeof o, cudaMemcpyDeviceToHost, stream_), "stats") ||
+            check(cudaMemcpyAsync(&fl, S_.flags, 4, cudaMemcpyDeviceToHost, stream_), "flags") ||
+            check(cudaStreamSynchronize(stream_), "stats sync"))
+            return IFL_ERR_CUDA;
+        st->pressure = {o[0].iterations, o[0].status, o[0].max_error};
+        st->heat = {o[1].iterations, o[1].status, o[1].max_error};
+        st->device_flags = fl;
+        st->steps = steps_;
+        return IFL_OK;
+    }
+
+    size_t pitch() const override { return (size_t)P_; }
+    size_t device_bytes() const override { return arena_bytes_; }
+
+  private:
+    bool present(int q) const { return q != 1 || nq_ == 4; }
+
+    void carve(char *base, Carver &c) {
+        const size_t N = (size_t)P_ * rows_;
+        const bool geo = prm_.variant >= IFL_SOLID;
+        S_.variant = prm_.variant;
+        S_.w = prm_.w;
+        S_.h = prm_.h;
+        S_.P = P_;
+        S_.nq = nq_;
+        S_.hx = 1.0 / std::min(prm_.w, prm_.h);
+        S_.rho_air = prm_.density_air;
+        S_.rho_soot = prm_.density_soot;
+        S_.diffusion = prm_.diffusion;
+        S_.t_amb = 294.0;  // 7-variable-density/Fluid.cpp:950
+        S_.g = 9.81;
+        const double ox[4] = {0.5, 0.5, 0.0, 0.5}, oy[4] = {0.5, 0.5, 0.5, 0.0};
+        const int qw[4] = {prm_.w, prm_.w, prm_.w + 1, prm_.w};
+        const int qh[4] = {prm_.h, prm_.h, prm_.h, prm_.h + 1};
+        for (int q = 0; q < 4; q++) {
+            Quant<F> &Q = S_.q[q];
+            Q = Quant<F>{};
+            Q.w = qw[q];
+            Q.h = qh[q];
+            Q.ox = ox[q];
+            Q.oy = oy[q];
+            if (!present(q)) continue;
+            Q.src = c.take<F>(base, N);
+            Q.dst = c.take<F>(base, N);
+            Q.cell = c.take<uint8_t>(base, N);
+            if (geo) {
+                Q.phi = prm_.variant >= IFL_CURVED ? c.take<double>(base, N) : nullptr;
+                Q.vol = prm_.variant >= IFL_CURVED ? c.take<double>(base, N) : nullptr;
+                Q.nx = c.take<double>(base, N);
+                Q.ny = c.take<double>(base, N);
+                Q.body = c.take<uint8_t>(base, N);
+                Q.ready = c.take<uint8_t>(base, N);
+                Q.list = c.take<int>(base, 2 * N);
+            }
+        }
+        S_.r = c.take<F>(base, N);
+        S_.p = c.take<F>(base, N);
+        S_.z = c.take<F>(base, N);
+        S_.sa = c.take<F>(base, N);
+        S_.sb = c.take<F>(base, N);
+        S_.as = c.take<F>(base, N);
+        S_.adiag = c.take<F>(base, N);
+        S_.ax = c.take<F>(base, N);
+        S_.ay = c.take<F>(base, N);
+        S_.lx = c.take<F>(base, N);
+        S_.ly = c.take<F>(base, N);
+        S_.pcf = c.take<F>(base, N);
+        S_.pc = c.take<double>(base, N);
+        S_.nb = c.take<uint8_t>(base, N);
+        if (prm_.variant == IFL_VARDENS) {
+            S_.udens = c.take<F>(base, N);
+            S_.vdens = c.take<F>(base, N);
+        } else {
+            S_.udens = S_.vdens = nullptr;
+        }
+        d_bodies_ = c.take<DevBody>(base, 256);
+        S_.bodies = d_bodies_;
+        S_.nbodies = 0;
+        S_.flags = c.take<unsigned>(base, 8);
+        scratch_.max_blocks = max_blocks_;
+        scratch_.partials = c.take<double>(base, 4 * (size_t)std::max(max_blocks_, 1));
+        scratch_.barrier = c.take<unsigned>(base, 2);
+        scratch_.progress = c.take<unsigned>(base, (size_t)(prm_.h + 31) / 32 + 1);
+        scratch_.out = c.take<PcgOut>(base, 2);
+    }
+
+    int upload_bodies() {
+        if (!bodies_dirty_) return IFL_OK;
+        std::vector<DevBody> db(bodies_.size());
+        for (size_t i = 0; i < bodies_.size(); i++) {
+            const ifl_body &b = bodies_[i];
+            DevBody &d = db[i];
+            d.type = b.type;
+            d.pad_ = 0;
+            d.px = b.pos_x;
+            d.py = b.pos_y;
+            d.sx = b.scale_x;
+            d.sy = b.type == 0 ? b.scale_y : b.scale_x;  // SolidSphere(x, y, s, ...) sets both scales to s
+            d.vx = b.vel_x;
+            d.vy = b.vel_y;
+            d.vth = b.vel_theta;
+            d.cpos = std::cos(b.theta);
+            d.spos = std::sin(b.theta);
+            d.cneg = std::cos(-b.theta);
+            d.sneg = std::sin(-b.theta);
+        }
+        if (check(cudaMemcpyAsync(d_bodies_, db.data(), db.size() * sizeof(DevBody), cudaMemcpyHostToDevice,
+                                  stream_),
+                  "bodies"))
+            return IFL_ERR_CUDA;
+        // pageable source: make sure the copy has been taken before db dies
+        if (check(cudaStreamSynchronize(stream_), "bodies sync")) return IFL_ERR_CUDA;
+        S_.nbodies = (int)bodies_.size();
+        bodies_dirty_ = false;
+        return IFL_OK;
+    }
+
+    void assemble(double dt, int what) {
+        launch_assemble<F>(S_, dt, what, stream_);
+        launches_++;
+    }
+
+    void extrapolate(unsigned qmask) {
+        if (prm_.variant < IFL_SOLID) return;
+        launch_extrapolate<F>(S_, qmask, stream_);
+        launches_ += 2;
+    }
+
+    int pcg(int mode, bool heat) {
+        PcgConfig cfg;
+        cfg.mode = mode;
+        cfg.limit = heat ? prm_.max_iter_heat : prm_.max_iter_pressure;
+        cfg.pinned = pinned_;
+        cfg.heat = heat ? 1 : 0;
+        int G = 0;
+        if (check(launch_pcg<F>(S_, scratch_, cfg, stream_, &G), "pcg launch")) return IFL_ERR_CUDA;
+        launches_++;
+        return IFL_OK;
+    }
+
+    // r = T; heat matrix; MIC(0); PCG; T = p  (7-variable-density/Fluid.cpp:1001-1005)
+    int heat_solve(double dt) {
+        launch_heat_assemble<F>(S_, dt, stream_);
+        launches_++;
+        if (int e = pcg(PCG_FACTOR | PCG_SOLVE, true)) return e;
+        if (check(cudaMemcpy2DAsync(S_.q[1].src, (size_t)P_ * sizeof(F), S_.p, (size_t)P_ * sizeof(F),
+                                    (size_t)prm_.w * sizeof(F), prm_.h, cudaMemcpyDeviceToDevice, stream_),
+                  "T = p"))
+            return IFL_ERR_CUDA;
+        return IFL_OK;
+    }
+
+    int launch_check(const char *what) {
+        return check(cudaGetLastError(), what) ? IFL_ERR_CUDA : IFL_OK;
+    }
+
+    void release() {
+        if (arena_) cudaFree(arena_);
+        arena_ = nullptr;
+        if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+        stream_ = nullptr;
+    }
+
+    Scene<F> S_{};
+    PcgScratch scratch_{};
+    DevBody *d_bodies_ = nullptr;
+    void *arena_ = nullptr;
+    size_t arena_bytes_ = 0;
+    int P_ = 0, rows_ = 0, nq_ = 3, max_blocks_ = 1;
+};
+
+// ------------------------------------------------------------ SolverBase
+bool SolverBase::check(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return false;
+    err_ = std::string(what) + ": " + cudaGetErrorString(e);
+    return true;
+}
+
+int SolverBase::set_bodies(const ifl_body *b, int n) {
+    if (n < 0 || n > 256 || (n > 0 && !b)) return IFL_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (b[i].type != 0 && b[i].type != 1) return IFL_ERR_ARG;
+    bodies_.assign(b, b + n);
+    bodies_dirty_ = true;
+    return IFL_OK;
+}
+
+// SolidBody::update (4-solid-boundaries/Fluid.cpp:140-148)
+int SolverBase::advance_bodies(double dt) {
+    for (ifl_body &b : bodies_) {
+        b.pos_x += b.vel_x * dt;
+        b.pos_y += b.vel_y * dt;
+        b.theta += b.vel_theta * dt;
+    }
+    bodies_dirty_ = true;
+    return IFL_OK;
+}
+
+int SolverBase::read_field(int field, void *host, size_t bytes, int dtype) {
+    void *ptr;
+    int elem, w, h;
+    if (int e = field_info(field, &ptr, &elem, &w, &h)) return e;
+    const size_t n = (size_t)w * h;
+    const size_t out_es = dtype == IFL_DT_F64 ? 8 : dtype == IFL_DT_F32 ? 4 : dtype == IFL_DT_U8 ? 1 : 0;
+    if (!out_es || !host || bytes < n * out_es) return IFL_ERR_ARG;
+    if ((elem == IFL_DT_U8) != (dtype == IFL_DT_U8)) return IFL_ERR_ARG;
+    const size_t es = elem == IFL_DT_F64 ? 8 : elem == IFL_DT_F32 ? 4 : 1;
+    std::vector<char> tmp;
+    void *dst = host;
+    if (elem != dtype) {
+        tmp.resize(n * es);
+        dst = tmp.data();
+    }
+    if (check(cudaMemcpy2DAsync(dst, w * es, ptr, pitch() * es, w * es, h, cudaMemcpyDeviceToHost, stream()),
+              "read field") ||
+        check(cudaStreamSynchronize(stream()), "read sync"))
+        return IFL_ERR_CUDA;
+    if (elem != dtype) {
+        if (elem == IFL_DT_F64) {
+            const double *s = (const double *)dst;
+            float *o = (float *)host;
+            for (size_t i = 0; i < n; i++) o[i] = (float)s[i];
+        } else {
+            const float *s = (const float *)dst;
+            double *o = (double *)host;
+            for (size_t i = 0; i < n; i++) o[i] = (double)s[i];
+        }
+    }
+    return IFL_OK;
+}
+
+int SolverBase::write_field(int field, const void *host, size_t bytes, int dtype) {
+    void *ptr;
+    int elem, w, h;
+    if (int e = field_info(field, &ptr, &elem, &w, &h)) return e;
+    const size_t n = (size_t)w * h;
+    const size_t in_es = dtype == IFL_DT_F64 ? 8 : dtype == IFL_DT_F32 ? 4 : dtype == IFL_DT_U8 ? 1 : 0;
+    if (!in_es || !host || bytes < n * in_es) return IFL_ERR_ARG;
+    if ((elem == IFL_DT_U8) != (dtype == IFL_DT_U8)) return IFL_ERR_ARG;
+    const size_t es = elem == IFL_DT_F64 ? 8 : elem == IFL_DT_F32 ? 4 : 1;
+    std::vector<char> tmp;
+    const void *src = host;
+    if (elem != dtype) {
+        tmp.resize(n * es);
+        if (elem == IFL_DT_F64) {
+            const float *s = (const float *)host;
+            double *o = (double *)tmp.data();
+            for (size_t i = 0; i < n; i++) o[i] = (double)s[i];
+        } else {
+            const double *s = (const double *)host;
+            float *o = (float *)tmp.data();
+            for (size_t i = 0; i < n; i++) o[i] = (float)s[i];
+        }
+        src = tmp.data();
+    }
+    if (check(cudaMemcpy2DAsync(ptr, pitch() * es, src, w * es, w * es, h, cudaMemcpyHostToDevice, stream()),
+              "write field") ||
+        check(cudaStreamSynchronize(stream()), "write sync"))
+        return IFL_ERR_CUDA;
+    return IFL_OK;
+}
+
+std::unique_ptr<SolverBase> make_solver(const ifl_params &p) {
+    if (p.precision == IFL_FP32) return std::unique_ptr<SolverBase>(new SolverImpl<float>(p));
+    return std::unique_ptr<SolverBase>(new SolverImpl<double>(p));
+}
+
+}  // namespace ifl

@@ -1,0 +1,324 @@
+"""Python mirror of the reference FluidSolver surface over the GB300 C ABI.
+
+The classes here follow the reference's own interface (tunabrain/
+incremental-fluids): ``FluidSolver(w, h, density)`` (step 3),
+``FluidSolver(w, h, density, bodies)`` (steps 4/5),
+``FluidSolver(w, h, rhoAir, rhoSoot, diffusion, bodies)`` (steps 6/7),
+``addInflow``, ``update``, ``ambientT``, and ``SolidBox`` / ``SolidSphere``
+bodies with ``update(dt)``.  Field readback (``read_field``) replaces the
+reference's PNG output.  Every call goes through ``libifluids.so``
+(``include/ifluids.h``); there is no CPU fallback: if the library is missing
+or no GPU is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Iterable, List, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libifluids.so")
+
+# include/ifluids.h constants
+OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5
+PLAIN, SOLID, CURVED, HEAT, VARDENS = 3, 4, 5, 6, 7
+FP64, FP32 = 0, 1
+DT_F64, DT_F32, DT_U8 = 0, 1, 2
+Q_D, Q_T, Q_U, Q_V = 0, 1, 2, 3
+A_SRC, A_DST, A_PHI, A_VOLUME, A_NORMALX, A_NORMALY, A_CELL, A_BODY = 0, 1, 2, 3, 4, 5, 8, 9
+F_R, F_P, F_Z, F_S, F_PRECON, F_ADIAG, F_APLUSX, F_APLUSY, F_UDENS, F_VDENS = range(16, 26)
+(PH_FILL_SOLID, PH_HEAT, PH_EXTRAP_T, PH_BUOYANCY, PH_BC, PH_RHS, PH_DENSITIES, PH_MATRIX,
+ PH_PRECON, PH_PROJECT, PH_APPLY_P, PH_EXTRAP_DUV, PH_ADVECT) = range(13)
+PCG_CONVERGED, PCG_INITIAL, PCG_CAP = 0, 1, 2
+
+EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", "ifl_get_bodies",
+           "ifl_advance_bodies", "ifl_add_inflow", "ifl_update", "ifl_run_phase", "ifl_ambient_t",
+           "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_flip", "ifl_get_stats",
+           "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
+           "ifl_last_error", "ifl_version")
+
+
+def field_id(quantity: int, array: int) -> int:
+    return (quantity << 8) | array
+
+
+_NAMED = {"d": field_id(Q_D, A_SRC), "t": field_id(Q_T, A_SRC), "u": field_id(Q_U, A_SRC),
+          "v": field_id(Q_V, A_SRC), "p": F_P, "r": F_R, "z": F_Z, "s": F_S, "precon": F_PRECON,
+          "adiag": F_ADIAG, "aplusx": F_APLUSX, "aplusy": F_APLUSY, "udens": F_UDENS, "vdens": F_VDENS}
+
+
+class Params(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("w", C.c_int32), ("h", C.c_int32), ("precision", C.c_int32),
+                ("density_air", C.c_double), ("density_soot", C.c_double), ("diffusion", C.c_double),
+                ("max_iter_pressure", C.c_int32), ("max_iter_heat", C.c_int32), ("stream", C.c_void_p)]
+
+
+class _CBody(C.Structure):
+    _fields_ = [("type", C.c_int32), ("pad_", C.c_int32)] + [
+        (n, C.c_double) for n in ("pos_x", "pos_y", "scale_x", "scale_y", "theta", "vel_x", "vel_y",
+                                  "vel_theta")]
+
+
+class PcgStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("max_error", C.c_double)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("pressure", PcgStats), ("heat", PcgStats), ("device_flags", C.c_uint32),
+                ("steps", C.c_uint32)]
+
+
+class IflError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ifluids error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libifluids.so and declare its C signatures (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"libifluids.so not built ({path}); run incremental-fluids_gb300/build.py")
+    L = C.CDLL(path)
+    vp, i, d, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    L.ifl_default_params.argtypes = [C.POINTER(Params), i, i, i]
+    L.ifl_default_params.restype = None
+    L.ifl_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.ifl_destroy.argtypes = [vp]
+    L.ifl_set_bodies.argtypes = [vp, C.POINTER(_CBody), i]
+    L.ifl_get_bodies.argtypes = [vp, C.POINTER(_CBody), i, C.POINTER(i)]
+    L.ifl_advance_bodies.argtypes = [vp, d]
+    L.ifl_add_inflow.argtypes = [vp] + [d] * 8
+    L.ifl_update.argtypes = [vp, d]
+    L.ifl_run_phase.argtypes = [vp, i, d]
+    L.ifl_ambient_t.argtypes = [vp]
+    L.ifl_ambient_t.restype = d
+    L.ifl_field_shape.argtypes = [vp, i, C.POINTER(i), C.POINTER(i)]
+    L.ifl_read_field.argtypes = [vp, i, vp, sz, i]
+    L.ifl_write_field.argtypes = [vp, i, vp, sz, i]
+    L.ifl_flip.argtypes = [vp, i]
+    L.ifl_get_stats.argtypes = [vp, C.POINTER(StepStats)]
+    L.ifl_set_pinned_iterations.argtypes = [vp, i]
+    L.ifl_synchronize.argtypes = [vp]
+    L.ifl_stream.argtypes = [vp]
+    L.ifl_stream.restype = vp
+    L.ifl_launch_count.argtypes = [vp]
+    L.ifl_launch_count.restype = C.c_int64
+    L.ifl_last_error.argtypes = [vp]
+    L.ifl_last_error.restype = C.c_char_p
+    L.ifl_version.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+class SolidBody:
+    """Rigid body of the reference (4-solid-boundaries/Fluid.cpp:79-149)."""
+
+    type = 0
+
+    def __init__(self, pos_x, pos_y, scale_x, scale_y, theta, vel_x, vel_y, vel_theta):
+        self.pos_x, self.pos_y = float(pos_x), float(pos_y)
+        self.scale_x, self.scale_y = float(scale_x), float(scale_y)
+        self.theta = float(theta)
+        self.vel_x, self.vel_y, self.vel_theta = float(vel_x), float(vel_y), float(vel_theta)
+
+    def update(self, timestep: float):
+        """SolidBody::update: explicit Euler step of position and angle."""
+        self.pos_x += self.vel_x * timestep
+        self.pos_y += self.vel_y * timestep
+        self.theta += self.vel_theta * timestep
+
+    def as_tuple(self):
+        return (self.type, self.pos_x, self.pos_y, self.scale_x, self.scale_y, self.theta,
+                self.vel_x, self.vel_y, self.vel_theta)
+
+
+class SolidBox(SolidBody):
+    """SolidBox(x, y, sx, sy, t, vx, vy, vt): full side lengths sx, sy."""
+    type = 0
+
+
+class SolidSphere(SolidBody):
+    """SolidSphere(x, y, s, t, vx, vy, vt): diameter s."""
+    type = 1
+
+    def __init__(self, pos_x, pos_y, scale, theta, vel_x, vel_y, vel_theta):
+        super().__init__(pos_x, pos_y, scale, scale, theta, vel_x, vel_y, vel_theta)
+
+
+def _body_tuple(b):
+    return b.as_tuple() if isinstance(b, SolidBody) else tuple(b)
+
+
+class FluidSolver:
+    """Device-resident FluidSolver.
+
+    Positional forms follow the reference constructors::
+
+        FluidSolver(w, h, density)                          # 3-conjugate-gradients
+        FluidSolver(w, h, density, bodies)                  # 4-solid-boundaries (variant=5: curved)
+        FluidSolver(w, h, rhoAir, rhoSoot, diffusion, bodies)  # 7-variable-density (variant=6: heat)
+
+    Bodies are held by reference as in the reference: before every update()
+    their current state is sent to the device, so callers move them with
+    ``SolidBody.update(dt)`` between steps exactly as the reference's main()
+    does.  ``precision`` selects the FP64 drop-in or the FP32 form.
+    """
+
+    def __init__(self, w: int, h: int, *args, variant: Optional[int] = None, precision: int = FP64,
+                 max_iter_pressure: Optional[int] = None, max_iter_heat: Optional[int] = None,
+                 stream: Optional[int] = None):
+        self._L = load_library()
+        bodies: Sequence = ()
+        soot = diffusion = None
+        if len(args) == 1:
+            density = args[0]
+            v = PLAIN
+        elif len(args) == 2:
+            density, bodies = args
+            v = SOLID
+        elif len(args) == 4:
+            density, soot, diffusion, bodies = args
+            v = VARDENS
+        else:
+            raise TypeError("FluidSolver(w, h, density[, bodies]) or (w, h, rhoAir, rhoSoot, diffusion, bodies)")
+        if variant is not None:
+            v = variant
+        p = Params()
+        self._L.ifl_default_params(C.byref(p), v, int(w), int(h))
+        p.precision = precision
+        p.density_air = float(density)
+        if soot is not None:
+            p.density_soot = float(soot)
+        if diffusion is not None:
+            p.diffusion = float(diffusion)
+        if max_iter_pressure is not None:
+            p.max_iter_pressure = int(max_iter_pressure)
+        if max_iter_heat is not None:
+            p.max_iter_heat = int(max_iter_heat)
+        p.stream = stream
+        h_ = C.c_void_p()
+        rc = self._L.ifl_create(C.byref(p), C.byref(h_))
+        if rc != OK:
+            raise IflError(rc, "ifl_create failed (is a GPU present and the size valid?)")
+        self._h = h_
+        self.variant, self.w, self.h, self.precision = v, int(w), int(h), precision
+        self._bodies: List = list(bodies)
+        self._uploaded = None
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ifl_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            msg = self._L.ifl_last_error(self._h)
+            raise IflError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- bodies
+    @property
+    def bodies(self):
+        return self._bodies
+
+    def set_bodies(self, bodies: Iterable):
+        self._bodies = list(bodies)
+        self._uploaded = None
+
+    def _sync_bodies(self):
+        if self.variant < SOLID:
+            return
+        cur = tuple(_body_tuple(b) for b in self._bodies)
+        if cur == self._uploaded:
+            return
+        arr = (_CBody * max(1, len(cur)))()
+        for k, b in enumerate(cur):
+            arr[k].type = int(b[0])
+            (arr[k].pos_x, arr[k].pos_y, arr[k].scale_x, arr[k].scale_y, arr[k].theta, arr[k].vel_x,
+             arr[k].vel_y, arr[k].vel_theta) = [float(x) for x in b[1:9]]
+        self._check(self._L.ifl_set_bodies(self._h, arr, len(cur)), "set_bodies")
+        self._uploaded = cur
+
+    # -- reference surface
+    def addInflow(self, x, y, w, h, d, *rest):
+        """addInflow(x, y, w, h, d, u, v) (steps 3-5) or (x, y, w, h, d, t, u, v) (steps 6-7)."""
+        if len(rest) == 2:
+            t, (u, v) = 0.0, rest
+        elif len(rest) == 3:
+            t, u, v = rest
+        else:
+            raise TypeError("addInflow(x, y, w, h, d, [t,] u, v)")
+        self._check(self._L.ifl_add_inflow(self._h, x, y, w, h, d, t, u, v), "addInflow")
+
+    def update(self, timestep: float):
+        self._sync_bodies()
+        self._check(self._L.ifl_update(self._h, timestep), "update")
+
+    def ambientT(self) -> float:
+        return float(self._L.ifl_ambient_t(self._h))
+
+    # -- additions: readback, phases, statistics
+    def run_phase(self, phase: int, timestep: float):
+        self._sync_bodies()
+        self._check(self._L.ifl_run_phase(self._h, phase, timestep), "run_phase")
+
+    def shape(self, field: int):
+        w, h = C.c_int(), C.c_int()
+        self._check(self._L.ifl_field_shape(self._h, field, C.byref(w), C.byref(h)), "field_shape")
+        return h.value, w.value
+
+    def read_field(self, field, dtype=np.float64) -> np.ndarray:
+        fid = _NAMED[field] if isinstance(field, str) else int(field)
+        h, w = self.shape(fid)
+        arr = np.empty((h, w), dtype=dtype)
+        code = {np.dtype(np.float64): DT_F64, np.dtype(np.float32): DT_F32, np.dtype(np.uint8): DT_U8}[
+            np.dtype(dtype)]
+        self._check(self._L.ifl_read_field(self._h, fid, arr.ctypes.data, arr.nbytes, code), "read_field")
+        return arr
+
+    def write_field(self, field, values: np.ndarray):
+        fid = _NAMED[field] if isinstance(field, str) else int(field)
+        h, w = self.shape(fid)
+        arr = np.ascontiguousarray(values)
+        if arr.shape != (h, w):
+            raise ValueError(f"field {fid}: expected shape {(h, w)}, got {arr.shape}")
+        code = {np.dtype(np.float64): DT_F64, np.dtype(np.float32): DT_F32, np.dtype(np.uint8): DT_U8}[
+            arr.dtype]
+        self._check(self._L.ifl_write_field(self._h, fid, arr.ctypes.data, arr.nbytes, code), "write_field")
+
+    def flip(self, quantity: int):
+        self._check(self._L.ifl_flip(self._h, quantity), "flip")
+
+    def set_pinned_iterations(self, k: int):
+        self._check(self._L.ifl_set_pinned_iterations(self._h, k), "pinned")
+
+    def stats(self):
+        st = StepStats()
+        self._check(self._L.ifl_get_stats(self._h, C.byref(st)), "stats")
+        return ((st.pressure.iterations, st.pressure.status, st.pressure.max_error),
+                (st.heat.iterations, st.heat.status, st.heat.max_error), st.device_flags)
+
+    def synchronize(self):
+        self._check(self._L.ifl_synchronize(self._h), "synchronize")
+
+    @property
+    def stream(self) -> int:
+        return self._L.ifl_stream(self._h) or 0
+
+    def launch_count(self) -> int:
+        """Kernel launches this solver has issued since it was created."""
+        return int(self._L.ifl_launch_count(self._h))

@@ -1,0 +1,269 @@
+"""ctypes front-end of the CPU oracle (test infrastructure only).
+
+Two back-ends with one interface:
+
+* ``OracleSolver`` drives ``oracle/liboracle.so``, the plain-C restatement of
+  the reference solver (tutorial steps 3-7).  It builds on any host and is the
+  parity checker the GPU tests use, and the CPU baseline bench.py times.
+* ``RefSolver`` drives ``oracle/_ref/libref<step>.so``: the reference's own
+  ``Fluid.cpp`` compiled unmodified (see ``oracle/ref_shim.cpp``).  It exists
+  only where the reference checkout was available at build time and is used to
+  pin ``OracleSolver`` bit-for-bit.
+
+Only tests, ``__graft_entry__.smoke`` and bench.py's CPU-baseline leg may use
+this module.  Bodies are plain tuples
+``(type, pos_x, pos_y, scale_x, scale_y, theta, vel_x, vel_y, vel_theta)``
+with type 0 = box (full side lengths) and 1 = sphere (diameter in scale_x).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+PLAIN, SOLID, CURVED, HEAT, VARDENS = 3, 4, 5, 6, 7
+QD, QT, QU, QV = 0, 1, 2, 3
+A_SRC, A_DST, A_PHI, A_VOLUME, A_NORMALX, A_NORMALY = 0, 1, 2, 3, 4, 5
+A_R, A_P, A_Z, A_S, A_PRECON, A_ADIAG, A_APLUSX, A_APLUSY, A_UDENS, A_VDENS = range(16, 26)
+B_CELL, B_BODY, B_MASK = 0, 1, 2
+(PH_FILL_SOLID, PH_HEAT, PH_EXTRAP_T, PH_BUOYANCY, PH_BC, PH_RHS, PH_DENSITIES,
+ PH_MATRIX, PH_PRECON, PH_PROJECT, PH_APPLY_P, PH_EXTRAP_DUV, PH_ADVECT) = range(13)
+PCG_CONVERGED, PCG_INITIAL, PCG_CAP = 0, 1, 2
+
+
+class _Body(C.Structure):
+    _fields_ = [("type", C.c_int32), ("pad_", C.c_int32)] + [
+        (n, C.c_double) for n in ("pos_x", "pos_y", "scale_x", "scale_y", "theta",
+                                  "vel_x", "vel_y", "vel_theta")]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("status", C.c_int32), ("max_error", C.c_double)]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the committed Makefile (gcc, -ffp-contract=off)."""
+    if force or not os.path.exists(LIB_PATH) or (
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "ifl_oracle.c"))):
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "all", "liboracle.so"],
+                       check=True)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def _oracle_lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, i, d = C.c_void_p, C.c_int, C.c_double
+        L.ifo_create.restype = vp
+        L.ifo_create.argtypes = [i, i, i, d, d, d]
+        L.ifo_destroy.argtypes = [vp]
+        L.ifo_set_bodies.argtypes = [vp, C.POINTER(_Body), i]
+        L.ifo_get_bodies.argtypes = [vp, C.POINTER(_Body)]
+        L.ifo_advance_bodies.argtypes = [vp, d]
+        L.ifo_add_inflow.argtypes = [vp] + [d] * 8
+        L.ifo_update.argtypes = [vp, d]
+        L.ifo_phase.argtypes = [vp, i, d]
+        L.ifo_set_pinned_iterations.argtypes = [vp, i]
+        L.ifo_get_stats.argtypes = [vp, C.POINTER(_Stats), C.POINTER(_Stats)]
+        L.ifo_array.restype = C.POINTER(C.c_double)
+        L.ifo_array.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
+        L.ifo_bytes.restype = C.POINTER(C.c_uint8)
+        L.ifo_bytes.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
+        L.ifo_flip.argtypes = [vp, i]
+        L.ifo_occupancy.argtypes = [d, d, d, d]
+        L.ifo_occupancy.restype = d
+        L.ifo_cerp.argtypes = [d, d, d, d, d]
+        L.ifo_cerp.restype = d
+        _lib = L
+    return _lib
+
+
+def _view(ptr, w, h, dtype):
+    if not ptr:
+        return None
+    n = w * h
+    ctype = C.c_double if dtype == np.float64 else C.c_uint8
+    arr = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(n,))
+    return arr.reshape(h, w)
+
+
+class OracleSolver:
+    """The C restatement of FluidSolver (steps 3-7), FP64, zero-initialised."""
+
+    def __init__(self, variant: int, w: int, h: int, density: float = 0.1,
+                 density_soot: float = 1.0, diffusion: float = 0.01):
+        self.L = _oracle_lib()
+        self.variant, self.w, self.h = variant, w, h
+        self.p = self.L.ifo_create(variant, w, h, density, density_soot, diffusion)
+        if not self.p:
+            raise ValueError("oracle: bad solver parameters")
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            self.L.ifo_destroy(self.p)
+            self.p = None
+
+    def set_bodies(self, bodies):
+        arr = (_Body * max(1, len(bodies)))()
+        for k, b in enumerate(bodies):
+            arr[k].type = int(b[0])
+            (arr[k].pos_x, arr[k].pos_y, arr[k].scale_x, arr[k].scale_y, arr[k].theta,
+             arr[k].vel_x, arr[k].vel_y, arr[k].vel_theta) = [float(x) for x in b[1:9]]
+        if self.L.ifo_set_bodies(self.p, arr, len(bodies)) != 0:
+            raise ValueError("oracle: at most 256 bodies")
+        self._nb = len(bodies)
+
+    def bodies(self):
+        n = getattr(self, "_nb", 0)
+        arr = (_Body * max(1, n))()
+        self.L.ifo_get_bodies(self.p, arr)
+        return [(b.type, b.pos_x, b.pos_y, b.scale_x, b.scale_y, b.theta, b.vel_x, b.vel_y,
+                 b.vel_theta) for b in arr[:n]]
+
+    def advance_bodies(self, dt):
+        self.L.ifo_advance_bodies(self.p, dt)
+
+    def add_inflow(self, x, y, w, h, d, t, u, v):
+        self.L.ifo_add_inflow(self.p, x, y, w, h, d, t, u, v)
+
+    def update(self, dt):
+        self.L.ifo_update(self.p, dt)
+
+    def phase(self, ph, dt):
+        self.L.ifo_phase(self.p, ph, dt)
+
+    def flip(self, q):
+        self.L.ifo_flip(self.p, q)
+
+    def set_pinned_iterations(self, k: int):
+        self.L.ifo_set_pinned_iterations(self.p, k)
+
+    def stats(self):
+        a, b = _Stats(), _Stats()
+        self.L.ifo_get_stats(self.p, C.byref(a), C.byref(b))
+        return ((a.iterations, a.status, a.max_error), (b.iterations, b.status, b.max_error))
+
+    def array(self, q: int, which: int):
+        w, h = C.c_int(), C.c_int()
+        return _view(self.L.ifo_array(self.p, q, which, C.byref(w), C.byref(h)),
+                     w.value, h.value, np.float64)
+
+    def bytes(self, q: int, which: int):
+        w, h = C.c_int(), C.c_int()
+        return _view(self.L.ifo_bytes(self.p, q, which, C.byref(w), C.byref(h)),
+                     w.value, h.value, np.uint8)
+
+
+def occupancy(d11, d12, d21, d22) -> float:
+    return _oracle_lib().ifo_occupancy(d11, d12, d21, d22)
+
+
+def cerp(a, b, c, d, x) -> float:
+    return _oracle_lib().ifo_cerp(a, b, c, d, x)
+
+
+def ref_available(step: int) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, f"libref{step}.so"))
+
+
+_ref_libs = {}
+
+
+def _ref_lib(step):
+    if step not in _ref_libs:
+        L = C.CDLL(os.path.join(REF_DIR, f"libref{step}.so"))
+        vp, i, d = C.c_void_p, C.c_int, C.c_double
+        L.ref_create.restype = vp
+        L.ref_create.argtypes = [i, i, d, d, d]
+        L.ref_destroy.argtypes = [vp]
+        L.ref_add_body.argtypes = [vp, i] + [d] * 8
+        L.ref_get_body.argtypes = [vp, i, C.POINTER(C.c_double)]
+        L.ref_advance_bodies.argtypes = [vp, d]
+        L.ref_add_inflow.argtypes = [vp] + [d] * 8
+        L.ref_update.argtypes = [vp, d]
+        L.ref_pcg_record.argtypes = [i, C.POINTER(i), C.POINTER(i), C.POINTER(d)]
+        L.ref_array.restype = C.POINTER(C.c_double)
+        L.ref_array.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
+        L.ref_bytes.restype = C.POINTER(C.c_uint8)
+        L.ref_bytes.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
+        _ref_libs[step] = L
+    return _ref_libs[step]
+
+
+class RefSolver:
+    """The reference's own FluidSolver of one tutorial step (zero-initialised)."""
+
+    def __init__(self, variant: int, w: int, h: int, density: float = 0.1,
+                 density_soot: float = 1.0, diffusion: float = 0.01):
+        self.L = _ref_lib(variant)
+        self.variant, self.w, self.h = variant, w, h
+        self.p = self.L.ref_create(w, h, density, density_soot, diffusion)
+        self._nb = 0
+        self.last_records = []
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            self.L.ref_destroy(self.p)
+            self.p = None
+
+    def set_bodies(self, bodies):
+        if self._nb:
+            raise RuntimeError("reference bodies can only be added once")
+        for b in bodies:
+            self.L.ref_add_body(self.p, int(b[0]), *[float(x) for x in b[1:9]])
+        self._nb = len(bodies)
+
+    def bodies(self):
+        out = []
+        for k in range(self._nb):
+            buf = (C.c_double * 8)()
+            self.L.ref_get_body(self.p, k, buf)
+            out.append((0,) + tuple(buf))
+        return out
+
+    def advance_bodies(self, dt):
+        self.L.ref_advance_bodies(self.p, dt)
+
+    def add_inflow(self, x, y, w, h, d, t, u, v):
+        self.L.ref_add_inflow(self.p, x, y, w, h, d, t, u, v)
+
+    def update(self, dt):
+        n = self.L.ref_update(self.p, dt)
+        recs = []
+        for k in range(n):
+            it, st, e = C.c_int(), C.c_int(), C.c_double()
+            self.L.ref_pcg_record(k, C.byref(it), C.byref(st), C.byref(e))
+            recs.append((it.value, st.value, e.value))
+        self.last_records = recs
+
+    def stats(self):
+        """(pressure, heat) records of the last update, as the oracle reports them.
+        A solve that returned on its initial residual prints nothing in steps 3-5."""
+        recs = list(self.last_records)
+        need = 2 if self.variant >= HEAT else 1
+        while len(recs) < need:
+            recs.append((0, PCG_INITIAL, 0.0))
+        if self.variant >= HEAT:
+            return recs[1], recs[0]
+        return recs[0], (0, PCG_INITIAL, 0.0)
+
+    def array(self, q: int, which: int):
+        w, h = C.c_int(), C.c_int()
+        return _view(self.L.ref_array(self.p, q, which, C.byref(w), C.byref(h)),
+                     w.value, h.value, np.float64)
+
+    def bytes(self, q: int, which: int):
+        w, h = C.c_int(), C.c_int()
+        return _view(self.L.ref_bytes(self.p, q, which, C.byref(w), C.byref(h)),
+                     w.value, h.value, np.uint8)

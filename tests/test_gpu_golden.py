@@ -1,0 +1,57 @@
+"""CUDA path against the golden fixtures made from the reference itself."""
+import glob
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+
+
+def _scenes():
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "golden", "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return {s[0]: s for s in mod.SCENES}
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_gpu_fp64_matches_golden(ifl, path):
+    name = os.path.basename(path)[:-4]
+    _, variant, w, h, dt, steps, inflow, bodies = _scenes()[name]
+    g = np.load(path)
+    objs = []
+    for b in bodies:
+        objs.append(ifl.SolidBox(*b[1:]) if b[0] == 0 else ifl.SolidSphere(b[1], b[2], b[3], *b[5:]))
+    if variant == 3:
+        s = ifl.FluidSolver(w, h, 0.1)
+    elif variant in (4, 5):
+        s = ifl.FluidSolver(w, h, 0.1, objs, variant=variant)
+    else:
+        s = ifl.FluidSolver(w, h, 0.1, 1.0, 0.01, objs, variant=variant)
+    iters = []
+    for _ in range(steps):
+        if variant >= 6:
+            s.addInflow(*inflow)
+        else:
+            s.addInflow(*inflow[:5], *inflow[6:])
+        s.update(dt)
+        for b in objs:
+            b.update(dt)
+        (pi, ps, _), (hi, hs, _), flags = s.stats()
+        assert flags & 1 == 0
+        iters.append((pi, ps))
+    ref_iters = g["iters"][:, :2]
+    capped = (ref_iters[:, 1] == 2).any()
+    if capped:
+        # 2000 iterations of a stagnating solve amplify rounding; only the outcome is compared
+        assert all(st == 2 for _, st in iters)
+        return
+    assert np.abs(np.array(iters)[:, 0] - ref_iters[:, 0]).max() <= 1
+    for key in ("d", "t", "u", "v", "p"):
+        if key in g:
+            a, b = s.read_field(key), g[key]
+            assert np.abs(a - b).max() <= 1e-9 * max(np.abs(b).max(), 1e-300), key

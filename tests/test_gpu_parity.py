@@ -1,0 +1,220 @@
+"""CUDA path against the oracle, through the C ABI (needs a GB300).
+
+Bars (written per comparison below):
+* bit-exact (equal IEEE values) for every phase except the PCG solves,
+  starting from the oracle's own state: inflow, solid fields, boundary
+  conditions, buoyancy, RHS, densities, matrix, MIC(0) factor, applyPressure,
+  extrapolation and advection;
+* PCG pressure / heat: 1e-10 relative (max-norm) for the FP64 path with the
+  same iteration count; FP32 form: 1e-4 relative against the FP64 oracle from
+  the same state.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+BOX = (0, 0.5, 0.6, 0.7, 0.1, math.pi * 0.25, 0.0, 0.0, 0.0)
+SPIN = (0, 0.55, 0.55, 0.3, 0.12, 0.7, 0.0, 0.0, 1.0)
+BALL = (1, 0.3, 0.45, 0.2, 0.2, 0.0, 0.1, 0.0, 1.0)
+
+# variant, w, h, warm-up steps on the oracle, inflow, bodies
+CASES = [
+    (3, 64, 64, 3, (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.0, 3.0), []),
+    (3, 72, 40, 3, (0.3, 0.2, 0.4, 0.1, 1.0, 0.0, 0.5, 3.0), []),
+    (3, 40, 70, 3, (0.3, 0.2, 0.6, 0.05, 1.0, 0.0, 0.0, 3.0), []),  # inflow x-range wraps (uses h)
+    (4, 64, 64, 3, (0.45, 0.2, 0.15, 0.05, 1.0, 0.0, 0.0, 3.0), [SPIN, BALL]),
+    (4, 50, 66, 3, (0.3, 0.2, 0.4, 0.05, 1.0, 0.0, 0.0, 3.0), [BALL]),
+    (5, 64, 64, 2, (0.45, 0.2, 0.15, 0.05, 1.0, 0.0, 0.0, 3.0), [BOX]),
+    (6, 64, 64, 2, (0.35, 0.2, 0.2, 0.1, 1.0, 594.0, 0.0, 0.0), [BOX]),
+    (7, 64, 64, 2, (0.45, 0.2, 0.1, 0.1, 1.0, 700.0, 0.0, 0.0), [BOX]),
+    (7, 64, 60, 2, (0.45, 0.2, 0.1, 0.1, 1.0, 700.0, 0.0, 0.0), [BOX]),
+]
+IDS = [f"v{c[0]}-{c[1]}x{c[2]}" for c in CASES]
+DT = 0.005
+
+
+def rel_err(a, b):
+    den = np.abs(b).max()
+    return float(np.abs(a - b).max() / (den if den > 0 else 1.0))
+
+
+def make_gpu(ifl, variant, w, h, bodies, precision=0):
+    if variant == 3:
+        g = ifl.FluidSolver(w, h, 0.1, precision=precision)
+    elif variant in (4, 5):
+        g = ifl.FluidSolver(w, h, 0.1, list(bodies), variant=variant, precision=precision)
+    else:
+        g = ifl.FluidSolver(w, h, 0.1, 1.0, 0.01, list(bodies), variant=variant, precision=precision)
+    return g
+
+
+def quantities(variant):
+    return [O.QD, O.QU, O.QV] + ([O.QT] if variant >= 6 else [])
+
+
+def upload(ifl, g, o, variant):
+    """Copy every state array of the oracle into the GPU solver."""
+    fdt = np.float64 if g.precision == ifl.FP64 else np.float32
+    for q in quantities(variant):
+        for a in (O.A_SRC, O.A_DST):
+            g.write_field(ifl.field_id(q, a), o.array(q, a).astype(fdt))
+        if variant >= 4:
+            g.write_field(ifl.field_id(q, ifl.A_CELL), o.bytes(q, O.B_CELL).copy())
+            g.write_field(ifl.field_id(q, ifl.A_BODY), o.bytes(q, O.B_BODY).copy())
+            g.write_field(ifl.field_id(q, ifl.A_NORMALX), o.array(q, O.A_NORMALX).copy())
+            g.write_field(ifl.field_id(q, ifl.A_NORMALY), o.array(q, O.A_NORMALY).copy())
+        if variant >= 5:
+            g.write_field(ifl.field_id(q, ifl.A_PHI), o.array(q, O.A_PHI).copy())
+            g.write_field(ifl.field_id(q, ifl.A_VOLUME), o.array(q, O.A_VOLUME).copy())
+    for f, a in ((ifl.F_R, O.A_R), (ifl.F_P, O.A_P), (ifl.F_ADIAG, O.A_ADIAG),
+                 (ifl.F_APLUSX, O.A_APLUSX), (ifl.F_APLUSY, O.A_APLUSY)):
+        g.write_field(f, o.array(0, a).astype(fdt))
+    g.write_field(ifl.F_PRECON, o.array(0, O.A_PRECON).copy())
+    if variant == 7:
+        g.write_field(ifl.F_UDENS, o.array(0, O.A_UDENS).astype(fdt))
+        g.write_field(ifl.F_VDENS, o.array(0, O.A_VDENS).astype(fdt))
+
+
+def assert_same(ifl, g, o, variant, what, arrays):
+    for q, a in arrays:
+        if a in ("cell", "body"):
+            got = g.read_field(ifl.field_id(q, ifl.A_CELL if a == "cell" else ifl.A_BODY), np.uint8)
+            ref = o.bytes(q, O.B_CELL if a == "cell" else O.B_BODY)
+        elif a >= 16:
+            got = g.read_field(a)
+            ref = o.array(0, a)
+        else:
+            got = g.read_field(ifl.field_id(q, a))
+            ref = o.array(q, a)
+        bad = np.argwhere(got != ref)
+        assert bad.size == 0, f"{what}: q={q} a={a} first mismatch at {bad[0]} " \
+                              f"gpu={got[tuple(bad[0])]!r} oracle={ref[tuple(bad[0])]!r} ({len(bad)} cells)"
+
+
+def warm_oracle(variant, w, h, steps, inflow, bodies):
+    o = O.OracleSolver(variant, w, h)
+    if bodies:
+        o.set_bodies(bodies)
+    for _ in range(steps):
+        o.add_inflow(*inflow)
+        o.update(DT)
+        o.advance_bodies(DT)
+    return o
+
+
+def src_dst(variant):
+    return [(q, a) for q in quantities(variant) for a in (O.A_SRC, O.A_DST)]
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_phases_bit_exact_fp64(ifl, case):
+    variant, w, h, warm, inflow, bodies = case
+    o = warm_oracle(variant, w, h, warm, inflow, bodies)
+    g = make_gpu(ifl, variant, w, h, o.bodies())
+    upload(ifl, g, o, variant)
+
+    o.add_inflow(*inflow)
+    g.addInflow(*inflow[:5], *inflow[5:]) if variant >= 6 else g.addInflow(*inflow[:5], *inflow[6:])
+    assert_same(ifl, g, o, variant, "inflow", [(q, O.A_SRC) for q in quantities(variant)])
+
+    geo = []
+    if variant >= 4:
+        for q in quantities(variant):
+            geo += [(q, "cell"), (q, "body"), (q, O.A_NORMALX), (q, O.A_NORMALY)]
+            if variant >= 5:
+                geo += [(q, O.A_PHI), (q, O.A_VOLUME)]
+    plan = [(O.PH_FILL_SOLID, geo)]
+    if variant >= 6:
+        plan += [(O.PH_HEAT, None), (O.PH_EXTRAP_T, [(O.QT, O.A_SRC)]),
+                 (O.PH_BUOYANCY, [(O.QV, O.A_SRC)])]
+    plan += [(O.PH_BC, [(O.QU, O.A_SRC), (O.QV, O.A_SRC)]), (O.PH_RHS, [(0, O.A_R)])]
+    if variant == 7:
+        plan += [(O.PH_DENSITIES, [(0, O.A_UDENS), (0, O.A_VDENS)])]
+    plan += [(O.PH_MATRIX, [(0, O.A_ADIAG), (0, O.A_APLUSX), (0, O.A_APLUSY)]),
+             (O.PH_PRECON, None), (O.PH_PROJECT, None),
+             (O.PH_APPLY_P, [(O.QU, O.A_SRC), (O.QV, O.A_SRC)]),
+             (O.PH_EXTRAP_DUV, [(q, O.A_SRC) for q in (O.QD, O.QU, O.QV)]),
+             (O.PH_BC, [(O.QU, O.A_SRC), (O.QV, O.A_SRC)]),
+             (O.PH_ADVECT, src_dst(variant))]
+    for ph, arrays in plan:
+        o.phase(ph, DT)
+        g.run_phase(ph, DT)
+        if ph == O.PH_PRECON:
+            pc_g, pc_o = g.read_field(ifl.F_PRECON), o.array(0, O.A_PRECON)
+            if variant >= 4:  # non-fluid cells keep stale values on both sides
+                fl = o.bytes(O.QD, O.B_CELL) == 0
+                pc_g, pc_o = pc_g[fl], pc_o[fl]
+            assert np.array_equal(pc_g, pc_o), "MIC(0) factor"
+        elif ph in (O.PH_PROJECT, O.PH_HEAT):
+            (pi, ps, pe), (hi, hs, he), flags = g.stats()
+            (opi, ops, ope), (ohi, ohs, ohe) = o.stats()
+            assert flags & 1 == 0, "device wait timed out"
+            if ph == O.PH_PROJECT:
+                assert (pi, ps) == (opi, ops)
+                assert rel_err(g.read_field("p"), o.array(0, O.A_P)) < 1e-10
+            else:
+                assert (hi, hs) == (ohi, ohs)
+                assert rel_err(g.read_field("t"), o.array(O.QT, O.A_SRC)) < 1e-10
+        else:
+            assert_same(ifl, g, o, variant, f"phase {ph}", arrays)
+        upload(ifl, g, o, variant)  # next phase starts from the oracle's exact state
+
+
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_trajectory_fp64(ifl, case):
+    """Whole update() calls from a zero state: fields stay within 1e-9 (PCG rounding only)."""
+    variant, w, h, _, inflow, bodies = case
+    o = O.OracleSolver(variant, w, h)
+    if bodies:
+        o.set_bodies(bodies)
+    g = make_gpu(ifl, variant, w, h, bodies)
+    for step in range(6):
+        o.add_inflow(*inflow)
+        g.addInflow(*inflow[:5], *inflow[5:]) if variant >= 6 else g.addInflow(*inflow[:5], *inflow[6:])
+        g.set_bodies(o.bodies())
+        o.update(DT)
+        g.update(DT)
+        o.advance_bodies(DT)
+        (pi, ps, _), _, flags = g.stats()
+        assert flags & 1 == 0
+        assert abs(pi - o.stats()[0][0]) <= 1, step
+        for name, q in (("d", O.QD), ("u", O.QU), ("v", O.QV)):
+            assert rel_err(g.read_field(name), o.array(q, O.A_SRC)) < 1e-9, (step, name)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c[1] == 64 and c[2] == 64], ids=lambda c: f"v{c[0]}")
+def test_fp32_form_error_vs_fp64_oracle(ifl, case):
+    """FP32 form, one update from the oracle's state: <= 1e-4 relative (pressure, velocity)."""
+    variant, w, h, warm, inflow, bodies = case
+    o = warm_oracle(variant, w, h, warm + 2, inflow, bodies)
+    g = make_gpu(ifl, variant, w, h, o.bodies(), precision=ifl.FP32)
+    upload(ifl, g, o, variant)
+    o.add_inflow(*inflow)
+    g.addInflow(*inflow[:5], *inflow[5:]) if variant >= 6 else g.addInflow(*inflow[:5], *inflow[6:])
+    o.update(DT)
+    g.update(DT)
+    _, _, flags = g.stats()
+    assert flags & 1 == 0
+    errs = {"p": rel_err(g.read_field("p"), o.array(0, O.A_P))}
+    for name, q in (("u", O.QU), ("v", O.QV), ("d", O.QD)):
+        errs[name] = rel_err(g.read_field(name), o.array(q, O.A_SRC))
+    assert errs["p"] < 1e-4 and errs["u"] < 1e-4 and errs["v"] < 1e-4, errs
+
+
+def test_deterministic_and_stream_ordered(ifl):
+    """Two identical runs give bit-identical fields (fixed-order reductions)."""
+    outs = []
+    for _ in range(2):
+        g = make_gpu(ifl, 4, 96, 80, [SPIN, BALL])
+        for _ in range(4):
+            g.addInflow(0.45, 0.2, 0.15, 0.05, 1.0, 0.0, 3.0)
+            g.update(DT)
+        outs.append([g.read_field(n) for n in ("d", "u", "v", "p")])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
