@@ -1,0 +1,350 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 incremental-fluids hot path (one JSON line on stdout).
+
+Workload (default): the solid-boundary scene with three seeded bodies at
+1024 x 1024 (hx = 1/1024, dt = 0.0025, config-0 inflow rectangle) in the FP32
+precision form; a step is one addInflow + update() of that scene.  Metric:
+cell-steps/s = w*h x update() calls per second.
+
+* value     device time of K steps (CUDA events on the solver's stream), L2
+            flushed (a 512 MiB write) between steps, outside the timed events;
+* e2e       the same steps through the public API (ifluids.FluidSolver over
+            the C ABI), wall clock, with the body table uploaded from pinned
+            host memory and the density field read back into a pinned buffer
+            every step;
+* roofline  persistent PCG kernel (the dominant kernel): algorithmic bytes /
+            device time from the library's own CUDA events around every PCG
+            launch inside the timed region, against MEASURED_PEAKS.json;
+* cpu_baseline  the C oracle (restatement of the reference, FP64, one scene
+            per process) on the host cores, one update of the same scene per
+            process.
+
+--impl reference times the reference's CPU algorithm (the oracle port; the
+reference's own sources are not present on the GPU host) on the same workload.
+Multi-GPU (torchrun): each rank runs an independent replica of the scene
+("replicas only": a single scene does not shard), barrier + max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "incremental-fluids_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "cell-steps/s"
+# Algorithmic bytes per cell of the persistent PCG kernel (strip-diagonal
+# arrays, F = storage width, neighbour bits 1 byte, FP64 factor):
+#   factor  reads adiag, ax, ay, nb; writes pc (8 B), pcf, lx, ly      = 6F + 9
+#   setup   p = 0, |r|_inf, forward (r, lx, ly, pcf, nb -> z) and
+#           backward (z, lx, ly, pcf, r, nb -> z) substitutions         = 13F + 3
+#   per iteration: s-update + matvec + dot (7F + 1), AXPYs + norm
+#           (6F + 1), forward (5F + 1) and backward (6F + 1)            = 24F + 4
+#   the last iteration stops after the AXPYs (no substitutions)         = -(11F + 2)
+
+
+def pcg_bytes_per_cell(F: int, launches: int, iterations: int) -> float:
+    return launches * ((6 * F + 9) + (13 * F + 3) - (11 * F + 2)) + iterations * (24 * F + 4)
+
+
+def load_peaks():
+    for path in (os.path.join(ROOT, "MEASURED_PEAKS.json"),):
+        try:
+            with open(path) as f:
+                d = json.load(f)
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        self.device = ids[device] if device < len(ids) else str(device)
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def _cpu_worker(args):
+    variant, n, steps, seed = args
+    from oracle import oracle as O
+    from ifluids import scenes
+    sc = scenes.config1(n=n, seed=seed, variant=variant)
+    o = O.OracleSolver(variant, n, n)
+    o.set_bodies(sc.bodies)
+    t0 = time.perf_counter()
+    its = []
+    for _ in range(steps):
+        o.add_inflow(*sc.inflows[0])
+        o.update(sc.dt)
+        o.advance_bodies(sc.dt)
+        its.append(o.stats()[0][0])
+    return time.perf_counter() - t0, its
+
+
+def cpu_baseline(n: int, steps: int, procs: int, seed: int):
+    """The oracle on `procs` host cores, one independent scene per process."""
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_worker, [(4, n, steps, seed)] * procs)
+    t = max(r[0] for r in res)
+    return {"value": procs * n * n * steps / t, "unit": METRIC, "cores": procs, "kind": "port",
+            "sample": f"{steps} update() of the {n}x{n} solid-boundary scene from its initial state "
+                      f"(PCG iterations {res[0][1]}) in each of {procs} processes, FP64 oracle",
+            "seconds": round(t, 2)}
+
+
+# ----------------------------------------------------------------- GPU arm
+def make_solver(ifl, sc, precision, device, bodies):
+    return ifl.FluidSolver(sc.w, sc.h, sc.density, bodies, variant=sc.variant, precision=precision,
+                           device=device)
+
+
+def body_objs(ifl, sc):
+    out = []
+    for b in sc.bodies:
+        out.append(ifl.SolidBox(*b[1:]) if b[0] == 0 else ifl.SolidSphere(b[1], b[2], b[3], *b[5:]))
+    return out
+
+
+def step_host(g, sc, bodies):
+    x, y, w, h, d, t, u, v = sc.inflows[0]
+    g.addInflow(x, y, w, h, d, u, v)
+    g.update(sc.dt)
+    for b in bodies:
+        b.update(sc.dt)
+
+
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    import ifluids as ifl
+    from ifluids import scenes
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    prec = ifl.FP32 if args.precision == "fp32" else ifl.FP64
+    fbytes = 4 if prec == ifl.FP32 else 8
+    sc = scenes.config1(n=args.size, seed=args.seed)
+    cells = sc.cells
+    bodies = body_objs(ifl, sc)
+    g = make_solver(ifl, sc, prec, local_rank, bodies)
+    stream = torch.cuda.ExternalStream(g.stream, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    for _ in range(args.warmup):
+        step_host(g, sc, bodies)
+    g.synchronize()
+    g.set_timing(True)
+    g.timing()  # reset accumulators
+    launches0 = g.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))  # > L2: evict the previous step's working set
+                ev[k][0].record(stream)
+            step_host(g, sc, bodies)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+        g.synchronize()
+        torch.cuda.synchronize(dev)
+    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+    launches = g.launch_count() - launches0
+    kms, klaunch, iters = g.timing()
+    g.set_timing(False)
+    (pit, pst, perr), _, flags = g.stats()
+    if flags & 1:
+        raise RuntimeError("device-side wait timed out during the benchmark")
+
+    t_max = dev_ms
+    if world > 1:
+        t = torch.tensor([dev_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * cells * args.steps / (t_max / 1e3)
+
+    # ---- end to end through the public API with pinned host buffers
+    host_d = torch.empty((sc.h, sc.w), dtype=torch.float32 if prec == ifl.FP32 else torch.float64,
+                         pin_memory=True).numpy()
+    g.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        step_host(g, sc, bodies)                      # body table: pinned upload inside update
+        g.read_field("d", dtype=host_d.dtype, out=host_d)  # result back to the host
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * cells * args.steps / e2e_s, "unit": METRIC,
+           "h2d_bytes_per_step": 96 * len(sc.bodies), "d2h_bytes_per_step": cells * fbytes}
+
+    # ---- roofline of the persistent PCG kernel
+    peak, peak_kind = load_peaks()
+    pcg_bytes = cells * pcg_bytes_per_cell(fbytes, klaunch["pcg"], iters)
+    achieved = pcg_bytes / (kms["pcg"] / 1e3) / 1e9 if kms["pcg"] > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": "pcg_kernel", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": f"of {peak_kind}",
+            "traffic": None,
+            "pcg_ms_per_launch": round(kms["pcg"] / max(1, klaunch["pcg"]), 3),
+            "pcg_iterations_per_launch": round(iters / max(1, klaunch["pcg"]), 1),
+            "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()}}
+
+    # ---- FP64 drop-in on the same scene (reported beside the FP32 form)
+    fp64 = None
+    if prec == ifl.FP32 and args.fp64_steps > 0:
+        g64 = make_solver(ifl, sc, ifl.FP64, local_rank, body_objs(ifl, sc))
+        b64 = body_objs(ifl, sc)
+        g64.set_bodies(b64)
+        for _ in range(2):
+            step_host(g64, sc, b64)
+        g64.synchronize()
+        s64 = torch.cuda.ExternalStream(g64.stream, device=dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s64):
+            e0.record(s64)
+        for _ in range(args.fp64_steps):
+            step_host(g64, sc, b64)
+        with torch.cuda.stream(s64):
+            e1.record(s64)
+        g64.synchronize()
+        fp64 = {"value": cells * args.fp64_steps / (e0.elapsed_time(e1) / 1e3), "unit": METRIC,
+                "steps": args.fp64_steps, "pcg_iterations_last": g64.stats()[0][0]}
+        g64.close()
+    g.close()
+    return {"value": value, "ms_per_step": t_max / args.steps, "e2e": e2e, "roofline": roof,
+            "gpu_launches": launches, "clocks": clk.summary(), "pcg_iterations_last": pit,
+            "pcg_status_last": pst, "fp64_dropin": fp64, "cells": cells, "scene": sc}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--precision", choices=("fp32", "fp64"), default="fp32")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    procs = args.cpu_procs or max(1, min(16, os.cpu_count() or 1))
+    config = {"workload": f"solid-boundary scene {args.size}x{args.size}, 3 seeded bodies, "
+                          f"dt=0.0025, config-0 inflow (configs[1])",
+              "variant": "4-solid-boundaries", "grid": [args.size, args.size], "bodies": 3, "seed": args.seed,
+              "precision_form": args.precision, "l2": "flushed between timed steps (512 MiB write)",
+              "scene_data": "seeded synthetic scene"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = max(1, min(args.steps, 2))
+        cb = cpu_baseline(args.size, steps, procs, args.seed)
+        line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": args.gpus,
+                "steps": args.steps, "steps_timed": steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * cb["seconds"] / steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+                "impl": "reference", "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference algorithm on the host cores (oracle port of the reference sources, "
+                        "bit-identical to them where they compile); each step a full update of the scene "
+                        "in every process; steps capped to keep the run within minutes"}
+        print(json.dumps(line), flush=True)
+        return
+
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cb = cpu_baseline(args.size, 1, procs, args.seed)  # before any GPU work (spawned pool)
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    r = run_gpu(args, rank, world, local_rank)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+            "data": "synthetic", "config": config, "e2e": r["e2e"], "roofline": r["roofline"],
+            "cpu_baseline": cb, "gpu_launches": r["gpu_launches"], "clocks": r["clocks"],
+            "pcg": {"iterations_last_step": r["pcg_iterations_last"], "status_last_step": r["pcg_status_last"]},
+            "fp64_dropin": r["fp64_dropin"]}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

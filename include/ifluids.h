@@ -109,6 +109,8 @@ typedef struct {
     int32_t max_iter_pressure; /* 600 in step 3, 2000 in steps 4-7               */
     int32_t max_iter_heat;     /* 2000                                           */
     void *stream;              /* cudaStream_t to use; NULL = handle-owned stream */
+    int32_t device;            /* CUDA device ordinal the handle lives on (0)    */
+    int32_t pad_;
 } ifl_params;
 
 /* Solid body; same parameters as SolidBox(x, y, sx, sy, t, vx, vy, vt) and
@@ -168,8 +170,30 @@ int ifl_flip(ifl_solver *s, int quantity);
 
 /* PCG outcome of the last update (synchronises). */
 int ifl_get_stats(ifl_solver *s, ifl_step_stats *out);
-/* -1: stop on the residual test (default); k >= 0: run exactly k iterations. */
-int ifl_set_pinned_iterations(ifl_solver *s, int k);
+/* Per solve: -1 stops on the residual test (default); k >= 0 runs exactly k
+ * iterations (separates rounding drift from a flip of the termination test). */
+int ifl_set_pinned_iterations(ifl_solver *s, int pressure, int heat);
+
+/* Kernel timing.  When on, every kernel group launched by the handle is
+ * bracketed by CUDA events on the handle's stream (no host synchronisation);
+ * ifl_get_timing synchronises, returns the accumulated device time per group
+ * and resets the accumulators. */
+enum {
+    IFL_K_PCG = 0,         /* persistent MIC(0)-PCG kernel (factor + solve)   */
+    IFL_K_ASSEMBLE = 1,    /* RHS / densities / matrix / heat matrix          */
+    IFL_K_ADVECT = 2,      /* fused advection of every quantity               */
+    IFL_K_SOLID = 3,       /* distance field, cells, normals, volumes         */
+    IFL_K_EXTRAPOLATE = 4, /* solid-cell extrapolation                        */
+    IFL_K_FACES = 5,       /* inflow, boundary conditions, buoyancy, pressure update */
+    IFL_K_GROUPS = 6
+};
+typedef struct {
+    double ms[IFL_K_GROUPS];           /* device time per group               */
+    int64_t launches[IFL_K_GROUPS];    /* timed launches per group            */
+    int64_t pcg_iterations;            /* PCG iterations inside the timed PCG launches */
+} ifl_timing;
+int ifl_set_timing(ifl_solver *s, int on);
+int ifl_get_timing(ifl_solver *s, ifl_timing *out);
 
 int ifl_synchronize(ifl_solver *s);
 void *ifl_stream(ifl_solver *s);

@@ -14,6 +14,10 @@ namespace {
 template <typename Fn>
 int guarded(ifl_solver *s, Fn fn) {
     if (!s || !s->impl) return IFL_ERR_ARG;
+    if (s->impl->activate() != 0) {
+        s->impl->set_error("cannot make the handle's device current");
+        return IFL_ERR_CUDA;
+    }
     try {
         return fn(*s->impl);
     } catch (const std::bad_alloc &) {
@@ -49,6 +53,7 @@ int ifl_create(const ifl_params *p, ifl_solver **out) {
     if (p->variant < IFL_PLAIN || p->variant > IFL_VARDENS) return IFL_ERR_ARG;
     if (p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768) return IFL_ERR_ARG;
     if (p->precision != IFL_FP64 && p->precision != IFL_FP32) return IFL_ERR_ARG;
+    if (p->device < 0) return IFL_ERR_ARG;
     if (p->max_iter_pressure < 0 || p->max_iter_heat < 0) return IFL_ERR_ARG;
     if (!(p->density_air > 0.0)) return IFL_ERR_ARG;
     ifl_solver *s = new (std::nothrow) ifl_solver;
@@ -70,7 +75,7 @@ int ifl_create(const ifl_params *p, ifl_solver **out) {
 
 int ifl_destroy(ifl_solver *s) {
     if (!s) return IFL_ERR_ARG;
-    if (s->impl) cudaStreamSynchronize(s->impl->stream());
+    if (s->impl) s->impl->activate();
     delete s;
     return IFL_OK;
 }
@@ -114,8 +119,8 @@ double ifl_ambient_t(const ifl_solver *s) {
 int ifl_field_shape(const ifl_solver *s, int field, int *w, int *h) {
     if (!s || !s->impl || !w || !h) return IFL_ERR_ARG;
     void *p;
-    int elem;
-    return s->impl->field_info(field, &p, &elem, w, h);
+    int elem, sd;
+    return s->impl->field_info(field, &p, &elem, w, h, &sd);
 }
 
 int ifl_read_field(ifl_solver *s, int field, void *host, size_t bytes, int dtype) {
@@ -142,11 +147,20 @@ int ifl_get_stats(ifl_solver *s, ifl_step_stats *out) {
     });
 }
 
-int ifl_set_pinned_iterations(ifl_solver *s, int k) {
+int ifl_set_pinned_iterations(ifl_solver *s, int pressure, int heat) {
     return guarded(s, [&](ifl::SolverBase &v) {
-        v.set_pinned(k < 0 ? -1 : k);
+        v.set_pinned(pressure < 0 ? -1 : pressure, heat < 0 ? -1 : heat);
         return (int)IFL_OK;
     });
+}
+
+int ifl_set_timing(ifl_solver *s, int on) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.set_timing(on != 0); });
+}
+
+int ifl_get_timing(ifl_solver *s, ifl_timing *out) {
+    if (!out) return IFL_ERR_ARG;
+    return guarded(s, [&](ifl::SolverBase &v) { return v.get_timing(out); });
 }
 
 int ifl_synchronize(ifl_solver *s) {

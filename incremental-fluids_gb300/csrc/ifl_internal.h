@@ -8,6 +8,14 @@
 //   cell (x, y) of any grid lives at x + y*P.
 // Field storage type F is double (IFL_FP64) or float (IFL_FP32); solid
 // geometry (distance, normals, volumes) and the MIC(0) factor stay FP64.
+//
+// The pressure system (matrix, MIC(0) operands, PCG vectors) uses the
+// strip-diagonal layout SDIdx: rows are grouped in 32-row strips and, inside a
+// strip, cells are ordered by anti-diagonal d = x + lane (lane = y mod 32),
+// 32 lanes contiguous.  A MIC(0) wavefront step of a strip touches exactly one
+// diagonal, so every array is read and written as one contiguous 32-element
+// line per step and a run of steps is one contiguous block (streamed into
+// shared memory by bulk copies).
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -38,6 +46,26 @@ struct DevBody {
     double cpos, spos, cneg, sneg;
 };
 
+// Strip-diagonal index: slot(x, y) = ((s*D + x + l)*32 + l), s = y/32, l = y%32.
+// D (diagonals per strip) covers W + 31 and is padded to a multiple of kSweepBlock.
+constexpr int kSweepBlock = 16;
+struct SDIdx {
+    int W, H, S, D;
+    __host__ __device__ __forceinline__ size_t slot(int x, int y) const {
+        const int s = y >> 5, l = y & 31;
+        return ((size_t)s * D + x + l) * 32 + l;
+    }
+    __host__ __device__ __forceinline__ size_t total() const { return (size_t)S * D * 32; }
+    static SDIdx make(int w, int h) {
+        SDIdx r;
+        r.W = w;
+        r.H = h;
+        r.S = (h + 31) / 32;
+        r.D = (w + 31 + kSweepBlock - 1) / kSweepBlock * kSweepBlock;
+        return r;
+    }
+};
+
 template <typename F>
 struct Quant {
     F *src, *dst;
@@ -55,6 +83,7 @@ struct Scene {
     double hx;
     double rho_air, rho_soot, diffusion, t_amb, g;
     Quant<F> q[4];  // d, t, u, v
+    SDIdx sd;          // layout of the pressure-system arrays below
     F *r, *p, *z, *sa, *sb, *as;
     F *adiag, *ax, *ay;
     F *lx, *ly, *pcf;  // MIC(0) apply operands in storage precision
@@ -78,6 +107,7 @@ struct PcgScratch {
     unsigned *barrier;   // 2 words
     unsigned *progress;  // one word per 32-row strip
     PcgOut *out;
+    unsigned long long *iter_total;  // PCG iterations summed over launches
     int max_blocks;
 };
 
@@ -101,6 +131,8 @@ template <typename F> void launch_heat_assemble(const Scene<F> &S, double dt, cu
 template <typename F> void launch_apply_pressure(const Scene<F> &S, double dt, cudaStream_t st);
 template <typename F> void launch_extrapolate(const Scene<F> &S, unsigned qmask, cudaStream_t st);
 template <typename F> void launch_advect(const Scene<F> &S, double dt, cudaStream_t st);
+// strip-diagonal <-> row-major copy of one w x h array (dir 0: SD -> rows)
+template <typename F> void launch_sd_copy(const Scene<F> &S, F *rows, F *sd_arr, int dir, cudaStream_t st);
 template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
                                              cudaStream_t st, int *blocks_used);
 template <typename F> int pcg_max_blocks();

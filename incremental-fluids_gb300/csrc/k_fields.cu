@@ -232,6 +232,7 @@ __global__ void assemble_kernel(Scene<F> S, double dt, int what) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
     const size_t c = x + (size_t)y * P;
+    const size_t k = S.sd.slot(x, y);  // pressure-system arrays are strip-diagonal
     const int var = S.variant;
     const uint8_t *cell = S.q[0].cell;
     const bool plain = var == 3;
@@ -263,7 +264,7 @@ __global__ void assemble_kernel(Scene<F> S, double dt, int what) {
                     r += (vv1 - vol) * body_vel_y(S.bodies[body[c + P]], (x + 0.5) * hx, (y + 1.0) * hx);
             }
         }
-        S.r[c] = (F)r;
+        S.r[k] = (F)r;
     }
 
     if (what & ASM_DENS) {  // face densities for applyPressure (step 7)
@@ -297,9 +298,9 @@ __global__ void assemble_kernel(Scene<F> S, double dt, int what) {
                 ay = -f;
             }
         }
-        S.adiag[c] = (F)diag;
-        S.ax[c] = (F)ax;
-        S.ay[c] = (F)ay;
+        S.adiag[k] = (F)diag;
+        S.ax[k] = (F)ax;
+        S.ay[k] = (F)ay;
         uint8_t nb = (fl ? NB_SELF : 0) | (fL ? NB_LEFT : 0) | (fD ? NB_DOWN : 0) | (fR ? NB_RIGHT : 0) |
                      (fU ? NB_UP : 0) | ((var < 6 || cell[c] == CELL_FLUID) ? NB_RED : 0);
         // The MIC(0) sweeps use the fluid test of each neighbour, independent
@@ -311,7 +312,7 @@ __global__ void assemble_kernel(Scene<F> S, double dt, int what) {
             if (x < w - 1 && cell[c + 1] == CELL_FLUID) nb |= NB_RIGHT;
             if (y < h - 1 && cell[c + P] == CELL_FLUID) nb |= NB_UP;
         }
-        S.nb[c] = nb;
+        S.nb[k] = nb;
     }
 }
 
@@ -323,9 +324,10 @@ __global__ void heat_assemble_kernel(Scene<F> S, double dt) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
     const size_t c = x + (size_t)y * P;
+    const size_t k = S.sd.slot(x, y);
     const uint8_t *cell = S.q[0].cell;
     const bool fl = cell[c] == CELL_FLUID;
-    S.r[c] = S.q[1].src[c];
+    S.r[k] = S.q[1].src[c];
     double scale = S.diffusion * dt * 1.0 / (S.hx * S.hx);
     bool fL = x > 0 && fl && cell[c - 1] == CELL_FLUID;
     bool fR = x < w - 1 && fl && cell[c + 1] == CELL_FLUID;
@@ -336,15 +338,15 @@ __global__ void heat_assemble_kernel(Scene<F> S, double dt) {
     if (fL) diag += scale;
     if (fR) diag += scale;
     if (fU) diag += scale;
-    S.adiag[c] = (F)diag;
-    S.ax[c] = (F)(fR ? -scale : 0.0);
-    S.ay[c] = (F)(fU ? -scale : 0.0);
+    S.adiag[k] = (F)diag;
+    S.ax[k] = (F)(fR ? -scale : 0.0);
+    S.ay[k] = (F)(fU ? -scale : 0.0);
     uint8_t nb = (fl ? NB_SELF : 0) | (fl ? NB_RED : 0);
     if (x > 0 && cell[c - 1] == CELL_FLUID) nb |= NB_LEFT;
     if (y > 0 && cell[c - P] == CELL_FLUID) nb |= NB_DOWN;
     if (x < w - 1 && cell[c + 1] == CELL_FLUID) nb |= NB_RIGHT;
     if (y < h - 1 && cell[c + P] == CELL_FLUID) nb |= NB_UP;
-    S.nb[c] = nb;
+    S.nb[k] = nb;
 }
 
 // ---------------------------------------------------------- applyPressure
@@ -367,11 +369,11 @@ __global__ void apply_pressure_kernel(Scene<F> S, double dt) {
         }
         double val = (double)*u;
         if (fx > 0 && (var == 3 || cell[f - 1] == CELL_FLUID)) {
-            double pv = (double)S.p[f - 1];
+            double pv = (double)S.p[S.sd.slot(fx - 1, fy)];
             val += (var == 7) ? scale * pv / (double)S.udens[f] : scale * pv;
         }
         if (fx < w && (var == 3 || cell[f] == CELL_FLUID)) {
-            double pv = (double)S.p[f];
+            double pv = (double)S.p[S.sd.slot(fx, fy)];
             val -= (var == 7) ? scale * pv / (double)S.udens[f] : scale * pv;
         }
         *u = (F)val;
@@ -385,11 +387,11 @@ __global__ void apply_pressure_kernel(Scene<F> S, double dt) {
         }
         double val = (double)*v;
         if (fy > 0 && (var == 3 || cell[f - P] == CELL_FLUID)) {
-            double pv = (double)S.p[f - P];
+            double pv = (double)S.p[S.sd.slot(fx, fy - 1)];
             val += (var == 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
         }
         if (fy < h && (var == 3 || cell[f] == CELL_FLUID)) {
-            double pv = (double)S.p[f];
+            double pv = (double)S.p[S.sd.slot(fx, fy)];
             val -= (var == 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
         }
         *v = (F)val;
@@ -577,6 +579,16 @@ __global__ void advect_kernel(Scene<F> S, F dt) {
     }
 }
 
+// Strip-diagonal <-> row-major copy of one w x h array (T = p after the heat solve).
+template <typename F>
+__global__ void sd_copy_kernel(SDIdx sd, int P, F *rows, F *sd_arr, int dir) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= sd.W || y >= sd.H) return;
+    size_t r = x + (size_t)y * P, k = sd.slot(x, y);
+    if (dir == 0) rows[r] = sd_arr[k];
+    else sd_arr[k] = rows[r];
+}
+
 inline dim3 grid2(int nx, int ny, int nz, dim3 b) {
     return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y, nz);
 }
@@ -643,6 +655,12 @@ void launch_advect(const Scene<F> &S, double dt, cudaStream_t st) {
     advect_kernel<F><<<grid2(S.w + 1, S.h + 1, 3, b), b, 0, st>>>(S, (F)dt);
 }
 
+template <typename F>
+void launch_sd_copy(const Scene<F> &S, F *rows, F *sd_arr, int dir, cudaStream_t st) {
+    dim3 b(32, 8);
+    sd_copy_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S.sd, S.P, rows, sd_arr, dir);
+}
+
 #define IFL_INST(F)                                                                                        \
     template void launch_inflow<F>(const Scene<F> &, int, double, double, double, double, double,           \
                                    cudaStream_t);                                                          \
@@ -653,7 +671,8 @@ void launch_advect(const Scene<F> &S, double dt, cudaStream_t st) {
     template void launch_heat_assemble<F>(const Scene<F> &, double, cudaStream_t);                          \
     template void launch_apply_pressure<F>(const Scene<F> &, double, cudaStream_t);                         \
     template void launch_extrapolate<F>(const Scene<F> &, unsigned, cudaStream_t);                          \
-    template void launch_advect<F>(const Scene<F> &, double, cudaStream_t);
+    template void launch_advect<F>(const Scene<F> &, double, cudaStream_t);                                 \
+    template void launch_sd_copy<F>(const Scene<F> &, F *, F *, int, cudaStream_t);
 IFL_INST(double)
 IFL_INST(float)
 

@@ -7,36 +7,47 @@
 // masked forms in 4-solid-boundaries/Fluid.cpp:656-721 and
 // 6-heat/Fluid.cpp:781-826.
 //
+// Data: every array of the pressure system is in the strip-diagonal layout
+// (SDIdx): a 32-row strip stores its cells diagonal by diagonal, 32 lanes
+// contiguous.
+//
 // Work decomposition
-//  * Elementwise phases (fused s-update + matvec + dot; AXPYs + max-norm):
-//    grid-stride over cells, per-block partial sums in FP64, a fixed-order
-//    cross-block reduction that every block performs identically, so all
-//    blocks take the same branch and the result is run-to-run deterministic.
-//  * MIC(0) factor and both triangular solves: anti-diagonal wavefronts.  A
-//    warp owns a 32-row strip; lane y handles row y and lags lane y-1 by one
-//    step, receiving the lower neighbour through a register shuffle.  The
-//    strip below publishes its progress (columns completed in its top row)
-//    through a release flag that the next strip's lane 0 waits on.  Every cell
-//    performs exactly the reference's arithmetic in a dependency-respecting
-//    order, so the factor and the solves are bit-identical to the sequential
-//    loops.
-//  * Phases are separated by a grid barrier of this file (bounded waits).
-// Every wait is bounded: on timeout the status word gets FLAG_TIMEOUT, waits
-// stop waiting, the kernel runs to its end and the host reports an error.
+//  * Elementwise phases (fused s-update + matvec + dot; AXPYs + max-norm): each
+//    warp takes whole diagonals (32 contiguous slots), per-block partial sums
+//    in FP64, and a fixed-order cross-block reduction that every block performs
+//    identically, so all blocks take the same branch and results are
+//    run-to-run deterministic.
+//  * MIC(0) factor and both triangular solves: anti-diagonal wavefronts.  Warp
+//    0 of block s owns strip s; lane l handles row 32s+l and at step t works on
+//    diagonal t (backward: the mirrored diagonal), so the lower (upper)
+//    neighbour's result arrives from lane l-1 (l+1) through a register
+//    shuffle.  Operands stream through a shared-memory ring filled by bulk
+//    asynchronous copies (cp.async.bulk, completion on an mbarrier), one
+//    contiguous block of kSweepBlock diagonals per array.  Strips hand their
+//    boundary row to the next strip through a release flag.  Every cell runs
+//    exactly the reference's arithmetic in a dependency-respecting order, so
+//    the factor and the solves are bit-identical to the sequential loops.
+//  * Phases are separated by a grid barrier of this file.
+// Every wait is bounded: on timeout the status word gets FLAG_TIMEOUT, later
+// waits stop waiting, the kernel runs to its end and the host reports an error.
+#include <type_traits>
+
 #include "ifl_device.cuh"
 
 namespace ifl {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr long long kWaitLimit = 1ll << 22;  // ~1 s of polling
+constexpr int kB = kSweepBlock;
+constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of flag polling
+constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
 constexpr double kTau = 0.97, kSigma = 0.25, kTol = 1e-5;
 
 template <typename F>
 struct PcgArgs {
-    int w, h, P, nstrips;
+    SDIdx sd;
     const F *adiag, *ax, *ay;
     double *pc;
     F *pcf, *lx, *ly;
@@ -45,12 +56,44 @@ struct PcgArgs {
     double *partials;
     unsigned *barrier, *progress, *flags;
     PcgOut *out;
+    unsigned long long *iter_total;
     int mode, limit, pinned;
+    int stages, stage_bytes;
 };
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// 1-D bulk copy global -> shared (16-byte aligned, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
 
 __device__ __forceinline__ bool timed_out(const unsigned *flags) { return ld_volatile(flags) & FLAG_TIMEOUT; }
 
-// Grid barrier: arrival counter + generation word.
+// Grid barrier: arrival counter + generation word, bounded wait.
 __device__ void grid_barrier(unsigned *bar, unsigned *flags) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -114,146 +157,286 @@ __device__ double grid_reduce(const double *partials, int slot, bool is_max, dou
     return r;
 }
 
-template <typename T> __device__ __forceinline__ T shfl_up1(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
-
-template <typename T> __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
-
-// Products for the dot: exact FP64 products of the stored values.
+// FP64 dot-product accumulation of stored values (explicit FMA for FP32 data).
 __device__ __forceinline__ double dacc(double acc, double a, double b) { return acc + a * b; }
 __device__ __forceinline__ double dacc(double acc, float a, float b) { return fma((double)a, (double)b, acc); }
 
-// One 32-row strip of a wavefront sweep.
-// KIND 0: MIC(0) factor (FP64), KIND 1: forward solve L q = r,
-// KIND 2: backward solve L^T z = q (+ partial dot(z, r)).
-template <int KIND, typename F>
-__device__ void sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, double &dot) {
-    using V = typename std::conditional<KIND == 0, double, F>::type;
-    const int lane = threadIdx.x & 31;
-    const int w = A.w, h = A.h, P = A.P;
-    const int ys = s * 32 + lane;
-    const bool rowok = ys < h;
-    const int y = (KIND == 2) ? h - 1 - ys : ys;
-    const unsigned tag = sid << 16;
-    const V *out_below;
-    if constexpr (KIND == 0) out_below = A.pc;
-    else out_below = A.z;
-    V prev = V(0);
-    unsigned seen = 0;
-    const bool publish = (lane == 31) && (s + 1 < A.nstrips);
-    for (int t = 0; t < w + 31; ++t) {
-        const int xs = t - lane;
-        V below = shfl_up1(prev);
-        const bool active = rowok && xs >= 0 && xs < w;
-        const int x = (KIND == 2) ? w - 1 - xs : xs;
-        if (lane == 0 && s > 0 && active) {
-            if (seen <= (unsigned)xs) {
-                long long n = 0;
-                unsigned v;
-                for (;;) {
-                    v = ld_volatile(A.progress + s - 1);
-                    if (v >= tag + (unsigned)xs + 1u) break;
-                    if (++n > kWaitLimit || timed_out(A.flags)) {
-                        atomicOr(A.flags, FLAG_TIMEOUT);
-                        v = tag + (unsigned)w;
-                        break;
-                    }
-                }
-                __threadfence();
-                seen = v - tag;
-            }
-            const int yb = (KIND == 2) ? y + 1 : y - 1;
-            below = ld_cg(out_below + x + (size_t)yb * P);
-        }
-        V val = prev;
-        if (active) {
-            const size_t c = x + (size_t)y * P;
-            const uint8_t b = A.nb[c];
-            if (b & NB_SELF) {
-                if constexpr (KIND == 0) {
-                    // buildPreconditioner (3-conjugate-gradients/Fluid.cpp:253-269)
-                    const double diag = (double)A.adiag[c];
-                    double e = diag;
-                    if (b & NB_LEFT) {
-                        double px = (double)A.ax[c - 1] * prev;
-                        double py = (double)A.ay[c - 1] * prev;
-                        e = e - (px * px + kTau * px * py);
-                    }
-                    if (b & NB_DOWN) {
-                        double px = (double)A.ax[c - P] * below;
-                        double py = (double)A.ay[c - P] * below;
-                        e = e - (py * py + kTau * px * py);
-                    }
-                    if (e < kSigma * diag) e = diag;
-                    double pc = 1.0 / sqrt(e);
-                    A.pc[c] = pc;
-                    A.pcf[c] = (F)pc;
-                    A.lx[c] = (F)((double)A.ax[c] * pc);
-                    A.ly[c] = (F)((double)A.ay[c] * pc);
-                    val = pc;
-                } else if constexpr (KIND == 1) {
-                    // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
-                    F tt = A.r[c];
-                    if (b & NB_LEFT) tt = tt - A.lx[c - 1] * prev;
-                    if (b & NB_DOWN) tt = tt - A.ly[c - P] * below;
-                    val = tt * A.pcf[c];
-                    A.z[c] = val;
-                } else {
-                    // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
-                    F tt = A.z[c];
-                    if (b & NB_RIGHT) tt = tt - A.lx[c] * prev;
-                    if (b & NB_UP) tt = tt - A.ly[c] * below;
-                    val = tt * A.pcf[c];
-                    A.z[c] = val;
-                    if (b & NB_RED) dot = dacc(dot, val, A.r[c]);
-                }
-            }
-        }
-        prev = val;
-        if (publish && active && ((((xs + 1) & 15) == 0) || xs == w - 1)) {
-            __threadfence();
-            st_volatile(A.progress + s, tag + (unsigned)xs + 1u);
+// --------------------------------------------------------------- sweeps
+// Per-warp shared-memory ring: `stages` buffers of stage_bytes, each holding
+// kB diagonals (kB*32 slots) of up to five F arrays followed by the
+// neighbour-bit bytes.  ii / ci count issued / consumed blocks over the whole
+// kernel, so buffer = count % stages and mbarrier parity = (count/stages) & 1.
+struct Ring {
+    char *buf;
+    uint64_t *bars;
+    int stages, stage_bytes;
+    unsigned ii, ci;
+};
+
+// Bounded wait for the block that ci refers to.
+__device__ __forceinline__ void ring_wait(Ring &R, unsigned *flags) {
+    const unsigned st = R.ci % R.stages, parity = (R.ci / R.stages) & 1u;
+    long long n = 0;
+    while (!mbar_try_wait(R.bars + st, parity)) {
+        if (++n > kMbarWaitLimit || timed_out(flags)) {
+            atomicOr(flags, FLAG_TIMEOUT);
+            break;
         }
     }
+    R.ci++;
+}
+
+// Streams of one sweep kind: KIND 0 factor (adiag, ax, ay), 1 forward (r, lx,
+// ly, pcf), 2 backward (z, lx, ly, pcf, r); the neighbour bits always follow.
+template <int KIND, typename F>
+struct Streams {
+    static constexpr int n = KIND == 0 ? 3 : KIND == 1 ? 4 : 5;
+    const F *src[5];
+    __device__ explicit Streams(const PcgArgs<F> &A) {
+        if (KIND == 0) {
+            src[0] = A.adiag; src[1] = A.ax; src[2] = A.ay;
+        } else if (KIND == 1) {
+            src[0] = A.r; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf;
+        } else {
+            src[0] = A.z; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = A.r;
+        }
+        if (n < 5) src[n] = nullptr;
+    }
+};
+
+// Issue the bulk copies of diagonal block `blk` of strip s (lane 0 only).
+template <int KIND, typename F>
+__device__ __forceinline__ void ring_issue(Ring &R, const PcgArgs<F> &A, const Streams<KIND, F> &St, int s,
+                                           int blk) {
+    constexpr unsigned fbytes = kB * 32 * sizeof(F);
+    constexpr unsigned bbytes = kB * 32;
+    const int D = A.sd.D;
+    const int d0 = (KIND == 2) ? D - (blk + 1) * kB : blk * kB;
+    const size_t off = ((size_t)s * D + d0) * 32;
+    const unsigned st = R.ii % R.stages;
+    char *dst = R.buf + (size_t)st * R.stage_bytes;
+    uint64_t *bar = R.bars + st;
+    fence_proxy_async_smem();
+    mbar_expect_tx(bar, St.n * fbytes + bbytes);
+    for (int k = 0; k < St.n; k++) bulk_g2s(dst + k * fbytes, St.src[k] + off, fbytes, bar);
+    bulk_g2s(dst + 5 * fbytes, A.nb + off, bbytes, bar);
+    R.ii++;
+}
+
+// Wait until strip `src_strip` has published at least `need` (tagged) columns.
+__device__ __forceinline__ unsigned wait_progress(const unsigned *progress, int src_strip, unsigned need,
+                                                  unsigned *flags) {
+    long long n = 0;
+    unsigned v;
+    for (;;) {
+        v = ld_volatile(progress + src_strip);
+        if (v >= need) break;
+        if (++n > kWaitLimit || timed_out(flags)) {
+            atomicOr(flags, FLAG_TIMEOUT);
+            v = need;
+            break;
+        }
+    }
+    __threadfence();
+    return v;
+}
+
+// One strip of a wavefront sweep.  Returns the lane's partial dot(z, r) for
+// the backward solve.
+template <int KIND, typename F>
+__device__ double sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, Ring &R) {
+    using V = typename std::conditional<KIND == 0, double, F>::type;
+    constexpr unsigned fbytes = kB * 32 * sizeof(F);
+    const int lane = threadIdx.x & 31;
+    const SDIdx sd = A.sd;
+    const int W = sd.W, H = sd.H, D = sd.D, S = sd.S;
+    const int y = s * 32 + lane;
+    const bool rowok = y < H;
+    const unsigned tag = sid << 16;
+    const Streams<KIND, F> St(A);
+    const int nblk = D / kB;
+    // Backward sweeps run top strip first: lane 31 waits on strip s+1, lane 0 publishes.
+    const bool bwd = KIND == 2;
+    const int dep = bwd ? s + 1 : s - 1;
+    const bool has_dep = bwd ? (s + 1 < S) : (s > 0);
+    const bool waiter = bwd ? (lane == 31) : (lane == 0);
+    const bool publisher = (bwd ? (lane == 0) : (lane == 31)) && (bwd ? s > 0 : s + 1 < S);
+    unsigned seen = 0;
+    double dot = 0.0;
+
+    V prev = V(0);                  // result of the previous cell in sweep order
+    F prev_a = F(0), prev_b = F(0); // forward: lx, ly of that cell; factor: ax, ay
+
+    if (lane == 0) {
+        fence_proxy_async_global();  // generic-proxy writes before this sweep -> bulk copies
+        const int pro = nblk < R.stages - 1 ? nblk : R.stages - 1;
+        for (int b = 0; b < pro; b++) ring_issue<KIND, F>(R, A, St, s, b);
+    }
+    __syncwarp();
+    for (int blk = 0; blk < nblk; blk++) {
+        if (blk + R.stages - 1 < nblk) {
+            __syncwarp();
+            if (lane == 0) ring_issue<KIND, F>(R, A, St, s, blk + R.stages - 1);
+            else R.ii++;
+        }
+        const unsigned st = R.ci % R.stages;
+        ring_wait(R, A.flags);
+        const char *sb = R.buf + (size_t)st * R.stage_bytes;
+        const F *s0 = (const F *)sb;
+        const F *s1 = (const F *)(sb + fbytes);
+        const F *s2 = (const F *)(sb + 2 * fbytes);
+        const F *s3 = (const F *)(sb + 3 * fbytes);
+        const F *s4 = (const F *)(sb + 4 * fbytes);
+        const uint8_t *snb = (const uint8_t *)(sb + 5 * fbytes);
+#pragma unroll 4
+        for (int j = 0; j < kB; j++) {
+            const int t = blk * kB + j;
+            const int d = bwd ? D - 1 - t : t;
+            const int jj = bwd ? (kB - 1 - j) : j;
+            const int e = jj * 32 + lane;  // slot inside the staged block
+            const int x = d - lane;
+            const bool active = rowok && x >= 0 && x < W;
+            const size_t i = ((size_t)s * D + d) * 32 + lane;
+            const int xs = bwd ? W - 1 - x : x;  // sweep column
+            const uint8_t b = snb[e];
+            if constexpr (KIND == 0) {
+                // buildPreconditioner (3-conjugate-gradients/Fluid.cpp:253-269)
+                double pc_d = __shfl_up_sync(0xffffffffu, prev, 1);
+                F ax_d = __shfl_up_sync(0xffffffffu, prev_a, 1);
+                F ay_d = __shfl_up_sync(0xffffffffu, prev_b, 1);
+                const F axv = s1[e], ayv = s2[e];
+                V val = prev;
+                if (active && (b & NB_SELF)) {
+                    if (waiter && has_dep && (b & NB_DOWN)) {
+                        if (seen <= (unsigned)xs) seen = wait_progress(A.progress, dep, tag + xs + 1, A.flags) - tag;
+                        const size_t k = sd.slot(x, y - 1);
+                        pc_d = __ldcg(A.pc + k);
+                        ax_d = __ldcg(A.ax + k);
+                        ay_d = __ldcg(A.ay + k);
+                    }
+                    const double diag = (double)s0[e];
+                    double ev = diag;
+                    if (b & NB_LEFT) {
+                        double px = (double)prev_a * prev;
+                        double py = (double)prev_b * prev;
+                        ev = ev - (px * px + kTau * px * py);
+                    }
+                    if (b & NB_DOWN) {
+                        double px = (double)ax_d * pc_d;
+                        double py = (double)ay_d * pc_d;
+                        ev = ev - (py * py + kTau * px * py);
+                    }
+                    if (ev < kSigma * diag) ev = diag;
+                    const double pcv = 1.0 / sqrt(ev);
+                    A.pc[i] = pcv;
+                    A.pcf[i] = (F)pcv;
+                    A.lx[i] = (F)((double)axv * pcv);
+                    A.ly[i] = (F)((double)ayv * pcv);
+                    val = pcv;
+                }
+                prev = val;
+                prev_a = axv;
+                prev_b = ayv;
+            } else if constexpr (KIND == 1) {
+                // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
+                F q_d = __shfl_up_sync(0xffffffffu, prev, 1);
+                F ly_d = __shfl_up_sync(0xffffffffu, prev_b, 1);
+                const F lxv = s1[e], lyv = s2[e];
+                V val = prev;
+                if (active && (b & NB_SELF)) {
+                    if (waiter && has_dep && (b & NB_DOWN)) {
+                        if (seen <= (unsigned)xs) seen = wait_progress(A.progress, dep, tag + xs + 1, A.flags) - tag;
+                        const size_t k = sd.slot(x, y - 1);
+                        q_d = __ldcg(A.z + k);
+                        ly_d = __ldcg(A.ly + k);
+                    }
+                    F tt = s0[e];
+                    if (b & NB_LEFT) tt = tt - prev_a * prev;
+                    if (b & NB_DOWN) tt = tt - ly_d * q_d;
+                    val = tt * s3[e];
+                    A.z[i] = val;
+                }
+                prev = val;
+                prev_a = lxv;
+                prev_b = lyv;
+            } else {
+                // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
+                F z_u = __shfl_down_sync(0xffffffffu, prev, 1);
+                V val = prev;
+                if (active && (b & NB_SELF)) {
+                    if (waiter && has_dep && (b & NB_UP)) {
+                        if (seen <= (unsigned)xs) seen = wait_progress(A.progress, dep, tag + xs + 1, A.flags) - tag;
+                        z_u = __ldcg(A.z + sd.slot(x, y + 1));
+                    }
+                    F tt = s0[e];
+                    if (b & NB_RIGHT) tt = tt - s1[e] * prev;
+                    if (b & NB_UP) tt = tt - s2[e] * z_u;
+                    val = tt * s3[e];
+                    A.z[i] = val;
+                    if (b & NB_RED) dot = dacc(dot, val, s4[e]);
+                }
+                prev = val;
+            }
+            if (publisher && active && ((((xs + 1) & 7) == 0) || xs == W - 1)) {
+                __threadfence();
+                st_volatile(A.progress + s, tag + (unsigned)xs + 1u);
+            }
+        }
+    }
+    __syncwarp();
+    return dot;
 }
 
 template <int KIND, typename F>
-__device__ double sweep(const PcgArgs<F> &A, unsigned sid) {
-    const int warp = threadIdx.x >> 5;
-    const int total = gridDim.x * kWarps;
-    double dot = 0.0;
-    // strip s -> block s % G, warp s / G: consecutive strips on different SMs
-    for (int s = blockIdx.x + warp * gridDim.x; s < A.nstrips; s += total) sweep_strip<KIND, F>(A, s, sid, dot);
-    return dot;
+__device__ __forceinline__ double sweep(const PcgArgs<F> &A, unsigned sid, Ring &R, bool sweeper) {
+    if (!sweeper) return 0.0;
+    return sweep_strip<KIND, F>(A, blockIdx.x, sid, R);
 }
 
 template <typename F>
 __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
+    extern __shared__ __align__(128) char smem_raw[];
     __shared__ double sm[kWarps + 1];
-    const int w = A.w, h = A.h, P = A.P;
-    const int n = w * h;
-    const int gtid = blockIdx.x * kThreads + threadIdx.x;
-    const int gstride = gridDim.x * kThreads;
+    const SDIdx sd = A.sd;
+    const int W = sd.W, H = sd.H, D = sd.D;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rows = sd.S * D;  // diagonals of all strips
+    const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
+    const bool sweeper = warp == 0 && (int)blockIdx.x < sd.S;
     unsigned sid = 1;
 
+    Ring R;
+    R.bars = (uint64_t *)smem_raw;
+    R.buf = smem_raw + 128;
+    R.stages = A.stages;
+    R.stage_bytes = A.stage_bytes;
+    R.ii = R.ci = 0;
+    if (sweeper) {
+        if (lane == 0) {
+            for (int k = 0; k < R.stages; k++) mbar_init(R.bars + k, 1);
+            fence_mbar_init();
+        }
+        __syncwarp();
+    }
+
     if (A.mode & PCG_FACTOR) {
-        sweep<0, F>(A, sid++);
+        sweep<0, F>(A, sid++, R, sweeper);
         grid_barrier(A.barrier, A.flags);
     }
     if (!(A.mode & PCG_SOLVE)) return;
 
     // p = 0; maxError = |r|_inf   (3-conjugate-gradients/Fluid.cpp:350, 354)
     double mx = 0.0;
-    for (int i = gtid; i < n; i += gstride) {
-        int y = i / w, x = i - y * w;
-        size_t c = x + (size_t)y * P;
-        A.p[c] = F(0);
-        if (A.nb[c] & NB_RED) mx = smax(mx, (double)fabs(A.r[c]));
+    for (int row = gwarp; row < rows; row += nwarps) {
+        const size_t i = (size_t)row * 32 + lane;
+        A.p[i] = F(0);
+        if (A.nb[i] & NB_RED) mx = smax(mx, (double)fabs(A.r[i]));
     }
     block_store(mx, true, A.partials, 0, sm);
     // z = M^-1 r  (:351)
-    sweep<1, F>(A, sid++);
+    sweep<1, F>(A, sid++, R, sweeper);
     grid_barrier(A.barrier, A.flags);
-    double d = sweep<2, F>(A, sid++);
+    double d = sweep<2, F>(A, sid++, R, sweeper);
     block_store(d, false, A.partials, 2, sm);
     grid_barrier(A.barrier, A.flags);
 
@@ -268,25 +451,34 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
         F *s_old = A.sa, *s_new = A.sb;
         for (int iter = 0; iter < A.limit; iter++) {
             if (timed_out(A.flags)) break;
-            // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s
+            // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
             double dacc_ = 0.0;
             const F fbeta = (F)beta;
-            for (int i = gtid; i < n; i += gstride) {
-                int y = i / w, x = i - y * w;
-                size_t c = x + (size_t)y * P;
+            for (int row = gwarp; row < rows; row += nwarps) {
+                const int s = row / D, dd = row - s * D;
+                const int x = dd - lane, y = s * 32 + lane;
+                const size_t i = (size_t)row * 32 + lane;
+                if (x < 0 || x >= W || y >= H) {
+                    s_new[i] = F(0);
+                    A.as[i] = F(0);
+                    continue;
+                }
                 auto snew = [&](size_t k) -> F {
                     if (iter == 0) return A.z[k];
                     return (A.nb[k] & NB_RED) ? F(A.z[k] + s_old[k] * fbeta) : s_old[k];
                 };
-                F sc = snew(c);
-                F t = A.adiag[c] * sc;
-                if (x > 0) t += A.ax[c - 1] * snew(c - 1);
-                if (y > 0) t += A.ay[c - P] * snew(c - P);
-                if (x < w - 1) t += A.ax[c] * snew(c + 1);
-                if (y < h - 1) t += A.ay[c] * snew(c + P);
-                s_new[c] = sc;
-                A.as[c] = t;
-                if (A.nb[c] & NB_RED) dacc_ = dacc(dacc_, t, sc);
+                const F sc = snew(i);
+                F t = A.adiag[i] * sc;
+                if (x > 0) t += A.ax[i - 32] * snew(i - 32);
+                if (y > 0) {
+                    const size_t k = lane > 0 ? i - 33 : sd.slot(x, y - 1);
+                    t += A.ay[k] * snew(k);
+                }
+                if (x < W - 1) t += A.ax[i] * snew(i + 32);
+                if (y < H - 1) t += A.ay[i] * snew(lane < 31 ? i + 33 : sd.slot(x, y + 1));
+                s_new[i] = sc;
+                A.as[i] = t;
+                if (A.nb[i] & NB_RED) dacc_ = dacc(dacc_, t, sc);
             }
             block_store(dacc_, false, A.partials, 1, sm);
             grid_barrier(A.barrier, A.flags);
@@ -294,13 +486,12 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
             const F falpha = (F)alpha, fnalpha = (F)(-alpha);
             mx = 0.0;
-            for (int i = gtid; i < n; i += gstride) {
-                int y = i / w, x = i - y * w;
-                size_t c = x + (size_t)y * P;
-                if (A.nb[c] & NB_RED) {
-                    A.p[c] = A.p[c] + s_new[c] * falpha;
-                    F rn = A.r[c] + A.as[c] * fnalpha;
-                    A.r[c] = rn;
+            for (int row = gwarp; row < rows; row += nwarps) {
+                const size_t i = (size_t)row * 32 + lane;
+                if (A.nb[i] & NB_RED) {
+                    A.p[i] = A.p[i] + s_new[i] * falpha;
+                    const F rn = A.r[i] + A.as[i] * fnalpha;
+                    A.r[i] = rn;
                     mx = smax(mx, (double)fabs(rn));
                 }
             }
@@ -313,9 +504,9 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
                 break;
             }
             // z = M^-1 r; sigmaNew = z.r  (:372-376)
-            sweep<1, F>(A, sid++);
+            sweep<1, F>(A, sid++, R, sweeper);
             grid_barrier(A.barrier, A.flags);
-            d = sweep<2, F>(A, sid++);
+            d = sweep<2, F>(A, sid++, R, sweeper);
             block_store(d, false, A.partials, 2, sm);
             grid_barrier(A.barrier, A.flags);
             const double sigmaNew = grid_reduce(A.partials, 2, false, sm);
@@ -331,7 +522,21 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
         A.out->iterations = iterations;
         A.out->status = status;
         A.out->max_error = maxError;
+        atomicAdd(A.iter_total, (unsigned long long)iterations);
     }
+}
+
+template <typename F>
+int ring_stages() {
+    return sizeof(F) == 8 ? 3 : 4;
+}
+template <typename F>
+int ring_stage_bytes() {
+    return kB * 32 * (5 * (int)sizeof(F) + 1);
+}
+template <typename F>
+size_t smem_bytes() {
+    return 128 + (size_t)ring_stages<F>() * ring_stage_bytes<F>();
 }
 
 template <typename F>
@@ -341,7 +546,8 @@ int max_coresident() {
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel<F>, kThreads, 0);
+        cudaFuncSetAttribute(pcg_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<F>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel<F>, kThreads, smem_bytes<F>());
         cached = sms * (per > 2 ? 2 : per);
     }
     return cached;
@@ -358,10 +564,7 @@ template <typename F>
 cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &cfg, cudaStream_t st,
                        int *blocks_used) {
     PcgArgs<F> A;
-    A.w = S.w;
-    A.h = S.h;
-    A.P = S.P;
-    A.nstrips = (S.h + 31) / 32;
+    A.sd = S.sd;
     A.adiag = S.adiag;
     A.ax = S.ax;
     A.ay = S.ay;
@@ -381,20 +584,25 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     A.progress = X.progress;
     A.flags = S.flags;
     A.out = X.out + (cfg.heat ? 1 : 0);
+    A.iter_total = X.iter_total;
     A.mode = cfg.mode;
     A.limit = cfg.limit;
     A.pinned = cfg.pinned;
+    A.stages = ring_stages<F>();
+    A.stage_bytes = ring_stage_bytes<F>();
     int maxb = max_coresident<F>();
     if (maxb > X.max_blocks) maxb = X.max_blocks;
-    int want = (S.w * S.h + kThreads * 4 - 1) / (kThreads * 4);
-    if (want < A.nstrips) want = A.nstrips;
+    if (maxb < S.sd.S) return cudaErrorInvalidConfiguration;  // one block per 32-row strip
+    const long long slots = (long long)S.sd.total();
+    int want = (int)((slots + kThreads * 4 - 1) / (kThreads * 4));
+    if (want < S.sd.S) want = S.sd.S;
     int G = want < maxb ? want : maxb;
-    if (G < 1) G = 1;
     if (blocks_used) *blocks_used = G;
     cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
-    cudaMemsetAsync(X.progress, 0, (size_t)A.nstrips * sizeof(unsigned), st);
+    cudaMemsetAsync(X.progress, 0, (size_t)S.sd.S * sizeof(unsigned), st);
     void *args[] = {&A};
-    return cudaLaunchCooperativeKernel((const void *)pcg_kernel<F>, dim3(G), dim3(kThreads), args, 0, st);
+    return cudaLaunchCooperativeKernel((const void *)pcg_kernel<F>, dim3(G), dim3(kThreads), args,
+                                       smem_bytes<F>(), st);
 }
 
 template cudaError_t launch_pcg<double>(const Scene<double> &, const PcgScratch &, const PcgConfig &,

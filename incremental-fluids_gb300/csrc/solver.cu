@@ -42,6 +42,7 @@ class SolverImpl final : public SolverBase {
 
     int init() override {
         const int w = prm_.w, h = prm_.h;
+        if (check(cudaSetDevice(prm_.device), "set device")) return IFL_ERR_CUDA;
         P_ = (int)align_up((size_t)w + 2, 32);
         rows_ = h + 2;
         nq_ = prm_.variant >= IFL_HEAT ? 4 : 3;
@@ -90,7 +91,9 @@ class SolverImpl final : public SolverBase {
         const double val[4] = {d, t, u, v};
         for (int q = 0; q < 4; q++) {
             if (!present(q)) continue;
+            int t = tbegin(IFL_K_FACES);
             launch_inflow<F>(S_, q, x, y, x + w, y + h, val[q], stream_);
+            tend(t);
             launches_++;
         }
         return launch_check("inflow");
@@ -102,7 +105,9 @@ class SolverImpl final : public SolverBase {
         case IFL_PH_FILL_SOLID:
             if (var >= IFL_SOLID && !bodies_.empty()) {
                 if (int e = upload_bodies()) return e;
+                int t = tbegin(IFL_K_SOLID);
                 launch_fill_solid<F>(S_, stream_);
+                tend(t);
                 launches_ += var >= IFL_CURVED ? 2 : 1;
             }
             break;
@@ -114,13 +119,17 @@ class SolverImpl final : public SolverBase {
             break;
         case IFL_PH_BUOYANCY:
             if (var >= IFL_HEAT) {
+                int t = tbegin(IFL_K_FACES);
                 launch_buoyancy<F>(S_, dt, stream_);
+                tend(t);
                 launches_++;
             }
             break;
         case IFL_PH_BC:
             if (var >= IFL_SOLID) {
+                int t = tbegin(IFL_K_FACES);
                 launch_bc<F>(S_, stream_);
+                tend(t);
                 launches_++;
             }
             break;
@@ -131,19 +140,25 @@ class SolverImpl final : public SolverBase {
         case IFL_PH_MATRIX: assemble(dt, ASM_MATRIX); break;
         case IFL_PH_PRECON: return pcg(PCG_FACTOR, false);
         case IFL_PH_PROJECT: return pcg(PCG_SOLVE, false);
-        case IFL_PH_APPLY_P:
+        case IFL_PH_APPLY_P: {
+            int t = tbegin(IFL_K_FACES);
             launch_apply_pressure<F>(S_, dt, stream_);
+            tend(t);
             launches_++;
             break;
+        }
         case IFL_PH_EXTRAP_DUV:
             if (var >= IFL_SOLID) extrapolate((1u << 0) | (1u << 2) | (1u << 3));
             break;
-        case IFL_PH_ADVECT:
+        case IFL_PH_ADVECT: {
+            int t = tbegin(IFL_K_ADVECT);
             launch_advect<F>(S_, dt, stream_);
+            tend(t);
             launches_++;
             for (int q = 0; q < 4; q++)
                 if (present(q)) std::swap(S_.q[q].src, S_.q[q].dst);
             break;
+        }
         default: return IFL_ERR_ARG;
         }
         return launch_check("phase");
@@ -177,13 +192,17 @@ class SolverImpl final : public SolverBase {
     }
 
     // ------------------------------------------------------ field access
-    int field_info(int field, void **ptr, int *elem, int *w, int *h) const override {
+    SDIdx sd_index() const override { return S_.sd; }
+
+    int field_info(int field, void **ptr, int *elem, int *w, int *h, int *sd) const override {
         const int W = prm_.w, H = prm_.h;
         *w = W;
         *h = H;
+        *sd = 0;
         const int fe = sizeof(F) == 8 ? IFL_DT_F64 : IFL_DT_F32;
         if (field >= IFL_F_R && field <= IFL_F_VDENS) {
             *elem = fe;
+            *sd = field <= IFL_F_APLUSY ? 1 : 0;
             switch (field) {
             case IFL_F_R: *ptr = S_.r; return 0;
             case IFL_F_P: *ptr = S_.p; return 0;
@@ -236,6 +255,16 @@ class SolverImpl final : public SolverBase {
         return IFL_OK;
     }
 
+    int read_iteration_total(long long *out) override {
+        unsigned long long v = 0;
+        if (check(cudaMemcpyAsync(&v, scratch_.iter_total, 8, cudaMemcpyDeviceToHost, stream_), "iter total") ||
+            check(cudaMemsetAsync(scratch_.iter_total, 0, 8, stream_), "iter reset") ||
+            check(cudaStreamSynchronize(stream_), "iter sync"))
+            return IFL_ERR_CUDA;
+        *out = (long long)v;
+        return IFL_OK;
+    }
+
     size_t pitch() const override { return (size_t)P_; }
     size_t device_bytes() const override { return arena_bytes_; }
 
@@ -245,6 +274,8 @@ class SolverImpl final : public SolverBase {
     void carve(char *base, Carver &c) {
         const size_t N = (size_t)P_ * rows_;
         const bool geo = prm_.variant >= IFL_SOLID;
+        S_.sd = SDIdx::make(prm_.w, prm_.h);
+        const size_t NS = S_.sd.total();
         S_.variant = prm_.variant;
         S_.w = prm_.w;
         S_.h = prm_.h;
@@ -280,20 +311,20 @@ class SolverImpl final : public SolverBase {
                 Q.list = c.take<int>(base, 2 * N);
             }
         }
-        S_.r = c.take<F>(base, N);
-        S_.p = c.take<F>(base, N);
-        S_.z = c.take<F>(base, N);
-        S_.sa = c.take<F>(base, N);
-        S_.sb = c.take<F>(base, N);
-        S_.as = c.take<F>(base, N);
-        S_.adiag = c.take<F>(base, N);
-        S_.ax = c.take<F>(base, N);
-        S_.ay = c.take<F>(base, N);
-        S_.lx = c.take<F>(base, N);
-        S_.ly = c.take<F>(base, N);
-        S_.pcf = c.take<F>(base, N);
-        S_.pc = c.take<double>(base, N);
-        S_.nb = c.take<uint8_t>(base, N);
+        S_.r = c.take<F>(base, NS);
+        S_.p = c.take<F>(base, NS);
+        S_.z = c.take<F>(base, NS);
+        S_.sa = c.take<F>(base, NS);
+        S_.sb = c.take<F>(base, NS);
+        S_.as = c.take<F>(base, NS);
+        S_.adiag = c.take<F>(base, NS);
+        S_.ax = c.take<F>(base, NS);
+        S_.ay = c.take<F>(base, NS);
+        S_.lx = c.take<F>(base, NS);
+        S_.ly = c.take<F>(base, NS);
+        S_.pcf = c.take<F>(base, NS);
+        S_.pc = c.take<double>(base, NS);
+        S_.nb = c.take<uint8_t>(base, NS);
         if (prm_.variant == IFL_VARDENS) {
             S_.udens = c.take<F>(base, N);
             S_.vdens = c.take<F>(base, N);
@@ -307,13 +338,21 @@ class SolverImpl final : public SolverBase {
         scratch_.max_blocks = max_blocks_;
         scratch_.partials = c.take<double>(base, 4 * (size_t)std::max(max_blocks_, 1));
         scratch_.barrier = c.take<unsigned>(base, 2);
-        scratch_.progress = c.take<unsigned>(base, (size_t)(prm_.h + 31) / 32 + 1);
+        scratch_.progress = c.take<unsigned>(base, (size_t)S_.sd.S + 1);
         scratch_.out = c.take<PcgOut>(base, 2);
+        scratch_.iter_total = c.take<unsigned long long>(base, 1);
     }
 
     int upload_bodies() {
         if (!bodies_dirty_) return IFL_OK;
-        std::vector<DevBody> db(bodies_.size());
+        if (!staging_) {
+            if (check(cudaMallocHost((void **)&staging_, 256 * sizeof(DevBody)), "pinned staging") ||
+                check(cudaEventCreateWithFlags(&staging_done_, cudaEventDisableTiming), "staging event"))
+                return IFL_ERR_CUDA;
+        } else if (check(cudaEventSynchronize(staging_done_), "staging wait")) {
+            return IFL_ERR_CUDA;  // the previous upload must have left the buffer
+        }
+        DevBody *db = staging_;
         for (size_t i = 0; i < bodies_.size(); i++) {
             const ifl_body &b = bodies_[i];
             DevBody &d = db[i];
@@ -331,25 +370,28 @@ class SolverImpl final : public SolverBase {
             d.cneg = std::cos(-b.theta);
             d.sneg = std::sin(-b.theta);
         }
-        if (check(cudaMemcpyAsync(d_bodies_, db.data(), db.size() * sizeof(DevBody), cudaMemcpyHostToDevice,
+        if (check(cudaMemcpyAsync(d_bodies_, db, bodies_.size() * sizeof(DevBody), cudaMemcpyHostToDevice,
                                   stream_),
-                  "bodies"))
+                  "bodies") ||
+            check(cudaEventRecord(staging_done_, stream_), "staging record"))
             return IFL_ERR_CUDA;
-        // pageable source: make sure the copy has been taken before db dies
-        if (check(cudaStreamSynchronize(stream_), "bodies sync")) return IFL_ERR_CUDA;
         S_.nbodies = (int)bodies_.size();
         bodies_dirty_ = false;
         return IFL_OK;
     }
 
     void assemble(double dt, int what) {
+        int t = tbegin(IFL_K_ASSEMBLE);
         launch_assemble<F>(S_, dt, what, stream_);
+        tend(t);
         launches_++;
     }
 
     void extrapolate(unsigned qmask) {
         if (prm_.variant < IFL_SOLID) return;
+        int t = tbegin(IFL_K_EXTRAPOLATE);
         launch_extrapolate<F>(S_, qmask, stream_);
+        tend(t);
         launches_ += 2;
     }
 
@@ -357,24 +399,29 @@ class SolverImpl final : public SolverBase {
         PcgConfig cfg;
         cfg.mode = mode;
         cfg.limit = heat ? prm_.max_iter_heat : prm_.max_iter_pressure;
-        cfg.pinned = pinned_;
+        cfg.pinned = heat ? pinned_heat_ : pinned_;
         cfg.heat = heat ? 1 : 0;
         int G = 0;
-        if (check(launch_pcg<F>(S_, scratch_, cfg, stream_, &G), "pcg launch")) return IFL_ERR_CUDA;
+        int t = tbegin(IFL_K_PCG);
+        cudaError_t e = launch_pcg<F>(S_, scratch_, cfg, stream_, &G);
+        tend(t);
+        if (check(e, "pcg launch")) return IFL_ERR_CUDA;
         launches_++;
         return IFL_OK;
     }
 
     // r = T; heat matrix; MIC(0); PCG; T = p  (7-variable-density/Fluid.cpp:1001-1005)
     int heat_solve(double dt) {
+        int t = tbegin(IFL_K_ASSEMBLE);
         launch_heat_assemble<F>(S_, dt, stream_);
+        tend(t);
         launches_++;
         if (int e = pcg(PCG_FACTOR | PCG_SOLVE, true)) return e;
-        if (check(cudaMemcpy2DAsync(S_.q[1].src, (size_t)P_ * sizeof(F), S_.p, (size_t)P_ * sizeof(F),
-                                    (size_t)prm_.w * sizeof(F), prm_.h, cudaMemcpyDeviceToDevice, stream_),
-                  "T = p"))
-            return IFL_ERR_CUDA;
-        return IFL_OK;
+        t = tbegin(IFL_K_ASSEMBLE);
+        launch_sd_copy<F>(S_, S_.q[1].src, S_.p, 0, stream_);
+        tend(t);
+        launches_++;
+        return launch_check("T = p");
     }
 
     int launch_check(const char *what) {
@@ -382,6 +429,12 @@ class SolverImpl final : public SolverBase {
     }
 
     void release() {
+        if (stream_) cudaStreamSynchronize(stream_);
+        release_timing();
+        if (staging_) cudaFreeHost(staging_);
+        staging_ = nullptr;
+        if (staging_done_) cudaEventDestroy(staging_done_);
+        staging_done_ = nullptr;
         if (arena_) cudaFree(arena_);
         arena_ = nullptr;
         if (own_stream_ && stream_) cudaStreamDestroy(stream_);
@@ -391,12 +444,69 @@ class SolverImpl final : public SolverBase {
     Scene<F> S_{};
     PcgScratch scratch_{};
     DevBody *d_bodies_ = nullptr;
+    DevBody *staging_ = nullptr;  // pinned host copy of the body table
+    cudaEvent_t staging_done_ = nullptr;
     void *arena_ = nullptr;
     size_t arena_bytes_ = 0;
     int P_ = 0, rows_ = 0, nq_ = 3, max_blocks_ = 1;
 };
 
 // ------------------------------------------------------------ SolverBase
+int SolverBase::tbegin(int group) {
+    if (!timing_on_ || recs_.size() >= 1u << 16) return -1;
+    TimedRec r;
+    r.group = group;
+    for (cudaEvent_t *ev : {&r.start, &r.stop}) {
+        if (!event_pool_.empty()) {
+            *ev = event_pool_.back();
+            event_pool_.pop_back();
+        } else if (cudaEventCreate(ev) != cudaSuccess) {
+            return -1;
+        }
+    }
+    cudaEventRecord(r.start, stream_);
+    recs_.push_back(r);
+    return (int)recs_.size() - 1;
+}
+
+void SolverBase::tend(int rec) {
+    if (rec >= 0) cudaEventRecord(recs_[rec].stop, stream_);
+}
+
+int SolverBase::set_timing(bool on) {
+    timing_on_ = on;
+    return IFL_OK;
+}
+
+int SolverBase::get_timing(ifl_timing *out) {
+    std::memset(out, 0, sizeof *out);
+    if (check(cudaStreamSynchronize(stream_), "timing sync")) return IFL_ERR_CUDA;
+    for (TimedRec &r : recs_) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.start, r.stop) == cudaSuccess) {
+            out->ms[r.group] += ms;
+            out->launches[r.group]++;
+        }
+        event_pool_.push_back(r.start);
+        event_pool_.push_back(r.stop);
+    }
+    recs_.clear();
+    long long it = 0;
+    if (int e = read_iteration_total(&it)) return e;
+    out->pcg_iterations = it;
+    return IFL_OK;
+}
+
+void SolverBase::release_timing() {
+    for (TimedRec &r : recs_) {
+        event_pool_.push_back(r.start);
+        event_pool_.push_back(r.stop);
+    }
+    recs_.clear();
+    for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
+    event_pool_.clear();
+}
+
 bool SolverBase::check(cudaError_t e, const char *what) {
     if (e == cudaSuccess) return false;
     err_ = std::string(what) + ": " + cudaGetErrorString(e);
@@ -423,10 +533,24 @@ int SolverBase::advance_bodies(double dt) {
     return IFL_OK;
 }
 
+namespace {
+// Dense row-major <-> strip-diagonal permutation on the host (field transfer only).
+void sd_gather(const SDIdx &sd, const char *sdbuf, char *dense, size_t es) {
+    for (int y = 0; y < sd.H; y++)
+        for (int x = 0; x < sd.W; x++)
+            std::memcpy(dense + ((size_t)x + (size_t)y * sd.W) * es, sdbuf + sd.slot(x, y) * es, es);
+}
+void sd_scatter(const SDIdx &sd, const char *dense, char *sdbuf, size_t es) {
+    for (int y = 0; y < sd.H; y++)
+        for (int x = 0; x < sd.W; x++)
+            std::memcpy(sdbuf + sd.slot(x, y) * es, dense + ((size_t)x + (size_t)y * sd.W) * es, es);
+}
+}  // namespace
+
 int SolverBase::read_field(int field, void *host, size_t bytes, int dtype) {
     void *ptr;
-    int elem, w, h;
-    if (int e = field_info(field, &ptr, &elem, &w, &h)) return e;
+    int elem, w, h, sdl;
+    if (int e = field_info(field, &ptr, &elem, &w, &h, &sdl)) return e;
     const size_t n = (size_t)w * h;
     const size_t out_es = dtype == IFL_DT_F64 ? 8 : dtype == IFL_DT_F32 ? 4 : dtype == IFL_DT_U8 ? 1 : 0;
     if (!out_es || !host || bytes < n * out_es) return IFL_ERR_ARG;
@@ -434,14 +558,24 @@ int SolverBase::read_field(int field, void *host, size_t bytes, int dtype) {
     const size_t es = elem == IFL_DT_F64 ? 8 : elem == IFL_DT_F32 ? 4 : 1;
     std::vector<char> tmp;
     void *dst = host;
-    if (elem != dtype) {
+    if (elem != dtype || sdl) {
         tmp.resize(n * es);
         dst = tmp.data();
     }
-    if (check(cudaMemcpy2DAsync(dst, w * es, ptr, pitch() * es, w * es, h, cudaMemcpyDeviceToHost, stream()),
-              "read field") ||
-        check(cudaStreamSynchronize(stream()), "read sync"))
+    if (sdl) {
+        const SDIdx sd = sd_index();
+        std::vector<char> raw(sd.total() * es);
+        if (check(cudaMemcpyAsync(raw.data(), ptr, raw.size(), cudaMemcpyDeviceToHost, stream()), "read field") ||
+            check(cudaStreamSynchronize(stream()), "read sync"))
+            return IFL_ERR_CUDA;
+        sd_gather(sd, raw.data(), (char *)dst, es);
+        if (elem == dtype) std::memcpy(host, dst, n * es);
+    } else if (check(cudaMemcpy2DAsync(dst, w * es, ptr, pitch() * es, w * es, h, cudaMemcpyDeviceToHost,
+                                       stream()),
+                     "read field") ||
+               check(cudaStreamSynchronize(stream()), "read sync")) {
         return IFL_ERR_CUDA;
+    }
     if (elem != dtype) {
         if (elem == IFL_DT_F64) {
             const double *s = (const double *)dst;
@@ -458,8 +592,8 @@ int SolverBase::read_field(int field, void *host, size_t bytes, int dtype) {
 
 int SolverBase::write_field(int field, const void *host, size_t bytes, int dtype) {
     void *ptr;
-    int elem, w, h;
-    if (int e = field_info(field, &ptr, &elem, &w, &h)) return e;
+    int elem, w, h, sdl;
+    if (int e = field_info(field, &ptr, &elem, &w, &h, &sdl)) return e;
     const size_t n = (size_t)w * h;
     const size_t in_es = dtype == IFL_DT_F64 ? 8 : dtype == IFL_DT_F32 ? 4 : dtype == IFL_DT_U8 ? 1 : 0;
     if (!in_es || !host || bytes < n * in_es) return IFL_ERR_ARG;
@@ -479,6 +613,15 @@ int SolverBase::write_field(int field, const void *host, size_t bytes, int dtype
             for (size_t i = 0; i < n; i++) o[i] = (float)s[i];
         }
         src = tmp.data();
+    }
+    if (sdl) {
+        const SDIdx sd = sd_index();
+        std::vector<char> raw(sd.total() * es, 0);
+        sd_scatter(sd, (const char *)src, raw.data(), es);
+        if (check(cudaMemcpyAsync(ptr, raw.data(), raw.size(), cudaMemcpyHostToDevice, stream()), "write field") ||
+            check(cudaStreamSynchronize(stream()), "write sync"))
+            return IFL_ERR_CUDA;
+        return IFL_OK;
     }
     if (check(cudaMemcpy2DAsync(ptr, pitch() * es, src, w * es, w * es, h, cudaMemcpyHostToDevice, stream()),
               "write field") ||

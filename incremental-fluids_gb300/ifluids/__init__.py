@@ -37,6 +37,7 @@ EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", 
            "ifl_advance_bodies", "ifl_add_inflow", "ifl_update", "ifl_run_phase", "ifl_ambient_t",
            "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_flip", "ifl_get_stats",
            "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
+           "ifl_set_timing", "ifl_get_timing",
            "ifl_last_error", "ifl_version")
 
 
@@ -52,7 +53,16 @@ _NAMED = {"d": field_id(Q_D, A_SRC), "t": field_id(Q_T, A_SRC), "u": field_id(Q_
 class Params(C.Structure):
     _fields_ = [("variant", C.c_int32), ("w", C.c_int32), ("h", C.c_int32), ("precision", C.c_int32),
                 ("density_air", C.c_double), ("density_soot", C.c_double), ("diffusion", C.c_double),
-                ("max_iter_pressure", C.c_int32), ("max_iter_heat", C.c_int32), ("stream", C.c_void_p)]
+                ("max_iter_pressure", C.c_int32), ("max_iter_heat", C.c_int32), ("stream", C.c_void_p),
+                ("device", C.c_int32), ("pad_", C.c_int32)]
+
+
+K_PCG, K_ASSEMBLE, K_ADVECT, K_SOLID, K_EXTRAPOLATE, K_FACES = range(6)
+K_NAMES = ("pcg", "assemble", "advect", "solid", "extrapolate", "faces")
+
+
+class Timing(C.Structure):
+    _fields_ = [("ms", C.c_double * 6), ("launches", C.c_int64 * 6), ("pcg_iterations", C.c_int64)]
 
 
 class _CBody(C.Structure):
@@ -105,8 +115,10 @@ def load_library(path: str = LIB_PATH):
     L.ifl_write_field.argtypes = [vp, i, vp, sz, i]
     L.ifl_flip.argtypes = [vp, i]
     L.ifl_get_stats.argtypes = [vp, C.POINTER(StepStats)]
-    L.ifl_set_pinned_iterations.argtypes = [vp, i]
+    L.ifl_set_pinned_iterations.argtypes = [vp, i, i]
     L.ifl_synchronize.argtypes = [vp]
+    L.ifl_set_timing.argtypes = [vp, i]
+    L.ifl_get_timing.argtypes = [vp, C.POINTER(Timing)]
     L.ifl_stream.argtypes = [vp]
     L.ifl_stream.restype = vp
     L.ifl_launch_count.argtypes = [vp]
@@ -174,7 +186,7 @@ class FluidSolver:
 
     def __init__(self, w: int, h: int, *args, variant: Optional[int] = None, precision: int = FP64,
                  max_iter_pressure: Optional[int] = None, max_iter_heat: Optional[int] = None,
-                 stream: Optional[int] = None):
+                 stream: Optional[int] = None, device: int = 0):
         self._L = load_library()
         bodies: Sequence = ()
         soot = diffusion = None
@@ -204,6 +216,7 @@ class FluidSolver:
         if max_iter_heat is not None:
             p.max_iter_heat = int(max_iter_heat)
         p.stream = stream
+        p.device = int(device)
         h_ = C.c_void_p()
         rc = self._L.ifl_create(C.byref(p), C.byref(h_))
         if rc != OK:
@@ -281,10 +294,16 @@ class FluidSolver:
         self._check(self._L.ifl_field_shape(self._h, field, C.byref(w), C.byref(h)), "field_shape")
         return h.value, w.value
 
-    def read_field(self, field, dtype=np.float64) -> np.ndarray:
+    def read_field(self, field, dtype=np.float64, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Copy a field to the host (into `out` when given, e.g. a pinned buffer)."""
         fid = _NAMED[field] if isinstance(field, str) else int(field)
         h, w = self.shape(fid)
-        arr = np.empty((h, w), dtype=dtype)
+        if out is not None:
+            if out.shape != (h, w) or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous array of the field's shape")
+            arr, dtype = out, out.dtype
+        else:
+            arr = np.empty((h, w), dtype=dtype)
         code = {np.dtype(np.float64): DT_F64, np.dtype(np.float32): DT_F32, np.dtype(np.uint8): DT_U8}[
             np.dtype(dtype)]
         self._check(self._L.ifl_read_field(self._h, fid, arr.ctypes.data, arr.nbytes, code), "read_field")
@@ -303,14 +322,25 @@ class FluidSolver:
     def flip(self, quantity: int):
         self._check(self._L.ifl_flip(self._h, quantity), "flip")
 
-    def set_pinned_iterations(self, k: int):
-        self._check(self._L.ifl_set_pinned_iterations(self._h, k), "pinned")
+    def set_pinned_iterations(self, pressure: int, heat: int = -1):
+        """-1: stop on the residual test; k >= 0: run exactly k PCG iterations."""
+        self._check(self._L.ifl_set_pinned_iterations(self._h, pressure, heat), "pinned")
 
     def stats(self):
         st = StepStats()
         self._check(self._L.ifl_get_stats(self._h, C.byref(st)), "stats")
         return ((st.pressure.iterations, st.pressure.status, st.pressure.max_error),
                 (st.heat.iterations, st.heat.status, st.heat.max_error), st.device_flags)
+
+    def set_timing(self, on: bool = True):
+        self._check(self._L.ifl_set_timing(self._h, 1 if on else 0), "set_timing")
+
+    def timing(self):
+        """Device ms and launches per kernel group since the last call, and PCG iterations."""
+        t = Timing()
+        self._check(self._L.ifl_get_timing(self._h, C.byref(t)), "get_timing")
+        return ({n: t.ms[k] for k, n in enumerate(K_NAMES)},
+                {n: int(t.launches[k]) for k, n in enumerate(K_NAMES)}, int(t.pcg_iterations))
 
     def synchronize(self):
         self._check(self._L.ifl_synchronize(self._h), "synchronize")

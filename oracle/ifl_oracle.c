@@ -207,7 +207,7 @@ struct ifo_solver {
     double *r, *p, *z, *s, *precon, *adiag, *aplusx, *aplusy, *udens, *vdens;
     ifo_body bodies[256];
     int nbodies;
-    int pinned;
+    int pinned, pinned_heat;
     ifo_pcg_stats st_pressure, st_heat;
     int *stack;
 };
@@ -455,6 +455,7 @@ ifo_solver *ifo_create(int variant, int w, int h, double density_air,
     s->g = 9.81;
     s->hx = 1.0 / imin(w, h);
     s->pinned = -1;
+    s->pinned_heat = -1;
     s->st_pressure.status = IFO_PCG_INITIAL;
     s->st_heat.status = IFO_PCG_INITIAL;
     q_init(&s->q[IFO_QD], variant, w, h, 0.5, 0.5, s->hx);
@@ -759,7 +760,7 @@ static void matvec(const ifo_solver *s, double *dst, const double *b) {
 }
 
 /* project (PCG): 3-conjugate-gradients/Fluid.cpp:349-380 */
-static void project(ifo_solver *s, int limit, ifo_pcg_stats *st) {
+static void project(ifo_solver *s, int limit, int pinned, ifo_pcg_stats *st) {
     size_t n = (size_t)s->w * s->h;
     memset(s->p, 0, n * 8);
     apply_precon(s, s->z, s->r);
@@ -767,7 +768,7 @@ static void project(ifo_solver *s, int limit, ifo_pcg_stats *st) {
     double maxError = inf_norm(s, s->r);
     st->max_error = maxError;
     st->iterations = 0;
-    if (s->pinned >= 0 ? s->pinned == 0 : maxError < PCG_TOL) {
+    if (pinned >= 0 ? pinned == 0 : maxError < PCG_TOL) {
         st->status = IFO_PCG_INITIAL;
         return;
     }
@@ -780,7 +781,7 @@ static void project(ifo_solver *s, int limit, ifo_pcg_stats *st) {
         maxError = inf_norm(s, s->r);
         st->max_error = maxError;
         st->iterations = iter + 1;
-        if (s->pinned >= 0 ? iter + 1 >= s->pinned : maxError < PCG_TOL) {
+        if (pinned >= 0 ? iter + 1 >= pinned : maxError < PCG_TOL) {
             st->status = IFO_PCG_CONVERGED;
             return;
         }
@@ -866,7 +867,7 @@ static void heat_solve(ifo_solver *s, double dt) {
     memcpy(s->r, s->q[IFO_QT].src, n * 8);
     build_heat_matrix(s, dt);
     build_precon(s);
-    project(s, 2000, &s->st_heat);
+    project(s, 2000, s->pinned_heat, &s->st_heat);
     memcpy(s->q[IFO_QT].src, s->p, n * 8);
 }
 
@@ -894,7 +895,7 @@ void ifo_phase(ifo_solver *s, int phase, double dt) {
     case IFO_PH_DENSITIES: if (v == IFO_VARDENS) compute_densities(s); break;
     case IFO_PH_MATRIX: build_matrix(s, dt); break;
     case IFO_PH_PRECON: build_precon(s); break;
-    case IFO_PH_PROJECT: project(s, v == IFO_PLAIN ? 600 : 2000, &s->st_pressure); break;
+    case IFO_PH_PROJECT: project(s, v == IFO_PLAIN ? 600 : 2000, s->pinned, &s->st_pressure); break;
     case IFO_PH_APPLY_P: apply_pressure(s, dt); break;
     case IFO_PH_EXTRAP_DUV:
         if (v < IFO_SOLID) break;
@@ -945,7 +946,10 @@ void ifo_update(ifo_solver *s, double dt) {
     ifo_phase(s, IFO_PH_ADVECT, dt);
 }
 
-void ifo_set_pinned_iterations(ifo_solver *s, int k) { s->pinned = k; }
+void ifo_set_pinned_iterations(ifo_solver *s, int pressure, int heat) {
+    s->pinned = pressure;
+    s->pinned_heat = heat;
+}
 
 void ifo_get_stats(const ifo_solver *s, ifo_pcg_stats *pressure, ifo_pcg_stats *heat) {
     if (pressure) *pressure = s->st_pressure;

@@ -94,7 +94,7 @@ void ifo_phase(ifo_solver *s, int phase, double dt);
 /* -1: stop on the 1e-5 residual test (the reference); k >= 0: run exactly k
  * iterations (pinned mode, for separating rounding drift from a flip of the
  * termination test). */
-void ifo_set_pinned_iterations(ifo_solver *s, int k);
+void ifo_set_pinned_iterations(ifo_solver *s, int pressure, int heat);
 void ifo_get_stats(const ifo_solver *s, ifo_pcg_stats *pressure, ifo_pcg_stats *heat);
 
 /* Direct access to internal arrays (for state upload / download in tests). */

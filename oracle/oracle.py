@@ -74,7 +74,7 @@ def _oracle_lib():
         L.ifo_add_inflow.argtypes = [vp] + [d] * 8
         L.ifo_update.argtypes = [vp, d]
         L.ifo_phase.argtypes = [vp, i, d]
-        L.ifo_set_pinned_iterations.argtypes = [vp, i]
+        L.ifo_set_pinned_iterations.argtypes = [vp, i, i]
         L.ifo_get_stats.argtypes = [vp, C.POINTER(_Stats), C.POINTER(_Stats)]
         L.ifo_array.restype = C.POINTER(C.c_double)
         L.ifo_array.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
@@ -146,8 +146,9 @@ class OracleSolver:
     def flip(self, q):
         self.L.ifo_flip(self.p, q)
 
-    def set_pinned_iterations(self, k: int):
-        self.L.ifo_set_pinned_iterations(self.p, k)
+    def set_pinned_iterations(self, pressure: int, heat: int = -1):
+        """-1: stop on the residual test; k >= 0: run exactly k PCG iterations."""
+        self.L.ifo_set_pinned_iterations(self.p, pressure, heat)
 
     def stats(self):
         a, b = _Stats(), _Stats()

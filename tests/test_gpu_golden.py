@@ -1,4 +1,10 @@
-"""CUDA path against the golden fixtures made from the reference itself."""
+"""CUDA path against the golden fixtures made from the reference itself.
+
+Each scene runs several whole update() calls from the zero state with the PCG
+pinned to the reference's own per-step iteration counts; the final fields
+must then agree to 1e-9 relative (what remains is FP64 rounding of the
+parallel dot products, carried through the steps).  Unpinned, the counts
+agree within one iteration (test_gpu_parity.py)."""
 import glob
 import importlib.util
 import os
@@ -32,8 +38,14 @@ def test_gpu_fp64_matches_golden(ifl, path):
         s = ifl.FluidSolver(w, h, 0.1, objs, variant=variant)
     else:
         s = ifl.FluidSolver(w, h, 0.1, 1.0, 0.01, objs, variant=variant)
+    ref_iters = g["iters"]
+    capped = (ref_iters[:, 1] == 2).any()
     iters = []
-    for _ in range(steps):
+    for step in range(steps):
+        if not capped:
+            # run exactly the reference's iteration counts: no termination flips,
+            # so the remaining differences are rounding only
+            s.set_pinned_iterations(int(ref_iters[step, 0]), int(ref_iters[step, 2]))
         if variant >= 6:
             s.addInflow(*inflow)
         else:
@@ -44,13 +56,10 @@ def test_gpu_fp64_matches_golden(ifl, path):
         (pi, ps, _), (hi, hs, _), flags = s.stats()
         assert flags & 1 == 0
         iters.append((pi, ps))
-    ref_iters = g["iters"][:, :2]
-    capped = (ref_iters[:, 1] == 2).any()
     if capped:
         # 2000 iterations of a stagnating solve amplify rounding; only the outcome is compared
         assert all(st == 2 for _, st in iters)
         return
-    assert np.abs(np.array(iters)[:, 0] - ref_iters[:, 0]).max() <= 1
     for key in ("d", "t", "u", "v", "p"):
         if key in g:
             a, b = s.read_field(key), g[key]

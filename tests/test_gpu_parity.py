@@ -108,6 +108,13 @@ def warm_oracle(variant, w, h, steps, inflow, bodies):
     return o
 
 
+def add_inflow(g, variant, inflow):
+    if variant >= 6:
+        g.addInflow(*inflow)
+    else:
+        g.addInflow(*inflow[:5], *inflow[6:])
+
+
 def src_dst(variant):
     return [(q, a) for q in quantities(variant) for a in (O.A_SRC, O.A_DST)]
 
@@ -120,7 +127,7 @@ def test_phases_bit_exact_fp64(ifl, case):
     upload(ifl, g, o, variant)
 
     o.add_inflow(*inflow)
-    g.addInflow(*inflow[:5], *inflow[5:]) if variant >= 6 else g.addInflow(*inflow[:5], *inflow[6:])
+    add_inflow(g, variant, inflow)
     assert_same(ifl, g, o, variant, "inflow", [(q, O.A_SRC) for q in quantities(variant)])
 
     geo = []
@@ -168,22 +175,30 @@ def test_phases_bit_exact_fp64(ifl, case):
 
 @pytest.mark.parametrize("case", CASES, ids=IDS)
 def test_trajectory_fp64(ifl, case):
-    """Whole update() calls from a zero state: fields stay within 1e-9 (PCG rounding only)."""
+    """Whole update() calls from a zero state.  Unpinned, the iteration counts agree
+    within one; pinned to the oracle's counts the fields stay within 1e-9."""
     variant, w, h, _, inflow, bodies = case
     o = O.OracleSolver(variant, w, h)
     if bodies:
         o.set_bodies(bodies)
     g = make_gpu(ifl, variant, w, h, bodies)
+    free = make_gpu(ifl, variant, w, h, bodies)
     for step in range(6):
         o.add_inflow(*inflow)
-        g.addInflow(*inflow[:5], *inflow[5:]) if variant >= 6 else g.addInflow(*inflow[:5], *inflow[6:])
-        g.set_bodies(o.bodies())
+        for s in (g, free):
+            add_inflow(s, variant, inflow)
+            s.set_bodies(o.bodies())
         o.update(DT)
+        (opi, _, _), (ohi, _, _) = o.stats()
+        g.set_pinned_iterations(opi, ohi)
         g.update(DT)
+        free.update(DT)
         o.advance_bodies(DT)
         (pi, ps, _), _, flags = g.stats()
         assert flags & 1 == 0
-        assert abs(pi - o.stats()[0][0]) <= 1, step
+        assert pi == opi
+        (fpi, _, _), _, fflags = free.stats()
+        assert fflags & 1 == 0 and abs(fpi - opi) <= 1, (step, fpi, opi)
         for name, q in (("d", O.QD), ("u", O.QU), ("v", O.QV)):
             assert rel_err(g.read_field(name), o.array(q, O.A_SRC)) < 1e-9, (step, name)
 
@@ -196,7 +211,7 @@ def test_fp32_form_error_vs_fp64_oracle(ifl, case):
     g = make_gpu(ifl, variant, w, h, o.bodies(), precision=ifl.FP32)
     upload(ifl, g, o, variant)
     o.add_inflow(*inflow)
-    g.addInflow(*inflow[:5], *inflow[5:]) if variant >= 6 else g.addInflow(*inflow[:5], *inflow[6:])
+    add_inflow(g, variant, inflow)
     o.update(DT)
     g.update(DT)
     _, _, flags = g.stats()

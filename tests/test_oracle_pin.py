@@ -110,7 +110,7 @@ def test_config0_as_stated_injects_nothing():
 
 def test_pinned_iterations():
     s = O.OracleSolver(3, 32, 32)
-    s.set_pinned_iterations(7)
+    s.set_pinned_iterations(7, -1)
     s.add_inflow(0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.0, 3.0)
     s.update(0.005)
     assert s.stats()[0][0] == 7
