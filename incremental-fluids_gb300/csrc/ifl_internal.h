@@ -84,7 +84,8 @@ struct Scene {
     double rho_air, rho_soot, diffusion, t_amb, g;
     Quant<F> q[4];  // d, t, u, v
     SDIdx sd;          // layout of the pressure-system arrays below
-    F *r, *p, *z, *sa, *sb, *as;
+    double *r, *p;     // residual and solution stay FP64 in both forms
+    F *z, *sa, *sb, *as;
     F *adiag, *ax, *ay;
     F *lx, *ly, *pcf;  // MIC(0) apply operands in storage precision
     double *pc;        // MIC(0) factor, FP64
@@ -105,7 +106,8 @@ struct PcgOut {
 struct PcgScratch {
     double *partials;    // 4 * max_blocks
     unsigned *barrier;   // 2 words
-    unsigned *progress;  // one word per 32-row strip
+    double *halo_up;     // S x D: top row of each strip, for the strip above (sentinel protocol)
+    double *halo_down;   // S x D: bottom row of each strip, for the strip below
     PcgOut *out;
     unsigned long long *iter_total;  // PCG iterations summed over launches
     int max_blocks;
@@ -131,8 +133,8 @@ template <typename F> void launch_heat_assemble(const Scene<F> &S, double dt, cu
 template <typename F> void launch_apply_pressure(const Scene<F> &S, double dt, cudaStream_t st);
 template <typename F> void launch_extrapolate(const Scene<F> &S, unsigned qmask, cudaStream_t st);
 template <typename F> void launch_advect(const Scene<F> &S, double dt, cudaStream_t st);
-// strip-diagonal <-> row-major copy of one w x h array (dir 0: SD -> rows)
-template <typename F> void launch_sd_copy(const Scene<F> &S, F *rows, F *sd_arr, int dir, cudaStream_t st);
+// strip-diagonal FP64 array -> row-major field (T = p after the heat solve)
+template <typename F> void launch_sd_to_rows(const Scene<F> &S, F *rows, const double *sd_arr, cudaStream_t st);
 template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
                                              cudaStream_t st, int *blocks_used);
 template <typename F> int pcg_max_blocks();

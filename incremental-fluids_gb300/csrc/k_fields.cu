@@ -264,7 +264,7 @@ __global__ void assemble_kernel(Scene<F> S, double dt, int what) {
                     r += (vv1 - vol) * body_vel_y(S.bodies[body[c + P]], (x + 0.5) * hx, (y + 1.0) * hx);
             }
         }
-        S.r[k] = (F)r;
+        S.r[k] = r;
     }
 
     if (what & ASM_DENS) {  // face densities for applyPressure (step 7)
@@ -327,7 +327,7 @@ __global__ void heat_assemble_kernel(Scene<F> S, double dt) {
     const size_t k = S.sd.slot(x, y);
     const uint8_t *cell = S.q[0].cell;
     const bool fl = cell[c] == CELL_FLUID;
-    S.r[k] = S.q[1].src[c];
+    S.r[k] = (double)S.q[1].src[c];
     double scale = S.diffusion * dt * 1.0 / (S.hx * S.hx);
     bool fL = x > 0 && fl && cell[c - 1] == CELL_FLUID;
     bool fR = x < w - 1 && fl && cell[c + 1] == CELL_FLUID;
@@ -579,14 +579,12 @@ __global__ void advect_kernel(Scene<F> S, F dt) {
     }
 }
 
-// Strip-diagonal <-> row-major copy of one w x h array (T = p after the heat solve).
+// Strip-diagonal FP64 array -> row-major field (T = p after the heat solve).
 template <typename F>
-__global__ void sd_copy_kernel(SDIdx sd, int P, F *rows, F *sd_arr, int dir) {
+__global__ void sd_to_rows_kernel(SDIdx sd, int P, F *rows, const double *sd_arr) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= sd.W || y >= sd.H) return;
-    size_t r = x + (size_t)y * P, k = sd.slot(x, y);
-    if (dir == 0) rows[r] = sd_arr[k];
-    else sd_arr[k] = rows[r];
+    rows[x + (size_t)y * P] = (F)sd_arr[sd.slot(x, y)];
 }
 
 inline dim3 grid2(int nx, int ny, int nz, dim3 b) {
@@ -656,9 +654,9 @@ void launch_advect(const Scene<F> &S, double dt, cudaStream_t st) {
 }
 
 template <typename F>
-void launch_sd_copy(const Scene<F> &S, F *rows, F *sd_arr, int dir, cudaStream_t st) {
+void launch_sd_to_rows(const Scene<F> &S, F *rows, const double *sd_arr, cudaStream_t st) {
     dim3 b(32, 8);
-    sd_copy_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S.sd, S.P, rows, sd_arr, dir);
+    sd_to_rows_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S.sd, S.P, rows, sd_arr);
 }
 
 #define IFL_INST(F)                                                                                        \
@@ -672,7 +670,7 @@ void launch_sd_copy(const Scene<F> &S, F *rows, F *sd_arr, int dir, cudaStream_t
     template void launch_apply_pressure<F>(const Scene<F> &, double, cudaStream_t);                         \
     template void launch_extrapolate<F>(const Scene<F> &, unsigned, cudaStream_t);                          \
     template void launch_advect<F>(const Scene<F> &, double, cudaStream_t);                                 \
-    template void launch_sd_copy<F>(const Scene<F> &, F *, F *, int, cudaStream_t);
+    template void launch_sd_to_rows<F>(const Scene<F> &, F *, const double *, cudaStream_t);
 IFL_INST(double)
 IFL_INST(float)
 

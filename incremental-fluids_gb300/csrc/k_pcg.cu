@@ -24,7 +24,9 @@
 //    shuffle.  Operands stream through a shared-memory ring filled by bulk
 //    asynchronous copies (cp.async.bulk, completion on an mbarrier), one
 //    contiguous block of kSweepBlock diagonals per array.  Strips hand their
-//    boundary row to the next strip through a release flag.  Every cell runs
+//    boundary row to the next strip through a halo row (one 8-byte store per
+//    column, polled against a sentinel; no fence on the critical path).
+//    Every cell runs
 //    exactly the reference's arithmetic in a dependency-respecting order, so
 //    the factor and the solves are bit-identical to the sequential loops.
 //  * Phases are separated by a grid barrier of this file.
@@ -52,9 +54,11 @@ struct PcgArgs {
     double *pc;
     F *pcf, *lx, *ly;
     const uint8_t *nb;
-    F *r, *p, *z, *sa, *sb, *as;
+    double *r, *p;
+    F *z, *sa, *sb, *as;
     double *partials;
-    unsigned *barrier, *progress, *flags;
+    unsigned *barrier, *flags;
+    double *halo_up, *halo_down;
     PcgOut *out;
     unsigned long long *iter_total;
     int mode, limit, pinned;
@@ -187,20 +191,29 @@ __device__ __forceinline__ void ring_wait(Ring &R, unsigned *flags) {
 }
 
 // Streams of one sweep kind: KIND 0 factor (adiag, ax, ay), 1 forward (r, lx,
-// ly, pcf), 2 backward (z, lx, ly, pcf, r); the neighbour bits always follow.
+// ly, pcf), 2 backward (z, lx, ly, pcf, r).  Each stream owns a fixed 8-byte
+// wide slot of the stage; the neighbour bits follow.
+constexpr unsigned kSlotBytes = kB * 32 * 8;
+constexpr unsigned kNbBytes = kB * 32;
+constexpr int kStageBytes = 5 * kSlotBytes + kNbBytes;
+
 template <int KIND, typename F>
 struct Streams {
     static constexpr int n = KIND == 0 ? 3 : KIND == 1 ? 4 : 5;
-    const F *src[5];
+    const void *src[5];
+    unsigned esz[5];
     __device__ explicit Streams(const PcgArgs<F> &A) {
+        for (int k = 0; k < 5; k++) esz[k] = sizeof(F);
         if (KIND == 0) {
             src[0] = A.adiag; src[1] = A.ax; src[2] = A.ay;
         } else if (KIND == 1) {
             src[0] = A.r; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf;
+            esz[0] = 8;
         } else {
             src[0] = A.z; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = A.r;
+            esz[4] = 8;
         }
-        if (n < 5) src[n] = nullptr;
+        for (int k = n; k < 5; k++) src[k] = nullptr;
     }
 };
 
@@ -208,64 +221,69 @@ struct Streams {
 template <int KIND, typename F>
 __device__ __forceinline__ void ring_issue(Ring &R, const PcgArgs<F> &A, const Streams<KIND, F> &St, int s,
                                            int blk) {
-    constexpr unsigned fbytes = kB * 32 * sizeof(F);
-    constexpr unsigned bbytes = kB * 32;
     const int D = A.sd.D;
     const int d0 = (KIND == 2) ? D - (blk + 1) * kB : blk * kB;
     const size_t off = ((size_t)s * D + d0) * 32;
     const unsigned st = R.ii % R.stages;
     char *dst = R.buf + (size_t)st * R.stage_bytes;
     uint64_t *bar = R.bars + st;
+    unsigned total = kNbBytes;
+    for (int k = 0; k < St.n; k++) total += kB * 32 * St.esz[k];
     fence_proxy_async_smem();
-    mbar_expect_tx(bar, St.n * fbytes + bbytes);
-    for (int k = 0; k < St.n; k++) bulk_g2s(dst + k * fbytes, St.src[k] + off, fbytes, bar);
-    bulk_g2s(dst + 5 * fbytes, A.nb + off, bbytes, bar);
+    mbar_expect_tx(bar, total);
+    for (int k = 0; k < St.n; k++)
+        bulk_g2s(dst + k * kSlotBytes, (const char *)St.src[k] + off * St.esz[k], kB * 32 * St.esz[k], bar);
+    bulk_g2s(dst + 5 * kSlotBytes, A.nb + off, kNbBytes, bar);
     R.ii++;
 }
 
-// Wait until strip `src_strip` has published at least `need` (tagged) columns.
-__device__ __forceinline__ unsigned wait_progress(const unsigned *progress, int src_strip, unsigned need,
-                                                  unsigned *flags) {
+// Halo rows hand a strip's boundary row to its neighbour strip.  An entry is
+// the value's 8 bytes, or the sentinel while it has not been written; the
+// producer writes each column once per sweep with one 8-byte store (no
+// fence), the consumer polls and then puts the sentinel back.
+constexpr unsigned long long kSentinel = ~0ull;
+
+__device__ __forceinline__ double halo_take(double *slot, unsigned *flags) {
+    volatile unsigned long long *p = (volatile unsigned long long *)slot;
+    unsigned long long v = *p;
     long long n = 0;
-    unsigned v;
-    for (;;) {
-        v = ld_volatile(progress + src_strip);
-        if (v >= need) break;
+    while (v == kSentinel) {
         if (++n > kWaitLimit || timed_out(flags)) {
             atomicOr(flags, FLAG_TIMEOUT);
-            v = need;
             break;
         }
+        v = *p;
     }
-    __threadfence();
-    return v;
+    *p = kSentinel;
+    return __longlong_as_double((long long)v);
+}
+__device__ __forceinline__ void halo_put(double *slot, double v) {
+    *(volatile unsigned long long *)slot = (unsigned long long)__double_as_longlong(v);
 }
 
 // One strip of a wavefront sweep.  Returns the lane's partial dot(z, r) for
 // the backward solve.
 template <int KIND, typename F>
-__device__ double sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, Ring &R) {
+__device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring &R) {
     using V = typename std::conditional<KIND == 0, double, F>::type;
-    constexpr unsigned fbytes = kB * 32 * sizeof(F);
     const int lane = threadIdx.x & 31;
     const SDIdx sd = A.sd;
     const int W = sd.W, H = sd.H, D = sd.D, S = sd.S;
     const int y = s * 32 + lane;
     const bool rowok = y < H;
-    const unsigned tag = sid << 16;
     const Streams<KIND, F> St(A);
     const int nblk = D / kB;
-    // Backward sweeps run top strip first: lane 31 waits on strip s+1, lane 0 publishes.
+    // Backward sweeps run the top strip first: lane 31 takes from the strip
+    // above, lane 0 hands its row to the strip below.
     const bool bwd = KIND == 2;
-    const int dep = bwd ? s + 1 : s - 1;
     const bool has_dep = bwd ? (s + 1 < S) : (s > 0);
-    const bool waiter = bwd ? (lane == 31) : (lane == 0);
-    const bool publisher = (bwd ? (lane == 0) : (lane == 31)) && (bwd ? s > 0 : s + 1 < S);
-    unsigned seen = 0;
+    const bool producer = (lane == (bwd ? 0 : 31)) && (bwd ? s > 0 : s + 1 < S);
+    double *halo_in = bwd ? A.halo_down + (size_t)(s + 1) * D : A.halo_up + (size_t)(s - 1) * D;
+    double *halo_out = bwd ? A.halo_down + (size_t)s * D : A.halo_up + (size_t)s * D;
     double dot = 0.0;
 
-    V prev = V(0);                  // result of the previous cell in sweep order
-    F prev_a = F(0), prev_b = F(0); // forward: lx, ly of that cell; factor: ax, ay
+    V prev = V(0);                   // result of the previous cell in sweep order
+    F prev_a = F(0), prev_b = F(0);  // forward: lx, ly of that cell; factor: ax, ay
 
     if (lane == 0) {
         fence_proxy_async_global();  // generic-proxy writes before this sweep -> bulk copies
@@ -277,44 +295,59 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, Ring &R)
         if (blk + R.stages - 1 < nblk) {
             __syncwarp();
             if (lane == 0) ring_issue<KIND, F>(R, A, St, s, blk + R.stages - 1);
-            else R.ii++;
+        }
+        // Boundary values of this block for the waiting lane: lane j fetches
+        // the column the waiting lane works on at step j.
+        double hv = 0.0;
+        F ha = F(0), hb = F(0);
+        if (has_dep && lane < kB) {
+            const int xj = bwd ? D - 32 - blk * kB - lane : blk * kB + lane;
+            if (xj >= 0 && xj < W) {
+                if constexpr (KIND == 0) {
+                    const size_t k = sd.slot(xj, s * 32 - 1);
+                    ha = A.ax[k];
+                    hb = A.ay[k];
+                } else if constexpr (KIND == 1) {
+                    hb = A.ly[sd.slot(xj, s * 32 - 1)];
+                }
+                hv = halo_take(halo_in + xj, A.flags);
+            }
         }
         const unsigned st = R.ci % R.stages;
         ring_wait(R, A.flags);
         const char *sb = R.buf + (size_t)st * R.stage_bytes;
-        const F *s0 = (const F *)sb;
-        const F *s1 = (const F *)(sb + fbytes);
-        const F *s2 = (const F *)(sb + 2 * fbytes);
-        const F *s3 = (const F *)(sb + 3 * fbytes);
-        const F *s4 = (const F *)(sb + 4 * fbytes);
-        const uint8_t *snb = (const uint8_t *)(sb + 5 * fbytes);
+        const F *f0 = (const F *)sb;
+        const double *d0 = (const double *)sb;
+        const F *s1 = (const F *)(sb + kSlotBytes);
+        const F *s2 = (const F *)(sb + 2 * kSlotBytes);
+        const F *s3 = (const F *)(sb + 3 * kSlotBytes);
+        const double *d4 = (const double *)(sb + 4 * kSlotBytes);
+        const uint8_t *snb = (const uint8_t *)(sb + 5 * kSlotBytes);
 #pragma unroll 4
         for (int j = 0; j < kB; j++) {
             const int t = blk * kB + j;
             const int d = bwd ? D - 1 - t : t;
-            const int jj = bwd ? (kB - 1 - j) : j;
-            const int e = jj * 32 + lane;  // slot inside the staged block
+            const int e = (bwd ? (kB - 1 - j) : j) * 32 + lane;  // slot inside the staged block
             const int x = d - lane;
             const bool active = rowok && x >= 0 && x < W;
             const size_t i = ((size_t)s * D + d) * 32 + lane;
-            const int xs = bwd ? W - 1 - x : x;  // sweep column
             const uint8_t b = snb[e];
+            const double hvj = __shfl_sync(0xffffffffu, hv, j);
             if constexpr (KIND == 0) {
                 // buildPreconditioner (3-conjugate-gradients/Fluid.cpp:253-269)
                 double pc_d = __shfl_up_sync(0xffffffffu, prev, 1);
                 F ax_d = __shfl_up_sync(0xffffffffu, prev_a, 1);
                 F ay_d = __shfl_up_sync(0xffffffffu, prev_b, 1);
+                const F haj = __shfl_sync(0xffffffffu, ha, j), hbj = __shfl_sync(0xffffffffu, hb, j);
+                if (lane == 0) {
+                    pc_d = hvj;
+                    ax_d = haj;
+                    ay_d = hbj;
+                }
                 const F axv = s1[e], ayv = s2[e];
                 V val = prev;
                 if (active && (b & NB_SELF)) {
-                    if (waiter && has_dep && (b & NB_DOWN)) {
-                        if (seen <= (unsigned)xs) seen = wait_progress(A.progress, dep, tag + xs + 1, A.flags) - tag;
-                        const size_t k = sd.slot(x, y - 1);
-                        pc_d = __ldcg(A.pc + k);
-                        ax_d = __ldcg(A.ax + k);
-                        ay_d = __ldcg(A.ay + k);
-                    }
-                    const double diag = (double)s0[e];
+                    const double diag = (double)f0[e];
                     double ev = diag;
                     if (b & NB_LEFT) {
                         double px = (double)prev_a * prev;
@@ -341,16 +374,15 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, Ring &R)
                 // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
                 F q_d = __shfl_up_sync(0xffffffffu, prev, 1);
                 F ly_d = __shfl_up_sync(0xffffffffu, prev_b, 1);
+                const F hbj = __shfl_sync(0xffffffffu, hb, j);
+                if (lane == 0) {
+                    q_d = (F)hvj;
+                    ly_d = hbj;
+                }
                 const F lxv = s1[e], lyv = s2[e];
                 V val = prev;
                 if (active && (b & NB_SELF)) {
-                    if (waiter && has_dep && (b & NB_DOWN)) {
-                        if (seen <= (unsigned)xs) seen = wait_progress(A.progress, dep, tag + xs + 1, A.flags) - tag;
-                        const size_t k = sd.slot(x, y - 1);
-                        q_d = __ldcg(A.z + k);
-                        ly_d = __ldcg(A.ly + k);
-                    }
-                    F tt = s0[e];
+                    F tt = (F)d0[e];
                     if (b & NB_LEFT) tt = tt - prev_a * prev;
                     if (b & NB_DOWN) tt = tt - ly_d * q_d;
                     val = tt * s3[e];
@@ -362,25 +394,19 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, Ring &R)
             } else {
                 // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
                 F z_u = __shfl_down_sync(0xffffffffu, prev, 1);
+                if (lane == 31) z_u = (F)hvj;
                 V val = prev;
                 if (active && (b & NB_SELF)) {
-                    if (waiter && has_dep && (b & NB_UP)) {
-                        if (seen <= (unsigned)xs) seen = wait_progress(A.progress, dep, tag + xs + 1, A.flags) - tag;
-                        z_u = __ldcg(A.z + sd.slot(x, y + 1));
-                    }
-                    F tt = s0[e];
+                    F tt = f0[e];
                     if (b & NB_RIGHT) tt = tt - s1[e] * prev;
                     if (b & NB_UP) tt = tt - s2[e] * z_u;
                     val = tt * s3[e];
                     A.z[i] = val;
-                    if (b & NB_RED) dot = dacc(dot, val, s4[e]);
+                    if (b & NB_RED) dot = dacc(dot, (double)val, d4[e]);
                 }
                 prev = val;
             }
-            if (publisher && active && ((((xs + 1) & 7) == 0) || xs == W - 1)) {
-                __threadfence();
-                st_volatile(A.progress + s, tag + (unsigned)xs + 1u);
-            }
+            if (producer && active) halo_put(halo_out + x, (double)prev);
         }
     }
     __syncwarp();
@@ -388,9 +414,9 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, unsigned sid, Ring &R)
 }
 
 template <int KIND, typename F>
-__device__ __forceinline__ double sweep(const PcgArgs<F> &A, unsigned sid, Ring &R, bool sweeper) {
+__device__ __forceinline__ double sweep(const PcgArgs<F> &A, Ring &R, bool sweeper) {
     if (!sweeper) return 0.0;
-    return sweep_strip<KIND, F>(A, blockIdx.x, sid, R);
+    return sweep_strip<KIND, F>(A, blockIdx.x, R);
 }
 
 template <typename F>
@@ -403,7 +429,6 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
     const int rows = sd.S * D;  // diagonals of all strips
     const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
     const bool sweeper = warp == 0 && (int)blockIdx.x < sd.S;
-    unsigned sid = 1;
 
     Ring R;
     R.bars = (uint64_t *)smem_raw;
@@ -420,7 +445,7 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
     }
 
     if (A.mode & PCG_FACTOR) {
-        sweep<0, F>(A, sid++, R, sweeper);
+        sweep<0, F>(A, R, sweeper);
         grid_barrier(A.barrier, A.flags);
     }
     if (!(A.mode & PCG_SOLVE)) return;
@@ -429,14 +454,14 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
     double mx = 0.0;
     for (int row = gwarp; row < rows; row += nwarps) {
         const size_t i = (size_t)row * 32 + lane;
-        A.p[i] = F(0);
-        if (A.nb[i] & NB_RED) mx = smax(mx, (double)fabs(A.r[i]));
+        A.p[i] = 0.0;
+        if (A.nb[i] & NB_RED) mx = smax(mx, fabs(A.r[i]));
     }
     block_store(mx, true, A.partials, 0, sm);
     // z = M^-1 r  (:351)
-    sweep<1, F>(A, sid++, R, sweeper);
+    sweep<1, F>(A, R, sweeper);
     grid_barrier(A.barrier, A.flags);
-    double d = sweep<2, F>(A, sid++, R, sweeper);
+    double d = sweep<2, F>(A, R, sweeper);
     block_store(d, false, A.partials, 2, sm);
     grid_barrier(A.barrier, A.flags);
 
@@ -484,15 +509,14 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
             grid_barrier(A.barrier, A.flags);
             const double alpha = sigma / grid_reduce(A.partials, 1, false, sm);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
-            const F falpha = (F)alpha, fnalpha = (F)(-alpha);
             mx = 0.0;
             for (int row = gwarp; row < rows; row += nwarps) {
                 const size_t i = (size_t)row * 32 + lane;
                 if (A.nb[i] & NB_RED) {
-                    A.p[i] = A.p[i] + s_new[i] * falpha;
-                    const F rn = A.r[i] + A.as[i] * fnalpha;
+                    A.p[i] = A.p[i] + (double)s_new[i] * alpha;
+                    const double rn = A.r[i] + (double)A.as[i] * -alpha;
                     A.r[i] = rn;
-                    mx = smax(mx, (double)fabs(rn));
+                    mx = smax(mx, fabs(rn));
                 }
             }
             block_store(mx, true, A.partials, 0, sm);
@@ -504,9 +528,9 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
                 break;
             }
             // z = M^-1 r; sigmaNew = z.r  (:372-376)
-            sweep<1, F>(A, sid++, R, sweeper);
+            sweep<1, F>(A, R, sweeper);
             grid_barrier(A.barrier, A.flags);
-            d = sweep<2, F>(A, sid++, R, sweeper);
+            d = sweep<2, F>(A, R, sweeper);
             block_store(d, false, A.partials, 2, sm);
             grid_barrier(A.barrier, A.flags);
             const double sigmaNew = grid_reduce(A.partials, 2, false, sm);
@@ -528,11 +552,11 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
 
 template <typename F>
 int ring_stages() {
-    return sizeof(F) == 8 ? 3 : 4;
+    return 4;
 }
 template <typename F>
 int ring_stage_bytes() {
-    return kB * 32 * (5 * (int)sizeof(F) + 1);
+    return kStageBytes;
 }
 template <typename F>
 size_t smem_bytes() {
@@ -581,7 +605,8 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     A.as = S.as;
     A.partials = X.partials;
     A.barrier = X.barrier;
-    A.progress = X.progress;
+    A.halo_up = X.halo_up;
+    A.halo_down = X.halo_down;
     A.flags = S.flags;
     A.out = X.out + (cfg.heat ? 1 : 0);
     A.iter_total = X.iter_total;
@@ -599,7 +624,9 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     int G = want < maxb ? want : maxb;
     if (blocks_used) *blocks_used = G;
     cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
-    cudaMemsetAsync(X.progress, 0, (size_t)S.sd.S * sizeof(unsigned), st);
+    const size_t halo = (size_t)S.sd.S * S.sd.D * sizeof(double);
+    cudaMemsetAsync(X.halo_up, 0xff, halo, st);  // every entry starts as the sentinel
+    cudaMemsetAsync(X.halo_down, 0xff, halo, st);
     void *args[] = {&A};
     return cudaLaunchCooperativeKernel((const void *)pcg_kernel<F>, dim3(G), dim3(kThreads), args,
                                        smem_bytes<F>(), st);

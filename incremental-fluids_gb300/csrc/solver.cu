@@ -204,8 +204,8 @@ class SolverImpl final : public SolverBase {
             *elem = fe;
             *sd = field <= IFL_F_APLUSY ? 1 : 0;
             switch (field) {
-            case IFL_F_R: *ptr = S_.r; return 0;
-            case IFL_F_P: *ptr = S_.p; return 0;
+            case IFL_F_R: *ptr = S_.r; *elem = IFL_DT_F64; return 0;
+            case IFL_F_P: *ptr = S_.p; *elem = IFL_DT_F64; return 0;
             case IFL_F_Z: *ptr = S_.z; return 0;
             case IFL_F_S: *ptr = S_.sa; return 0;
             case IFL_F_PRECON: *ptr = S_.pc; *elem = IFL_DT_F64; return 0;
@@ -311,8 +311,8 @@ class SolverImpl final : public SolverBase {
                 Q.list = c.take<int>(base, 2 * N);
             }
         }
-        S_.r = c.take<F>(base, NS);
-        S_.p = c.take<F>(base, NS);
+        S_.r = c.take<double>(base, NS);
+        S_.p = c.take<double>(base, NS);
         S_.z = c.take<F>(base, NS);
         S_.sa = c.take<F>(base, NS);
         S_.sb = c.take<F>(base, NS);
@@ -338,7 +338,8 @@ class SolverImpl final : public SolverBase {
         scratch_.max_blocks = max_blocks_;
         scratch_.partials = c.take<double>(base, 4 * (size_t)std::max(max_blocks_, 1));
         scratch_.barrier = c.take<unsigned>(base, 2);
-        scratch_.progress = c.take<unsigned>(base, (size_t)S_.sd.S + 1);
+        scratch_.halo_up = c.take<double>(base, (size_t)S_.sd.S * S_.sd.D);
+        scratch_.halo_down = c.take<double>(base, (size_t)S_.sd.S * S_.sd.D);
         scratch_.out = c.take<PcgOut>(base, 2);
         scratch_.iter_total = c.take<unsigned long long>(base, 1);
     }
@@ -418,7 +419,7 @@ class SolverImpl final : public SolverBase {
         launches_++;
         if (int e = pcg(PCG_FACTOR | PCG_SOLVE, true)) return e;
         t = tbegin(IFL_K_ASSEMBLE);
-        launch_sd_copy<F>(S_, S_.q[1].src, S_.p, 0, stream_);
+        launch_sd_to_rows<F>(S_, S_.q[1].src, S_.p, stream_);
         tend(t);
         launches_++;
         return launch_check("T = p");

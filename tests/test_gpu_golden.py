@@ -60,7 +60,12 @@ def test_gpu_fp64_matches_golden(ifl, path):
         # 2000 iterations of a stagnating solve amplify rounding; only the outcome is compared
         assert all(st == 2 for _, st in iters)
         return
+    fluid = np.ones_like(g["p"], dtype=bool)
+    if variant >= 4:  # p at solid cells holds stale values nothing reads
+        fluid = s.read_field(ifl.field_id(ifl.Q_D, ifl.A_CELL), np.uint8) == 0
     for key in ("d", "t", "u", "v", "p"):
         if key in g:
             a, b = s.read_field(key), g[key]
+            if key == "p":
+                a, b = a[fluid], b[fluid]
             assert np.abs(a - b).max() <= 1e-9 * max(np.abs(b).max(), 1e-300), key

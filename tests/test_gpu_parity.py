@@ -44,6 +44,27 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / (den if den > 0 else 1.0))
 
 
+def fluid_mask(o, variant):
+    """Cells whose pressure is used.  In the solid variants the reference's
+    unmasked scaledAdd leaves stale, never-read values in p at solid cells."""
+    if variant < 4:
+        return np.ones((o.h, o.w), dtype=bool)
+    return o.bytes(O.QD, O.B_CELL) == 0
+
+
+def pressure_err(g, o, variant):
+    m = fluid_mask(o, variant)
+    return rel_err(g.read_field("p")[m], o.array(0, O.A_P)[m])
+
+
+def velocity_err(g, o):
+    """Max-norm error of the velocity field (u and v together) relative to its max."""
+    du = np.abs(g.read_field("u") - o.array(O.QU, O.A_SRC)).max()
+    dv = np.abs(g.read_field("v") - o.array(O.QV, O.A_SRC)).max()
+    den = max(np.abs(o.array(O.QU, O.A_SRC)).max(), np.abs(o.array(O.QV, O.A_SRC)).max(), 1e-300)
+    return float(max(du, dv) / den)
+
+
 def make_gpu(ifl, variant, w, h, bodies, precision=0):
     if variant == 3:
         g = ifl.FluidSolver(w, h, 0.1, precision=precision)
@@ -72,8 +93,9 @@ def upload(ifl, g, o, variant):
         if variant >= 5:
             g.write_field(ifl.field_id(q, ifl.A_PHI), o.array(q, O.A_PHI).copy())
             g.write_field(ifl.field_id(q, ifl.A_VOLUME), o.array(q, O.A_VOLUME).copy())
-    for f, a in ((ifl.F_R, O.A_R), (ifl.F_P, O.A_P), (ifl.F_ADIAG, O.A_ADIAG),
-                 (ifl.F_APLUSX, O.A_APLUSX), (ifl.F_APLUSY, O.A_APLUSY)):
+    for f, a in ((ifl.F_R, O.A_R), (ifl.F_P, O.A_P)):  # residual and pressure are FP64 in both forms
+        g.write_field(f, o.array(0, a).copy())
+    for f, a in ((ifl.F_ADIAG, O.A_ADIAG), (ifl.F_APLUSX, O.A_APLUSX), (ifl.F_APLUSY, O.A_APLUSY)):
         g.write_field(f, o.array(0, a).astype(fdt))
     g.write_field(ifl.F_PRECON, o.array(0, O.A_PRECON).copy())
     if variant == 7:
@@ -164,7 +186,7 @@ def test_phases_bit_exact_fp64(ifl, case):
             assert flags & 1 == 0, "device wait timed out"
             if ph == O.PH_PROJECT:
                 assert (pi, ps) == (opi, ops)
-                assert rel_err(g.read_field("p"), o.array(0, O.A_P)) < 1e-10
+                assert pressure_err(g, o, variant) < 1e-10
             else:
                 assert (hi, hs) == (ohi, ohs)
                 assert rel_err(g.read_field("t"), o.array(O.QT, O.A_SRC)) < 1e-10
@@ -205,7 +227,9 @@ def test_trajectory_fp64(ifl, case):
 
 @pytest.mark.parametrize("case", [c for c in CASES if c[1] == 64 and c[2] == 64], ids=lambda c: f"v{c[0]}")
 def test_fp32_form_error_vs_fp64_oracle(ifl, case):
-    """FP32 form, one update from the oracle's state: <= 1e-4 relative (pressure, velocity)."""
+    """FP32 form, one update from the oracle's state: <= 1e-4 relative for the
+    pressure (fluid cells) and for the velocity field (u and v against the
+    largest velocity component)."""
     variant, w, h, warm, inflow, bodies = case
     o = warm_oracle(variant, w, h, warm + 2, inflow, bodies)
     g = make_gpu(ifl, variant, w, h, o.bodies(), precision=ifl.FP32)
@@ -216,10 +240,9 @@ def test_fp32_form_error_vs_fp64_oracle(ifl, case):
     g.update(DT)
     _, _, flags = g.stats()
     assert flags & 1 == 0
-    errs = {"p": rel_err(g.read_field("p"), o.array(0, O.A_P))}
-    for name, q in (("u", O.QU), ("v", O.QV), ("d", O.QD)):
-        errs[name] = rel_err(g.read_field(name), o.array(q, O.A_SRC))
-    assert errs["p"] < 1e-4 and errs["u"] < 1e-4 and errs["v"] < 1e-4, errs
+    errs = {"p": pressure_err(g, o, variant), "velocity": velocity_err(g, o),
+            "d": rel_err(g.read_field("d"), o.array(O.QD, O.A_SRC))}
+    assert errs["p"] < 1e-4 and errs["velocity"] < 1e-4, errs
 
 
 def test_deterministic_and_stream_ordered(ifl):
