@@ -47,15 +47,23 @@ METRIC = "cell-steps/s"
 # Algorithmic bytes per cell of the persistent PCG kernel (strip-diagonal
 # arrays, F = storage width, neighbour bits 1 byte, FP64 factor):
 #   factor  reads adiag, ax, ay, nb; writes pc (8 B), pcf, lx, ly      = 6F + 9
-#   setup   p = 0, |r|_inf, forward (r, lx, ly, pcf, nb -> z) and
-#           backward (z, lx, ly, pcf, r, nb -> z) substitutions         = 13F + 3
-#   per iteration: s-update + matvec + dot (7F + 1), AXPYs + norm
-#           (6F + 1), forward (5F + 1) and backward (6F + 1)            = 24F + 4
-#   the last iteration stops after the AXPYs (no substitutions)         = -(11F + 2)
+#   r, p and A*s are FP64 in both forms (R = 8 bytes).
+#   setup   p = 0 (R), |r|_inf (R + 1), forward (r, lx, ly, pcf, nb -> z:
+#           R + 4F + 1) and backward (z, lx, ly, pcf, r, nb -> z: R + 5F + 1)
+#                                                                      = 4R + 9F + 3
+#   per iteration: s-update + matvec + dot (z, s, adiag, ax, ay, nb ->
+#           s, As: R + 6F + 1), AXPYs + norm (p, s, r, As, nb -> p, r:
+#           5R + F + 1), forward (R + 4F + 1), backward (R + 5F + 1)   = 8R + 16F + 4
+#   the last iteration stops after the AXPYs (no substitutions)         = -(2R + 9F + 2)
 
 
 def pcg_bytes_per_cell(F: int, launches: int, iterations: int) -> float:
-    return launches * ((6 * F + 9) + (13 * F + 3) - (11 * F + 2)) + iterations * (24 * F + 4)
+    R = 8
+    factor = 6 * F + 9
+    setup = 4 * R + 9 * F + 3
+    per_iter = 8 * R + 16 * F + 4
+    last = 2 * R + 9 * F + 2
+    return launches * (factor + setup - last) + iterations * per_iter
 
 
 def load_peaks():

@@ -85,7 +85,9 @@ struct Scene {
     Quant<F> q[4];  // d, t, u, v
     SDIdx sd;          // layout of the pressure-system arrays below
     double *r, *p;     // residual and solution stay FP64 in both forms
-    F *z, *sa, *sb, *as;
+    double *as;        // A*s, accumulated in FP64 (a consistent operator in both forms)
+    F *rf;             // r in storage precision for the substitutions (aliases r for FP64)
+    F *z, *sa, *sb;
     F *adiag, *ax, *ay;
     F *lx, *ly, *pcf;  // MIC(0) apply operands in storage precision
     double *pc;        // MIC(0) factor, FP64
@@ -106,8 +108,7 @@ struct PcgOut {
 struct PcgScratch {
     double *partials;    // 4 * max_blocks
     unsigned *barrier;   // 2 words
-    double *halo_up;     // S x D: top row of each strip, for the strip above (sentinel protocol)
-    double *halo_down;   // S x D: bottom row of each strip, for the strip below
+    unsigned long long *halo;  // 2 x S x D boundary rows handed between strips (sentinel protocol)
     PcgOut *out;
     unsigned long long *iter_total;  // PCG iterations summed over launches
     int max_blocks;

@@ -9,26 +9,29 @@
 //
 // Data: every array of the pressure system is in the strip-diagonal layout
 // (SDIdx): a 32-row strip stores its cells diagonal by diagonal, 32 lanes
-// contiguous.
+// contiguous.  r, p and A*s are FP64 in both forms; the FP32 form keeps an
+// FP32 copy of r for the substitutions.
 //
 // Work decomposition
 //  * Elementwise phases (fused s-update + matvec + dot; AXPYs + max-norm): each
-//    warp takes whole diagonals (32 contiguous slots), per-block partial sums
-//    in FP64, and a fixed-order cross-block reduction that every block performs
+//    warp takes whole diagonals (32 contiguous slots), FP64 partial sums per
+//    block and a fixed-order cross-block reduction that every block performs
 //    identically, so all blocks take the same branch and results are
 //    run-to-run deterministic.
-//  * MIC(0) factor and both triangular solves: anti-diagonal wavefronts.  Warp
-//    0 of block s owns strip s; lane l handles row 32s+l and at step t works on
-//    diagonal t (backward: the mirrored diagonal), so the lower (upper)
-//    neighbour's result arrives from lane l-1 (l+1) through a register
-//    shuffle.  Operands stream through a shared-memory ring filled by bulk
-//    asynchronous copies (cp.async.bulk, completion on an mbarrier), one
-//    contiguous block of kSweepBlock diagonals per array.  Strips hand their
-//    boundary row to the next strip through a halo row (one 8-byte store per
-//    column, polled against a sentinel; no fence on the critical path).
-//    Every cell runs
-//    exactly the reference's arithmetic in a dependency-respecting order, so
-//    the factor and the solves are bit-identical to the sequential loops.
+//  * MIC(0) factor and both triangular solves: anti-diagonal wavefronts.  A
+//    block owns K consecutive 32-row strips, one per warp; lane l handles row
+//    32s+l and at step t works on diagonal t (backward: the mirrored
+//    diagonal), so the lower (upper) neighbour's value arrives from lane l-1
+//    (l+1) through a register shuffle.  Operands stream through a per-warp
+//    shared-memory ring filled by bulk asynchronous copies (cp.async.bulk,
+//    completion on an mbarrier), one contiguous block of kSweepBlock diagonals
+//    per array.  A strip hands its boundary row to the neighbouring strip
+//    through a halo row: in shared memory between warps of one block, in
+//    global memory between blocks; each entry is written once per sweep with
+//    one 8-byte store and polled against a sentinel (no fences on the
+//    critical path).  Every cell runs exactly the reference's arithmetic in a
+//    dependency-respecting order, so the factor and the FP64 substitutions
+//    are bit-identical to the sequential loops.
 //  * Phases are separated by a grid barrier of this file.
 // Every wait is bounded: on timeout the status word gets FLAG_TIMEOUT, later
 // waits stop waiting, the kernel runs to its end and the host reports an error.
@@ -42,10 +45,13 @@ namespace {
 
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
-constexpr int kB = kSweepBlock;
-constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of flag polling
+constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
+constexpr int kHB = 8;                           // halo columns fetched together
+constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
 constexpr double kTau = 0.97, kSigma = 0.25, kTol = 1e-5;
+constexpr unsigned long long kSentinel = ~0ull;
+constexpr unsigned FULL = 0xffffffffu;
 
 template <typename F>
 struct PcgArgs {
@@ -54,15 +60,16 @@ struct PcgArgs {
     double *pc;
     F *pcf, *lx, *ly;
     const uint8_t *nb;
-    double *r, *p;
-    F *z, *sa, *sb, *as;
+    double *r, *p, *as;
+    F *rf;  // r in storage precision for the substitutions (== r when F is double)
+    F *z, *sa, *sb;
     double *partials;
     unsigned *barrier, *flags;
-    double *halo_up, *halo_down;
+    unsigned long long *halo;  // [2][S][D]: [0] rows handed upward, [1] rows handed downward
     PcgOut *out;
     unsigned long long *iter_total;
     int mode, limit, pinned;
-    int stages, stage_bytes;
+    int K, stages;
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -71,7 +78,6 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
@@ -123,11 +129,11 @@ __device__ void grid_barrier(unsigned *bar, unsigned *flags) {
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
     return v;
 }
 __device__ __forceinline__ double warp_max(double v) {
-    for (int o = 16; o > 0; o >>= 1) v = smax(v, __shfl_down_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = smax(v, __shfl_down_sync(FULL, v, o));
     return v;
 }
 
@@ -161,24 +167,58 @@ __device__ double grid_reduce(const double *partials, int slot, bool is_max, dou
     return r;
 }
 
-// FP64 dot-product accumulation of stored values (explicit FMA for FP32 data).
-__device__ __forceinline__ double dacc(double acc, double a, double b) { return acc + a * b; }
-__device__ __forceinline__ double dacc(double acc, float a, float b) { return fma((double)a, (double)b, acc); }
+// ------------------------------------------------------------ halo words
+__device__ __forceinline__ unsigned long long henc(double v) { return (unsigned long long)__double_as_longlong(v); }
+__device__ __forceinline__ unsigned long long henc(float v) { return (unsigned long long)__float_as_uint(v); }
+template <typename V> __device__ __forceinline__ V hdec(unsigned long long w);
+template <> __device__ __forceinline__ double hdec<double>(unsigned long long w) {
+    return __longlong_as_double((long long)w);
+}
+template <> __device__ __forceinline__ float hdec<float>(unsigned long long w) { return __uint_as_float((unsigned)w); }
+
+__device__ __forceinline__ unsigned long long hload(const unsigned long long *p) {
+    return *(const volatile unsigned long long *)p;
+}
+__device__ __forceinline__ void hstore(unsigned long long *p, unsigned long long v) {
+    *(volatile unsigned long long *)p = v;
+}
+
+// Take a halo word (bounded poll), then put the sentinel back for the next sweep.
+__device__ __forceinline__ unsigned long long halo_take(unsigned long long *p, unsigned long long pre,
+                                                        unsigned *flags) {
+    unsigned long long v = pre;
+    long long n = 0;
+    while (v == kSentinel) {
+        v = hload(p);
+        if (v != kSentinel) break;
+        if (++n > kWaitLimit || timed_out(flags)) {
+            atomicOr(flags, FLAG_TIMEOUT);
+            v = 0;
+            break;
+        }
+    }
+    hstore(p, kSentinel);
+    return v;
+}
 
 // --------------------------------------------------------------- sweeps
-// Per-warp shared-memory ring: `stages` buffers of stage_bytes, each holding
+// Per-warp shared-memory ring: `stages` buffers of kStageBytes, each holding
 // kB diagonals (kB*32 slots) of up to five F arrays followed by the
 // neighbour-bit bytes.  ii / ci count issued / consumed blocks over the whole
 // kernel, so buffer = count % stages and mbarrier parity = (count/stages) & 1.
+template <typename F>
 struct Ring {
+    static constexpr unsigned kSlot = kB * 32 * sizeof(F);
+    static constexpr unsigned kNb = kB * 32;
+    static constexpr unsigned kStageBytes = 5 * kSlot + kNb;
     char *buf;
     uint64_t *bars;
-    int stages, stage_bytes;
+    int stages;
     unsigned ii, ci;
 };
 
-// Bounded wait for the block that ci refers to.
-__device__ __forceinline__ void ring_wait(Ring &R, unsigned *flags) {
+template <typename F>
+__device__ __forceinline__ void ring_wait(Ring<F> &R, unsigned *flags) {
     const unsigned st = R.ci % R.stages, parity = (R.ci / R.stages) & 1u;
     long long n = 0;
     while (!mbar_try_wait(R.bars + st, parity)) {
@@ -191,163 +231,135 @@ __device__ __forceinline__ void ring_wait(Ring &R, unsigned *flags) {
 }
 
 // Streams of one sweep kind: KIND 0 factor (adiag, ax, ay), 1 forward (r, lx,
-// ly, pcf), 2 backward (z, lx, ly, pcf, r).  Each stream owns a fixed 8-byte
-// wide slot of the stage; the neighbour bits follow.
-constexpr unsigned kSlotBytes = kB * 32 * 8;
-constexpr unsigned kNbBytes = kB * 32;
-constexpr int kStageBytes = 5 * kSlotBytes + kNbBytes;
-
+// ly, pcf), 2 backward (z, lx, ly, pcf, r); the neighbour bits follow.
 template <int KIND, typename F>
-struct Streams {
-    static constexpr int n = KIND == 0 ? 3 : KIND == 1 ? 4 : 5;
-    const void *src[5];
-    unsigned esz[5];
-    __device__ explicit Streams(const PcgArgs<F> &A) {
-        for (int k = 0; k < 5; k++) esz[k] = sizeof(F);
-        if (KIND == 0) {
-            src[0] = A.adiag; src[1] = A.ax; src[2] = A.ay;
-        } else if (KIND == 1) {
-            src[0] = A.r; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf;
-            esz[0] = 8;
-        } else {
-            src[0] = A.z; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = A.r;
-            esz[4] = 8;
-        }
-        for (int k = n; k < 5; k++) src[k] = nullptr;
+__device__ __forceinline__ void ring_issue(Ring<F> &R, const PcgArgs<F> &A, int s, int blk) {
+    const int n = KIND == 0 ? 3 : KIND == 1 ? 4 : 5;
+    const F *src[5];
+    if (KIND == 0) {
+        src[0] = A.adiag; src[1] = A.ax; src[2] = A.ay; src[3] = src[4] = nullptr;
+    } else if (KIND == 1) {
+        src[0] = A.rf; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = nullptr;
+    } else {
+        src[0] = A.z; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = A.rf;
     }
-};
-
-// Issue the bulk copies of diagonal block `blk` of strip s (lane 0 only).
-template <int KIND, typename F>
-__device__ __forceinline__ void ring_issue(Ring &R, const PcgArgs<F> &A, const Streams<KIND, F> &St, int s,
-                                           int blk) {
     const int D = A.sd.D;
     const int d0 = (KIND == 2) ? D - (blk + 1) * kB : blk * kB;
     const size_t off = ((size_t)s * D + d0) * 32;
     const unsigned st = R.ii % R.stages;
-    char *dst = R.buf + (size_t)st * R.stage_bytes;
+    char *dst = R.buf + (size_t)st * Ring<F>::kStageBytes;
     uint64_t *bar = R.bars + st;
-    unsigned total = kNbBytes;
-    for (int k = 0; k < St.n; k++) total += kB * 32 * St.esz[k];
-    fence_proxy_async_smem();
-    mbar_expect_tx(bar, total);
-    for (int k = 0; k < St.n; k++)
-        bulk_g2s(dst + k * kSlotBytes, (const char *)St.src[k] + off * St.esz[k], kB * 32 * St.esz[k], bar);
-    bulk_g2s(dst + 5 * kSlotBytes, A.nb + off, kNbBytes, bar);
+    mbar_expect_tx(bar, n * Ring<F>::kSlot + Ring<F>::kNb);
+    for (int k = 0; k < n; k++) bulk_g2s(dst + k * Ring<F>::kSlot, src[k] + off, Ring<F>::kSlot, bar);
+    bulk_g2s(dst + 5 * Ring<F>::kSlot, A.nb + off, Ring<F>::kNb, bar);
     R.ii++;
 }
 
-// Halo rows hand a strip's boundary row to its neighbour strip.  An entry is
-// the value's 8 bytes, or the sentinel while it has not been written; the
-// producer writes each column once per sweep with one 8-byte store (no
-// fence), the consumer polls and then puts the sentinel back.
-constexpr unsigned long long kSentinel = ~0ull;
-
-__device__ __forceinline__ double halo_take(double *slot, unsigned *flags) {
-    volatile unsigned long long *p = (volatile unsigned long long *)slot;
-    unsigned long long v = *p;
-    long long n = 0;
-    while (v == kSentinel) {
-        if (++n > kWaitLimit || timed_out(flags)) {
-            atomicOr(flags, FLAG_TIMEOUT);
-            break;
-        }
-        v = *p;
-    }
-    *p = kSentinel;
-    return __longlong_as_double((long long)v);
-}
-__device__ __forceinline__ void halo_put(double *slot, double v) {
-    *(volatile unsigned long long *)slot = (unsigned long long)__double_as_longlong(v);
-}
-
-// One strip of a wavefront sweep.  Returns the lane's partial dot(z, r) for
+// One strip of a wavefront sweep.  `in` is the halo row written by the
+// neighbouring strip this one depends on (nullptr: none), `out` the row this
+// strip hands on (nullptr: none).  Returns the lane's partial dot(z, r) for
 // the backward solve.
 template <int KIND, typename F>
-__device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring &R) {
+__device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned long long *in,
+                              unsigned long long *out) {
     using V = typename std::conditional<KIND == 0, double, F>::type;
+    constexpr bool bwd = KIND == 2;
     const int lane = threadIdx.x & 31;
     const SDIdx sd = A.sd;
-    const int W = sd.W, H = sd.H, D = sd.D, S = sd.S;
+    const int W = sd.W, H = sd.H, D = sd.D;
     const int y = s * 32 + lane;
     const bool rowok = y < H;
-    const Streams<KIND, F> St(A);
     const int nblk = D / kB;
-    // Backward sweeps run the top strip first: lane 31 takes from the strip
-    // above, lane 0 hands its row to the strip below.
-    const bool bwd = KIND == 2;
-    const bool has_dep = bwd ? (s + 1 < S) : (s > 0);
-    const bool producer = (lane == (bwd ? 0 : 31)) && (bwd ? s > 0 : s + 1 < S);
-    double *halo_in = bwd ? A.halo_down + (size_t)(s + 1) * D : A.halo_up + (size_t)(s - 1) * D;
-    double *halo_out = bwd ? A.halo_down + (size_t)s * D : A.halo_up + (size_t)s * D;
+    const bool has_in = in != nullptr;
+    const bool producer = out != nullptr && lane == (bwd ? 0 : 31);
     double dot = 0.0;
 
     V prev = V(0);                   // result of the previous cell in sweep order
     F prev_a = F(0), prev_b = F(0);  // forward: lx, ly of that cell; factor: ax, ay
 
+    // Halo prefetch: lane l < kHB holds the word of the column that the
+    // waiting lane (0 forward, 31 backward) reaches at step t0 + l.
+    unsigned long long hpre = kSentinel;
+    F spre_a = F(0), spre_b = F(0);
+    auto halo_col = [&](int t) { return bwd ? D - 32 - t : t; };
+    auto prefetch = [&](int t0) {
+        hpre = kSentinel;
+        if (has_in && lane < kHB) {
+            const int xc = halo_col(t0 + lane);
+            if (xc >= 0 && xc < W) {
+                hpre = hload(in + xc);
+                if constexpr (KIND == 0) {
+                    const size_t k = sd.slot(xc, s * 32 - 1);
+                    spre_a = A.ax[k];
+                    spre_b = A.ay[k];
+                } else if constexpr (KIND == 1) {
+                    spre_b = A.ly[sd.slot(xc, s * 32 - 1)];
+                }
+            }
+        }
+    };
+
     if (lane == 0) {
         fence_proxy_async_global();  // generic-proxy writes before this sweep -> bulk copies
         const int pro = nblk < R.stages - 1 ? nblk : R.stages - 1;
-        for (int b = 0; b < pro; b++) ring_issue<KIND, F>(R, A, St, s, b);
+        for (int b = 0; b < pro; b++) ring_issue<KIND, F>(R, A, s, b);
     }
+    prefetch(0);
     __syncwarp();
     for (int blk = 0; blk < nblk; blk++) {
         if (blk + R.stages - 1 < nblk) {
             __syncwarp();
-            if (lane == 0) ring_issue<KIND, F>(R, A, St, s, blk + R.stages - 1);
-        }
-        // Boundary values of this block for the waiting lane: lane j fetches
-        // the column the waiting lane works on at step j.
-        double hv = 0.0;
-        F ha = F(0), hb = F(0);
-        if (has_dep && lane < kB) {
-            const int xj = bwd ? D - 32 - blk * kB - lane : blk * kB + lane;
-            if (xj >= 0 && xj < W) {
-                if constexpr (KIND == 0) {
-                    const size_t k = sd.slot(xj, s * 32 - 1);
-                    ha = A.ax[k];
-                    hb = A.ay[k];
-                } else if constexpr (KIND == 1) {
-                    hb = A.ly[sd.slot(xj, s * 32 - 1)];
-                }
-                hv = halo_take(halo_in + xj, A.flags);
-            }
+            if (lane == 0) ring_issue<KIND, F>(R, A, s, blk + R.stages - 1);
         }
         const unsigned st = R.ci % R.stages;
         ring_wait(R, A.flags);
-        const char *sb = R.buf + (size_t)st * R.stage_bytes;
-        const F *f0 = (const F *)sb;
-        const double *d0 = (const double *)sb;
-        const F *s1 = (const F *)(sb + kSlotBytes);
-        const F *s2 = (const F *)(sb + 2 * kSlotBytes);
-        const F *s3 = (const F *)(sb + 3 * kSlotBytes);
-        const double *d4 = (const double *)(sb + 4 * kSlotBytes);
-        const uint8_t *snb = (const uint8_t *)(sb + 5 * kSlotBytes);
-#pragma unroll 4
-        for (int j = 0; j < kB; j++) {
-            const int t = blk * kB + j;
-            const int d = bwd ? D - 1 - t : t;
-            const int e = (bwd ? (kB - 1 - j) : j) * 32 + lane;  // slot inside the staged block
-            const int x = d - lane;
-            const bool active = rowok && x >= 0 && x < W;
-            const size_t i = ((size_t)s * D + d) * 32 + lane;
-            const uint8_t b = snb[e];
-            const double hvj = __shfl_sync(0xffffffffu, hv, j);
-            if constexpr (KIND == 0) {
-                // buildPreconditioner (3-conjugate-gradients/Fluid.cpp:253-269)
-                double pc_d = __shfl_up_sync(0xffffffffu, prev, 1);
-                F ax_d = __shfl_up_sync(0xffffffffu, prev_a, 1);
-                F ay_d = __shfl_up_sync(0xffffffffu, prev_b, 1);
-                const F haj = __shfl_sync(0xffffffffu, ha, j), hbj = __shfl_sync(0xffffffffu, hb, j);
-                if (lane == 0) {
-                    pc_d = hvj;
-                    ax_d = haj;
-                    ay_d = hbj;
+        const char *sbuf = R.buf + (size_t)st * Ring<F>::kStageBytes;
+        const F *s0 = (const F *)sbuf;
+        const F *s1 = (const F *)(sbuf + Ring<F>::kSlot);
+        const F *s2 = (const F *)(sbuf + 2 * Ring<F>::kSlot);
+        const F *s3 = (const F *)(sbuf + 3 * Ring<F>::kSlot);
+        const F *s4 = (const F *)(sbuf + 4 * Ring<F>::kSlot);
+        const uint8_t *snb = (const uint8_t *)(sbuf + 5 * Ring<F>::kSlot);
+        for (int sub = 0; sub < kB / kHB; sub++) {
+            const int t0 = blk * kB + sub * kHB;
+            // halo values of this sub-block: complete the prefetched words,
+            // then prefetch the next sub-block's columns
+            V hv = V(0);
+            F ha = F(0), hb = F(0);
+            if (has_in && lane < kHB) {
+                const int xc = halo_col(t0 + lane);
+                if (xc >= 0 && xc < W) {
+                    hv = hdec<V>(halo_take(in + xc, hpre, A.flags));
+                    ha = spre_a;
+                    hb = spre_b;
                 }
-                const F axv = s1[e], ayv = s2[e];
-                V val = prev;
-                if (active && (b & NB_SELF)) {
-                    const double diag = (double)f0[e];
+            }
+            prefetch(t0 + kHB);
+#pragma unroll
+            for (int jj = 0; jj < kHB; jj++) {
+                const int j = sub * kHB + jj;
+                const int t = t0 + jj;
+                const int d = bwd ? D - 1 - t : t;
+                const int e = (bwd ? (kB - 1 - j) : j) * 32 + lane;  // slot inside the staged block
+                const int x = d - lane;
+                const bool active = rowok && x >= 0 && x < W;
+                const size_t i = ((size_t)s * D + d) * 32 + lane;
+                const uint8_t b = snb[e];
+                const V hvj = __shfl_sync(FULL, hv, jj);
+                V val;
+                if constexpr (KIND == 0) {
+                    // buildPreconditioner (3-conjugate-gradients/Fluid.cpp:253-269)
+                    double pc_d = __shfl_up_sync(FULL, prev, 1);
+                    F ax_d = __shfl_up_sync(FULL, prev_a, 1);
+                    F ay_d = __shfl_up_sync(FULL, prev_b, 1);
+                    const F haj = __shfl_sync(FULL, ha, jj), hbj = __shfl_sync(FULL, hb, jj);
+                    if (lane == 0) {
+                        pc_d = hvj;
+                        ax_d = haj;
+                        ay_d = hbj;
+                    }
+                    const F axv = s1[e], ayv = s2[e];
+                    const double diag = (double)s0[e];
                     double ev = diag;
                     if (b & NB_LEFT) {
                         double px = (double)prev_a * prev;
@@ -360,67 +372,75 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring &R) {
                         ev = ev - (py * py + kTau * px * py);
                     }
                     if (ev < kSigma * diag) ev = diag;
-                    const double pcv = 1.0 / sqrt(ev);
-                    A.pc[i] = pcv;
-                    A.pcf[i] = (F)pcv;
-                    A.lx[i] = (F)((double)axv * pcv);
-                    A.ly[i] = (F)((double)ayv * pcv);
-                    val = pcv;
-                }
-                prev = val;
-                prev_a = axv;
-                prev_b = ayv;
-            } else if constexpr (KIND == 1) {
-                // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
-                F q_d = __shfl_up_sync(0xffffffffu, prev, 1);
-                F ly_d = __shfl_up_sync(0xffffffffu, prev_b, 1);
-                const F hbj = __shfl_sync(0xffffffffu, hb, j);
-                if (lane == 0) {
-                    q_d = (F)hvj;
-                    ly_d = hbj;
-                }
-                const F lxv = s1[e], lyv = s2[e];
-                V val = prev;
-                if (active && (b & NB_SELF)) {
-                    F tt = (F)d0[e];
-                    if (b & NB_LEFT) tt = tt - prev_a * prev;
-                    if (b & NB_DOWN) tt = tt - ly_d * q_d;
+                    val = 1.0 / sqrt(ev);
+                    if (active && (b & NB_SELF)) {
+                        A.pc[i] = val;
+                        A.pcf[i] = (F)val;
+                        A.lx[i] = (F)((double)axv * val);
+                        A.ly[i] = (F)((double)ayv * val);
+                    }
+                    prev_a = axv;
+                    prev_b = ayv;
+                } else if constexpr (KIND == 1) {
+                    // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
+                    const F q_sh = __shfl_up_sync(FULL, prev, 1);
+                    const F ly_sh = __shfl_up_sync(FULL, prev_b, 1);
+                    const F hbj = __shfl_sync(FULL, hb, jj);
+                    const F q_d = lane == 0 ? hvj : q_sh;
+                    const F ly_d = lane == 0 ? hbj : ly_sh;
+                    const F lxv = s1[e], lyv = s2[e];
+                    F tt = s0[e];
+                    tt = (b & NB_LEFT) ? tt - prev_a * prev : tt;
+                    tt = (b & NB_DOWN) ? tt - ly_d * q_d : tt;
                     val = tt * s3[e];
-                    A.z[i] = val;
-                }
-                prev = val;
-                prev_a = lxv;
-                prev_b = lyv;
-            } else {
-                // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
-                F z_u = __shfl_down_sync(0xffffffffu, prev, 1);
-                if (lane == 31) z_u = (F)hvj;
-                V val = prev;
-                if (active && (b & NB_SELF)) {
-                    F tt = f0[e];
-                    if (b & NB_RIGHT) tt = tt - s1[e] * prev;
-                    if (b & NB_UP) tt = tt - s2[e] * z_u;
+                    if (active && (b & NB_SELF)) A.z[i] = val;
+                    prev_a = lxv;
+                    prev_b = lyv;
+                } else {
+                    // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
+                    const F z_sh = __shfl_down_sync(FULL, prev, 1);
+                    const F z_u = lane == 31 ? hvj : z_sh;
+                    F tt = s0[e];
+                    tt = (b & NB_RIGHT) ? tt - s1[e] * prev : tt;
+                    tt = (b & NB_UP) ? tt - s2[e] * z_u : tt;
                     val = tt * s3[e];
-                    A.z[i] = val;
-                    if (b & NB_RED) dot = dacc(dot, (double)val, d4[e]);
+                    if (active && (b & NB_SELF)) {
+                        A.z[i] = val;
+                        if (b & NB_RED) dot = fma((double)val, (double)s4[e], dot);
+                    }
                 }
                 prev = val;
+                if (producer && active) hstore(out + x, henc(val));
             }
-            if (producer && active) halo_put(halo_out + x, (double)prev);
         }
     }
     __syncwarp();
     return dot;
 }
 
+// Sweep of all strips of this block; the halo rows between its own warps live
+// in shared memory, those to neighbouring blocks in global memory.
 template <int KIND, typename F>
-__device__ __forceinline__ double sweep(const PcgArgs<F> &A, Ring &R, bool sweeper) {
-    if (!sweeper) return 0.0;
-    return sweep_strip<KIND, F>(A, blockIdx.x, R);
+__device__ double sweep(const PcgArgs<F> &A, Ring<F> &R, unsigned long long *hsm, int nstrips_blk) {
+    const int w = threadIdx.x >> 5;
+    if (w >= nstrips_blk) return 0.0;
+    const SDIdx sd = A.sd;
+    const int s = blockIdx.x * A.K + w;
+    const size_t D = sd.D;
+    unsigned long long *up = A.halo, *down = A.halo + (size_t)sd.S * D;
+    unsigned long long *in = nullptr, *out = nullptr;
+    if (KIND != 2) {  // rows travel upward: strip s takes from s-1, gives to s+1
+        if (s > 0) in = (w > 0) ? hsm + (size_t)(w - 1) * D : up + (size_t)(s - 1) * D;
+        if (s + 1 < sd.S) out = (w + 1 < nstrips_blk) ? hsm + (size_t)w * D : up + (size_t)s * D;
+    } else {          // downward: strip s takes from s+1, gives to s-1
+        if (s + 1 < sd.S) in = (w + 1 < nstrips_blk) ? hsm + (size_t)w * D : down + (size_t)(s + 1) * D;
+        if (s > 0) out = (w > 0) ? hsm + (size_t)(w - 1) * D : down + (size_t)s * D;
+    }
+    return sweep_strip<KIND, F>(A, s, R, in, out);
 }
 
 template <typename F>
-__global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
+__global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
     extern __shared__ __align__(128) char smem_raw[];
     __shared__ double sm[kWarps + 1];
     const SDIdx sd = A.sd;
@@ -428,24 +448,29 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rows = sd.S * D;  // diagonals of all strips
     const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
-    const bool sweeper = warp == 0 && (int)blockIdx.x < sd.S;
+    int nstrips_blk = sd.S - (int)blockIdx.x * A.K;
+    nstrips_blk = nstrips_blk < 0 ? 0 : (nstrips_blk > A.K ? A.K : nstrips_blk);
+    constexpr bool kF32 = !std::is_same<F, double>::value;
 
-    Ring R;
-    R.bars = (uint64_t *)smem_raw;
-    R.buf = smem_raw + 128;
+    // shared memory: mbarriers | halo rows between this block's strips | rings
+    const size_t nh = (size_t)(A.K > 1 ? A.K - 1 : 0) * D;
+    uint64_t *bars = (uint64_t *)smem_raw;
+    unsigned long long *hsm = (unsigned long long *)(smem_raw + 32 * A.K);
+    char *rings = smem_raw + ((32 * A.K + nh * 8 + 127) / 128) * 128;
+    Ring<F> R;
+    R.bars = bars + warp * 4;
+    R.buf = rings + (size_t)warp * A.stages * Ring<F>::kStageBytes;
     R.stages = A.stages;
-    R.stage_bytes = A.stage_bytes;
     R.ii = R.ci = 0;
-    if (sweeper) {
-        if (lane == 0) {
-            for (int k = 0; k < R.stages; k++) mbar_init(R.bars + k, 1);
-            fence_mbar_init();
-        }
-        __syncwarp();
+    for (size_t k = threadIdx.x; k < nh; k += kThreads) hsm[k] = kSentinel;
+    if (warp < nstrips_blk && lane == 0) {
+        for (int k = 0; k < R.stages; k++) mbar_init(R.bars + k, 1);
+        fence_mbar_init();
     }
+    __syncthreads();
 
     if (A.mode & PCG_FACTOR) {
-        sweep<0, F>(A, R, sweeper);
+        sweep<0, F>(A, R, hsm, nstrips_blk);
         grid_barrier(A.barrier, A.flags);
     }
     if (!(A.mode & PCG_SOLVE)) return;
@@ -455,13 +480,15 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
     for (int row = gwarp; row < rows; row += nwarps) {
         const size_t i = (size_t)row * 32 + lane;
         A.p[i] = 0.0;
+        if (kF32) A.rf[i] = (F)A.r[i];
         if (A.nb[i] & NB_RED) mx = smax(mx, fabs(A.r[i]));
     }
     block_store(mx, true, A.partials, 0, sm);
+    if (kF32) grid_barrier(A.barrier, A.flags);  // FP32 copy of r complete
     // z = M^-1 r  (:351)
-    sweep<1, F>(A, R, sweeper);
+    sweep<1, F>(A, R, hsm, nstrips_blk);
     grid_barrier(A.barrier, A.flags);
-    double d = sweep<2, F>(A, R, sweeper);
+    double d = sweep<2, F>(A, R, hsm, nstrips_blk);
     block_store(d, false, A.partials, 2, sm);
     grid_barrier(A.barrier, A.flags);
 
@@ -477,7 +504,7 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
         for (int iter = 0; iter < A.limit; iter++) {
             if (timed_out(A.flags)) break;
             // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
-            double dacc_ = 0.0;
+            double dacc = 0.0;
             const F fbeta = (F)beta;
             for (int row = gwarp; row < rows; row += nwarps) {
                 const int s = row / D, dd = row - s * D;
@@ -485,27 +512,29 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
                 const size_t i = (size_t)row * 32 + lane;
                 if (x < 0 || x >= W || y >= H) {
                     s_new[i] = F(0);
-                    A.as[i] = F(0);
+                    A.as[i] = 0.0;
                     continue;
                 }
                 auto snew = [&](size_t k) -> F {
                     if (iter == 0) return A.z[k];
                     return (A.nb[k] & NB_RED) ? F(A.z[k] + s_old[k] * fbeta) : s_old[k];
                 };
+                // FP64 accumulation: with FP32 storage every product is exact,
+                // so the operator the recurrences see is the same every iteration.
                 const F sc = snew(i);
-                F t = A.adiag[i] * sc;
-                if (x > 0) t += A.ax[i - 32] * snew(i - 32);
+                double t = (double)A.adiag[i] * (double)sc;
+                if (x > 0) t += (double)A.ax[i - 32] * (double)snew(i - 32);
                 if (y > 0) {
                     const size_t k = lane > 0 ? i - 33 : sd.slot(x, y - 1);
-                    t += A.ay[k] * snew(k);
+                    t += (double)A.ay[k] * (double)snew(k);
                 }
-                if (x < W - 1) t += A.ax[i] * snew(i + 32);
-                if (y < H - 1) t += A.ay[i] * snew(lane < 31 ? i + 33 : sd.slot(x, y + 1));
+                if (x < W - 1) t += (double)A.ax[i] * (double)snew(i + 32);
+                if (y < H - 1) t += (double)A.ay[i] * (double)snew(lane < 31 ? i + 33 : sd.slot(x, y + 1));
                 s_new[i] = sc;
                 A.as[i] = t;
-                if (A.nb[i] & NB_RED) dacc_ = dacc(dacc_, t, sc);
+                if (A.nb[i] & NB_RED) dacc += t * (double)sc;
             }
-            block_store(dacc_, false, A.partials, 1, sm);
+            block_store(dacc, false, A.partials, 1, sm);
             grid_barrier(A.barrier, A.flags);
             const double alpha = sigma / grid_reduce(A.partials, 1, false, sm);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
@@ -514,8 +543,9 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
                 const size_t i = (size_t)row * 32 + lane;
                 if (A.nb[i] & NB_RED) {
                     A.p[i] = A.p[i] + (double)s_new[i] * alpha;
-                    const double rn = A.r[i] + (double)A.as[i] * -alpha;
+                    const double rn = A.r[i] + A.as[i] * -alpha;
                     A.r[i] = rn;
+                    if (kF32) A.rf[i] = (F)rn;
                     mx = smax(mx, fabs(rn));
                 }
             }
@@ -528,9 +558,9 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
                 break;
             }
             // z = M^-1 r; sigmaNew = z.r  (:372-376)
-            sweep<1, F>(A, R, sweeper);
+            sweep<1, F>(A, R, hsm, nstrips_blk);
             grid_barrier(A.barrier, A.flags);
-            d = sweep<2, F>(A, R, sweeper);
+            d = sweep<2, F>(A, R, hsm, nstrips_blk);
             block_store(d, false, A.partials, 2, sm);
             grid_barrier(A.barrier, A.flags);
             const double sigmaNew = grid_reduce(A.partials, 2, false, sm);
@@ -550,29 +580,31 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs<F> A) {
     }
 }
 
+// Strips per block: the rings of the sweeping warps and the halo rows between
+// them must fit in shared memory.
 template <typename F>
-int ring_stages() {
-    return 4;
+int strips_per_block() {
+    return sizeof(F) == 8 ? 2 : 4;
 }
+constexpr int kStages = 3;
 template <typename F>
-int ring_stage_bytes() {
-    return kStageBytes;
-}
-template <typename F>
-size_t smem_bytes() {
-    return 128 + (size_t)ring_stages<F>() * ring_stage_bytes<F>();
+size_t smem_bytes(int K, int D) {
+    const size_t nh = (size_t)(K > 1 ? K - 1 : 0) * D;
+    return ((32 * (size_t)K + nh * 8 + 127) / 128) * 128 + (size_t)K * kStages * Ring<F>::kStageBytes;
 }
 
 template <typename F>
-int max_coresident() {
+int max_coresident(size_t smem) {
+    static size_t cached_smem = 0;
     static int cached = -1;
-    if (cached < 0) {
+    if (cached < 0 || cached_smem != smem) {
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(pcg_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes<F>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel<F>, kThreads, smem_bytes<F>());
+        cudaFuncSetAttribute(pcg_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel<F>, kThreads, smem);
         cached = sms * (per > 2 ? 2 : per);
+        cached_smem = smem;
     }
     return cached;
 }
@@ -581,7 +613,10 @@ int max_coresident() {
 
 template <typename F>
 int pcg_max_blocks() {
-    return max_coresident<F>();
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return 2 * sms;
 }
 
 template <typename F>
@@ -599,37 +634,37 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     A.nb = S.nb;
     A.r = S.r;
     A.p = S.p;
+    A.as = S.as;
+    A.rf = S.rf;
     A.z = S.z;
     A.sa = S.sa;
     A.sb = S.sb;
-    A.as = S.as;
     A.partials = X.partials;
     A.barrier = X.barrier;
-    A.halo_up = X.halo_up;
-    A.halo_down = X.halo_down;
+    A.halo = X.halo;
     A.flags = S.flags;
     A.out = X.out + (cfg.heat ? 1 : 0);
     A.iter_total = X.iter_total;
     A.mode = cfg.mode;
     A.limit = cfg.limit;
     A.pinned = cfg.pinned;
-    A.stages = ring_stages<F>();
-    A.stage_bytes = ring_stage_bytes<F>();
-    int maxb = max_coresident<F>();
+    A.K = strips_per_block<F>();
+    if (A.K > S.sd.S) A.K = S.sd.S;
+    A.stages = kStages;
+    const size_t smem = smem_bytes<F>(A.K, S.sd.D);
+    int maxb = max_coresident<F>(smem);
     if (maxb > X.max_blocks) maxb = X.max_blocks;
-    if (maxb < S.sd.S) return cudaErrorInvalidConfiguration;  // one block per 32-row strip
+    const int need = (S.sd.S + A.K - 1) / A.K;  // blocks that own strips
+    if (maxb < need) return cudaErrorInvalidConfiguration;
     const long long slots = (long long)S.sd.total();
     int want = (int)((slots + kThreads * 4 - 1) / (kThreads * 4));
-    if (want < S.sd.S) want = S.sd.S;
+    if (want < need) want = need;
     int G = want < maxb ? want : maxb;
     if (blocks_used) *blocks_used = G;
     cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
-    const size_t halo = (size_t)S.sd.S * S.sd.D * sizeof(double);
-    cudaMemsetAsync(X.halo_up, 0xff, halo, st);  // every entry starts as the sentinel
-    cudaMemsetAsync(X.halo_down, 0xff, halo, st);
+    cudaMemsetAsync(X.halo, 0xff, 2 * (size_t)S.sd.S * S.sd.D * sizeof(unsigned long long), st);
     void *args[] = {&A};
-    return cudaLaunchCooperativeKernel((const void *)pcg_kernel<F>, dim3(G), dim3(kThreads), args,
-                                       smem_bytes<F>(), st);
+    return cudaLaunchCooperativeKernel((const void *)pcg_kernel<F>, dim3(G), dim3(kThreads), args, smem, st);
 }
 
 template cudaError_t launch_pcg<double>(const Scene<double> &, const PcgScratch &, const PcgConfig &,

@@ -316,7 +316,9 @@ class SolverImpl final : public SolverBase {
         S_.z = c.take<F>(base, NS);
         S_.sa = c.take<F>(base, NS);
         S_.sb = c.take<F>(base, NS);
-        S_.as = c.take<F>(base, NS);
+        S_.as = c.take<double>(base, NS);
+        if (sizeof(F) == 8) S_.rf = (F *)S_.r;
+        else S_.rf = c.take<F>(base, NS);
         S_.adiag = c.take<F>(base, NS);
         S_.ax = c.take<F>(base, NS);
         S_.ay = c.take<F>(base, NS);
@@ -338,8 +340,7 @@ class SolverImpl final : public SolverBase {
         scratch_.max_blocks = max_blocks_;
         scratch_.partials = c.take<double>(base, 4 * (size_t)std::max(max_blocks_, 1));
         scratch_.barrier = c.take<unsigned>(base, 2);
-        scratch_.halo_up = c.take<double>(base, (size_t)S_.sd.S * S_.sd.D);
-        scratch_.halo_down = c.take<double>(base, (size_t)S_.sd.S * S_.sd.D);
+        scratch_.halo = c.take<unsigned long long>(base, 2 * (size_t)S_.sd.S * S_.sd.D);
         scratch_.out = c.take<PcgOut>(base, 2);
         scratch_.iter_total = c.take<unsigned long long>(base, 1);
     }

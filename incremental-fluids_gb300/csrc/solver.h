@@ -4,7 +4,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/ifluids.h"
+#include "ifluids.h"
 #include "ifl_internal.h"
 
 namespace ifl {
