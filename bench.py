@@ -45,25 +45,25 @@ for _p in (ROOT, PKG):
 
 METRIC = "cell-steps/s"
 # Algorithmic bytes per cell of the persistent PCG kernel (strip-diagonal
-# arrays, F = storage width, neighbour bits 1 byte, FP64 factor):
-#   factor  reads adiag, ax, ay, nb; writes pc (8 B), pcf, lx, ly      = 6F + 9
-#   r, p and A*s are FP64 in both forms (R = 8 bytes).
-#   setup   p = 0 (R), |r|_inf (R + 1), forward (r, lx, ly, pcf, nb -> z:
-#           R + 4F + 1) and backward (z, lx, ly, pcf, r, nb -> z: R + 5F + 1)
-#                                                                      = 4R + 9F + 3
-#   per iteration: s-update + matvec + dot (z, s, adiag, ax, ay, nb ->
-#           s, As: R + 6F + 1), AXPYs + norm (p, s, r, As, nb -> p, r:
-#           5R + F + 1), forward (R + 4F + 1), backward (R + 5F + 1)   = 8R + 16F + 4
-#   the last iteration stops after the AXPYs (no substitutions)         = -(2R + 9F + 2)
+# arrays; F = storage width of the matrix and of z, s; r, p, A*s are FP64
+# (R = 8); nb = 1 byte of neighbour bits; the MIC record is {lx, ly, pc, nb}
+# in F; the FP32 form keeps an F copy of r for the substitutions):
+#   factor     adiag, ax, ay, nb -> pc (8 B), MIC record             = 7F + 9
+#   setup      p = 0, |r|_inf (r, nb), [r copy], forward (r, MIC -> z)
+#              and backward (z, r, MIC -> z) substitutions           = 2R + 1 + 13F [+ F]
+#   iteration  s-update + matvec + dot (z, s, nb, adiag, ax, ay -> s, As)
+#              AXPYs + norm (p, r, As, s, nb -> p, r [, r copy])
+#              forward (6F) and backward (7F)                        = 6R + 20F + 2 [+ F]
+#   the last iteration stops after the AXPYs                         = -13F
 
 
 def pcg_bytes_per_cell(F: int, launches: int, iterations: int) -> float:
     R = 8
-    factor = 6 * F + 9
-    setup = 4 * R + 9 * F + 3
-    per_iter = 8 * R + 16 * F + 4
-    last = 2 * R + 9 * F + 2
-    return launches * (factor + setup - last) + iterations * per_iter
+    copy = F if F == 4 else 0
+    factor = 7 * F + 9
+    setup = 2 * R + 1 + 13 * F + copy
+    per_iter = 6 * R + 20 * F + 2 + copy
+    return launches * (factor + setup - 13 * F) + iterations * per_iter
 
 
 def load_peaks():

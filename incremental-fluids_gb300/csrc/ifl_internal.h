@@ -89,7 +89,7 @@ struct Scene {
     F *rf;             // r in storage precision for the substitutions (aliases r for FP64)
     F *z, *sa, *sb;
     F *adiag, *ax, *ay;
-    F *lx, *ly, *pcf;  // MIC(0) apply operands in storage precision
+    F *mic;            // MIC(0) apply record per slot: {lx, ly, pc, neighbour bits}
     double *pc;        // MIC(0) factor, FP64
     uint8_t *nb;
     F *udens, *vdens;

@@ -531,7 +531,7 @@ __device__ __forceinline__ F q_cerp(const F *__restrict__ src, int P, int w, int
 // backtrace), 1 = u, 2 = v.  Every quantity reads the u, v sources and writes
 // its own destination, so all of them advect in one launch.
 template <typename F>
-__global__ void advect_kernel(Scene<F> S, F dt) {
+__global__ void advect_kernel(Scene<F> S, double dt) {
     const int z = blockIdx.z;
     const int qi = z == 0 ? 0 : z + 1;
     const Quant<F> &Q = S.q[qi];
@@ -544,38 +544,44 @@ __global__ void advect_kernel(Scene<F> S, F dt) {
     const Quant<F> &U = S.q[2], &V = S.q[3];
     const F hx = F(S.hx);
     const F uox = F(U.ox), uoy = F(U.oy), vox = F(V.ox), voy = F(V.oy);
-    F x = F(ix) + F(Q.ox);
-    F y = F(iy) + F(Q.oy);
+    // Positions are FP64 in both forms (the velocity samples and the
+    // interpolation run in the storage precision).  u and v faces sit on
+    // integer coordinates, where the truncation that selects the
+    // back-projection cell is discontinuous: an FP32 position would snap a
+    // near-zero displacement onto the face and pick another cell.
+    const double fdt = dt;
+    double x = ix + Q.ox;
+    double y = iy + Q.oy;
     {
-        F firstU = q_lerp(U.src, P, U.w, U.h, uox, uoy, x, y) / hx;
-        F firstV = q_lerp(V.src, P, V.w, V.h, vox, voy, x, y) / hx;
-        F midX = x - F(0.5) * dt * firstU;
-        F midY = y - F(0.5) * dt * firstV;
-        F midU = q_lerp(U.src, P, U.w, U.h, uox, uoy, midX, midY) / hx;
-        F midV = q_lerp(V.src, P, V.w, V.h, vox, voy, midX, midY) / hx;
-        F lastX = x - F(0.75) * dt * midU;
-        F lastY = y - F(0.75) * dt * midV;
-        F lastU = q_lerp(U.src, P, U.w, U.h, uox, uoy, lastX, lastY);
-        F lastV = q_lerp(V.src, P, V.w, V.h, vox, voy, lastX, lastY);
-        x -= dt * (F(2.0 / 9.0) * firstU + F(3.0 / 9.0) * midU + F(4.0 / 9.0) * lastU);
-        y -= dt * (F(2.0 / 9.0) * firstV + F(3.0 / 9.0) * midV + F(4.0 / 9.0) * lastV);
+        F firstU = q_lerp(U.src, P, U.w, U.h, uox, uoy, F(x), F(y)) / hx;
+        F firstV = q_lerp(V.src, P, V.w, V.h, vox, voy, F(x), F(y)) / hx;
+        double midX = x - 0.5 * fdt * (double)firstU;
+        double midY = y - 0.5 * fdt * (double)firstV;
+        F midU = q_lerp(U.src, P, U.w, U.h, uox, uoy, F(midX), F(midY)) / hx;
+        F midV = q_lerp(V.src, P, V.w, V.h, vox, voy, F(midX), F(midY)) / hx;
+        double lastX = x - 0.75 * fdt * (double)midU;
+        double lastY = y - 0.75 * fdt * (double)midV;
+        F lastU = q_lerp(U.src, P, U.w, U.h, uox, uoy, F(lastX), F(lastY));
+        F lastV = q_lerp(V.src, P, V.w, V.h, vox, voy, F(lastX), F(lastY));
+        x -= fdt * ((2.0 / 9.0) * (double)firstU + (3.0 / 9.0) * (double)midU + (4.0 / 9.0) * (double)lastU);
+        y -= fdt * ((2.0 / 9.0) * (double)firstV + (3.0 / 9.0) * (double)midV + (4.0 / 9.0) * (double)lastV);
     }
     if (solid) {
-        int rx = min(max((int)(x - F(Q.ox)), 0), Q.w - 1);
-        int ry = min(max((int)(y - F(Q.oy)), 0), Q.h - 1);
+        int rx = min(max((int)(x - Q.ox), 0), Q.w - 1);
+        int ry = min(max((int)(y - Q.oy), 0), Q.h - 1);
         size_t r = rx + (size_t)ry * P;
         if (Q.cell[r] != CELL_FLUID) {
-            double bx = ((double)x - Q.ox) * S.hx;
-            double by = ((double)y - Q.oy) * S.hx;
-            body_closest(S.bodies[Q.body[r]], bx, by);
-            x = F(bx / S.hx + Q.ox);
-            y = F(by / S.hx + Q.oy);
+            x = (x - Q.ox) * S.hx;
+            y = (y - Q.oy) * S.hx;
+            body_closest(S.bodies[Q.body[r]], x, y);
+            x = x / S.hx + Q.ox;
+            y = y / S.hx + Q.oy;
         }
     }
-    Q.dst[idx] = q_cerp(Q.src, P, Q.w, Q.h, F(Q.ox), F(Q.oy), x, y);
+    Q.dst[idx] = q_cerp(Q.src, P, Q.w, Q.h, F(Q.ox), F(Q.oy), F(x), F(y));
     if (z == 0 && S.nq == 4) {
         const Quant<F> &T = S.q[1];
-        T.dst[idx] = q_cerp(T.src, P, T.w, T.h, F(T.ox), F(T.oy), x, y);
+        T.dst[idx] = q_cerp(T.src, P, T.w, T.h, F(T.ox), F(T.oy), F(x), F(y));
     }
 }
 
@@ -650,7 +656,7 @@ void launch_extrapolate(const Scene<F> &S, unsigned qmask, cudaStream_t st) {
 template <typename F>
 void launch_advect(const Scene<F> &S, double dt, cudaStream_t st) {
     dim3 b(32, 8);
-    advect_kernel<F><<<grid2(S.w + 1, S.h + 1, 3, b), b, 0, st>>>(S, (F)dt);
+    advect_kernel<F><<<grid2(S.w + 1, S.h + 1, 3, b), b, 0, st>>>(S, dt);
 }
 
 template <typename F>

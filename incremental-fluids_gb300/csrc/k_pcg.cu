@@ -46,7 +46,6 @@ namespace {
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
-constexpr int kHB = 8;                           // halo columns fetched together
 constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
 constexpr double kTau = 0.97, kSigma = 0.25, kTol = 1e-5;
@@ -58,7 +57,7 @@ struct PcgArgs {
     SDIdx sd;
     const F *adiag, *ax, *ay;
     double *pc;
-    F *pcf, *lx, *ly;
+    F *mic;  // MIC record per slot: {lx, ly, pc, neighbour bits}
     const uint8_t *nb;
     double *r, *p, *as;
     F *rf;  // r in storage precision for the substitutions (== r when F is double)
@@ -202,15 +201,19 @@ __device__ __forceinline__ unsigned long long halo_take(unsigned long long *p, u
 }
 
 // --------------------------------------------------------------- sweeps
-// Per-warp shared-memory ring: `stages` buffers of kStageBytes, each holding
-// kB diagonals (kB*32 slots) of up to five F arrays followed by the
-// neighbour-bit bytes.  ii / ci count issued / consumed blocks over the whole
-// kernel, so buffer = count % stages and mbarrier parity = (count/stages) & 1.
+// Per-warp shared-memory ring: `stages` buffers, each holding kB diagonals
+// (kB*32 slots) of the streams of one sweep kind, in three regions:
+//   factor:   [adiag][ax][ay | neighbour bits]
+//   forward:  [r]    [--][MIC record]
+//   backward: [z]    [r] [MIC record]
+// A MIC record is {lx, ly, pc, neighbour bits} for one slot (lx = aPlusX*pc,
+// ly = aPlusY*pc, pc = precon, storage precision; written by the factor).
+// ii / ci count issued / consumed blocks over the whole kernel, so buffer =
+// count % stages and mbarrier parity = (count/stages) & 1.
 template <typename F>
 struct Ring {
     static constexpr unsigned kSlot = kB * 32 * sizeof(F);
-    static constexpr unsigned kNb = kB * 32;
-    static constexpr unsigned kStageBytes = 5 * kSlot + kNb;
+    static constexpr unsigned kStageBytes = 6 * kSlot;
     char *buf;
     uint64_t *bars;
     int stages;
@@ -230,40 +233,67 @@ __device__ __forceinline__ void ring_wait(Ring<F> &R, unsigned *flags) {
     R.ci++;
 }
 
-// Streams of one sweep kind: KIND 0 factor (adiag, ax, ay), 1 forward (r, lx,
-// ly, pcf), 2 backward (z, lx, ly, pcf, r); the neighbour bits follow.
 template <int KIND, typename F>
 __device__ __forceinline__ void ring_issue(Ring<F> &R, const PcgArgs<F> &A, int s, int blk) {
-    const int n = KIND == 0 ? 3 : KIND == 1 ? 4 : 5;
-    const F *src[5];
-    if (KIND == 0) {
-        src[0] = A.adiag; src[1] = A.ax; src[2] = A.ay; src[3] = src[4] = nullptr;
-    } else if (KIND == 1) {
-        src[0] = A.rf; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = nullptr;
-    } else {
-        src[0] = A.z; src[1] = A.lx; src[2] = A.ly; src[3] = A.pcf; src[4] = A.rf;
-    }
+    constexpr unsigned S1 = Ring<F>::kSlot;
     const int D = A.sd.D;
     const int d0 = (KIND == 2) ? D - (blk + 1) * kB : blk * kB;
     const size_t off = ((size_t)s * D + d0) * 32;
     const unsigned st = R.ii % R.stages;
     char *dst = R.buf + (size_t)st * Ring<F>::kStageBytes;
     uint64_t *bar = R.bars + st;
-    mbar_expect_tx(bar, n * Ring<F>::kSlot + Ring<F>::kNb);
-    for (int k = 0; k < n; k++) bulk_g2s(dst + k * Ring<F>::kSlot, src[k] + off, Ring<F>::kSlot, bar);
-    bulk_g2s(dst + 5 * Ring<F>::kSlot, A.nb + off, Ring<F>::kNb, bar);
+    if (KIND == 0) {
+        mbar_expect_tx(bar, 3 * S1 + kB * 32);
+        bulk_g2s(dst, A.adiag + off, S1, bar);
+        bulk_g2s(dst + S1, A.ax + off, S1, bar);
+        bulk_g2s(dst + 2 * S1, A.ay + off, S1, bar);
+        bulk_g2s(dst + 3 * S1, A.nb + off, kB * 32, bar);
+    } else if (KIND == 1) {
+        mbar_expect_tx(bar, 5 * S1);
+        bulk_g2s(dst, A.rf + off, S1, bar);
+        bulk_g2s(dst + 2 * S1, A.mic + 4 * off, 4 * S1, bar);
+    } else {
+        mbar_expect_tx(bar, 6 * S1);
+        bulk_g2s(dst, A.z + off, S1, bar);
+        bulk_g2s(dst + S1, A.rf + off, S1, bar);
+        bulk_g2s(dst + 2 * S1, A.mic + 4 * off, 4 * S1, bar);
+    }
     R.ii++;
 }
 
+__device__ __forceinline__ void ld4(const float *p, float &a, float &b, float &c, float &d) {
+    const float4 v = *(const float4 *)p;
+    a = v.x; b = v.y; c = v.z; d = v.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double &a, double &b, double &c, double &d) {
+    const double2 v0 = *(const double2 *)p, v1 = *(const double2 *)(p + 2);
+    a = v0.x; b = v0.y; c = v1.x; d = v1.y;
+}
+__device__ __forceinline__ void st4(float *p, float a, float b, float c, float d) {
+    *(float4 *)p = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void st4(double *p, double a, double b, double c, double d) {
+    *(double2 *)p = make_double2(a, b);
+    *(double2 *)(p + 2) = make_double2(c, d);
+}
+__device__ __forceinline__ unsigned nb_of(float w) { return __float_as_uint(w); }
+__device__ __forceinline__ unsigned nb_of(double w) { return (unsigned)__double_as_longlong(w); }
+__device__ __forceinline__ float nb_word(unsigned b, float) { return __uint_as_float(b); }
+__device__ __forceinline__ double nb_word(unsigned b, double) { return __longlong_as_double((long long)b); }
+
 // One strip of a wavefront sweep.  `in` is the halo row written by the
 // neighbouring strip this one depends on (nullptr: none), `out` the row this
-// strip hands on (nullptr: none).  Returns the lane's partial dot(z, r) for
-// the backward solve.
+// strip hands on (nullptr: none).  Each sub-block of kHB steps first stages
+// its operands from the ring into registers, then runs the dependency chain
+// (registers and shuffles only), then issues its stores.  Returns the lane's
+// partial dot(z, r) for the backward solve.
 template <int KIND, typename F>
 __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned long long *in,
                               unsigned long long *out) {
     using V = typename std::conditional<KIND == 0, double, F>::type;
+    constexpr int kHB = sizeof(F) == 8 ? 4 : 8;
     constexpr bool bwd = KIND == 2;
+    constexpr unsigned S1 = Ring<F>::kSlot;
     const int lane = threadIdx.x & 31;
     const SDIdx sd = A.sd;
     const int W = sd.W, H = sd.H, D = sd.D;
@@ -293,7 +323,9 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
                     spre_a = A.ax[k];
                     spre_b = A.ay[k];
                 } else if constexpr (KIND == 1) {
-                    spre_b = A.ly[sd.slot(xc, s * 32 - 1)];
+                    F a, b, c, d;
+                    ld4(A.mic + 4 * sd.slot(xc, s * 32 - 1), a, b, c, d);
+                    spre_b = b;  // ly of the cell below
                 }
             }
         }
@@ -314,16 +346,13 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
         const unsigned st = R.ci % R.stages;
         ring_wait(R, A.flags);
         const char *sbuf = R.buf + (size_t)st * Ring<F>::kStageBytes;
-        const F *s0 = (const F *)sbuf;
-        const F *s1 = (const F *)(sbuf + Ring<F>::kSlot);
-        const F *s2 = (const F *)(sbuf + 2 * Ring<F>::kSlot);
-        const F *s3 = (const F *)(sbuf + 3 * Ring<F>::kSlot);
-        const F *s4 = (const F *)(sbuf + 4 * Ring<F>::kSlot);
-        const uint8_t *snb = (const uint8_t *)(sbuf + 5 * Ring<F>::kSlot);
+        const F *g0 = (const F *)sbuf;
+        const F *g1 = (const F *)(sbuf + S1);
+        const F *g2 = (const F *)(sbuf + 2 * S1);
+        const uint8_t *gnb = (const uint8_t *)(sbuf + 3 * S1);
         for (int sub = 0; sub < kB / kHB; sub++) {
             const int t0 = blk * kB + sub * kHB;
-            // halo values of this sub-block: complete the prefetched words,
-            // then prefetch the next sub-block's columns
+            // halo words of this sub-block, then the next sub-block's prefetch
             V hv = V(0);
             F ha = F(0), hb = F(0);
             if (has_in && lane < kHB) {
@@ -335,31 +364,55 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
                 }
             }
             prefetch(t0 + kHB);
+            // stage this sub-block's operands in registers
+            F o0[kHB], o1[kHB], o2[kHB], o3[kHB], o4[kHB];
+            unsigned ob[kHB];
+            V hvv[kHB];
+            F hav[kHB], hbv[kHB];
 #pragma unroll
             for (int jj = 0; jj < kHB; jj++) {
                 const int j = sub * kHB + jj;
-                const int t = t0 + jj;
-                const int d = bwd ? D - 1 - t : t;
                 const int e = (bwd ? (kB - 1 - j) : j) * 32 + lane;  // slot inside the staged block
-                const int x = d - lane;
-                const bool active = rowok && x >= 0 && x < W;
-                const size_t i = ((size_t)s * D + d) * 32 + lane;
-                const uint8_t b = snb[e];
-                const V hvj = __shfl_sync(FULL, hv, jj);
+                if constexpr (KIND == 0) {
+                    o0[jj] = g0[e];
+                    o1[jj] = g1[e];
+                    o2[jj] = g2[e];
+                    ob[jj] = gnb[e];
+                    o3[jj] = o4[jj] = F(0);
+                } else if constexpr (KIND == 1) {
+                    F w3;
+                    o0[jj] = g0[e];
+                    ld4(g2 + 4 * e, o1[jj], o2[jj], o3[jj], w3);
+                    ob[jj] = nb_of(w3);
+                    o4[jj] = F(0);
+                } else {
+                    F w3;
+                    o0[jj] = g0[e];
+                    o4[jj] = g1[e];
+                    ld4(g2 + 4 * e, o1[jj], o2[jj], o3[jj], w3);
+                    ob[jj] = nb_of(w3);
+                }
+                hvv[jj] = __shfl_sync(FULL, hv, jj);
+                hav[jj] = __shfl_sync(FULL, ha, jj);
+                hbv[jj] = __shfl_sync(FULL, hb, jj);
+            }
+            // dependency chain
+            V res[kHB];
+#pragma unroll
+            for (int jj = 0; jj < kHB; jj++) {
+                const unsigned b = ob[jj];
                 V val;
                 if constexpr (KIND == 0) {
                     // buildPreconditioner (3-conjugate-gradients/Fluid.cpp:253-269)
                     double pc_d = __shfl_up_sync(FULL, prev, 1);
                     F ax_d = __shfl_up_sync(FULL, prev_a, 1);
                     F ay_d = __shfl_up_sync(FULL, prev_b, 1);
-                    const F haj = __shfl_sync(FULL, ha, jj), hbj = __shfl_sync(FULL, hb, jj);
                     if (lane == 0) {
-                        pc_d = hvj;
-                        ax_d = haj;
-                        ay_d = hbj;
+                        pc_d = hvv[jj];
+                        ax_d = hav[jj];
+                        ay_d = hbv[jj];
                     }
-                    const F axv = s1[e], ayv = s2[e];
-                    const double diag = (double)s0[e];
+                    const double diag = (double)o0[jj];
                     double ev = diag;
                     if (b & NB_LEFT) {
                         double px = (double)prev_a * prev;
@@ -373,44 +426,56 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
                     }
                     if (ev < kSigma * diag) ev = diag;
                     val = 1.0 / sqrt(ev);
-                    if (active && (b & NB_SELF)) {
-                        A.pc[i] = val;
-                        A.pcf[i] = (F)val;
-                        A.lx[i] = (F)((double)axv * val);
-                        A.ly[i] = (F)((double)ayv * val);
-                    }
-                    prev_a = axv;
-                    prev_b = ayv;
+                    prev_a = o1[jj];
+                    prev_b = o2[jj];
                 } else if constexpr (KIND == 1) {
                     // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
                     const F q_sh = __shfl_up_sync(FULL, prev, 1);
                     const F ly_sh = __shfl_up_sync(FULL, prev_b, 1);
-                    const F hbj = __shfl_sync(FULL, hb, jj);
-                    const F q_d = lane == 0 ? hvj : q_sh;
-                    const F ly_d = lane == 0 ? hbj : ly_sh;
-                    const F lxv = s1[e], lyv = s2[e];
-                    F tt = s0[e];
+                    const F q_d = lane == 0 ? hvv[jj] : q_sh;
+                    const F ly_d = lane == 0 ? hbv[jj] : ly_sh;
+                    F tt = o0[jj];
                     tt = (b & NB_LEFT) ? tt - prev_a * prev : tt;
                     tt = (b & NB_DOWN) ? tt - ly_d * q_d : tt;
-                    val = tt * s3[e];
-                    if (active && (b & NB_SELF)) A.z[i] = val;
-                    prev_a = lxv;
-                    prev_b = lyv;
+                    val = tt * o3[jj];
+                    prev_a = o1[jj];
+                    prev_b = o2[jj];
                 } else {
                     // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
                     const F z_sh = __shfl_down_sync(FULL, prev, 1);
-                    const F z_u = lane == 31 ? hvj : z_sh;
-                    F tt = s0[e];
-                    tt = (b & NB_RIGHT) ? tt - s1[e] * prev : tt;
-                    tt = (b & NB_UP) ? tt - s2[e] * z_u : tt;
-                    val = tt * s3[e];
-                    if (active && (b & NB_SELF)) {
-                        A.z[i] = val;
-                        if (b & NB_RED) dot = fma((double)val, (double)s4[e], dot);
-                    }
+                    const F z_u = lane == 31 ? hvv[jj] : z_sh;
+                    F tt = o0[jj];
+                    tt = (b & NB_RIGHT) ? tt - o1[jj] * prev : tt;
+                    tt = (b & NB_UP) ? tt - o2[jj] * z_u : tt;
+                    val = tt * o3[jj];
                 }
+                res[jj] = val;
                 prev = val;
-                if (producer && active) hstore(out + x, henc(val));
+            }
+            // stores
+#pragma unroll
+            for (int jj = 0; jj < kHB; jj++) {
+                const int t = t0 + jj;
+                const int d = bwd ? D - 1 - t : t;
+                const int x = d - lane;
+                const bool active = rowok && x >= 0 && x < W;
+                const size_t i = ((size_t)s * D + d) * 32 + lane;
+                const unsigned b = ob[jj];
+                if (active) {
+                    if constexpr (KIND == 0) {
+                        const bool self = b & NB_SELF;
+                        const double pcv = res[jj];
+                        if (self) A.pc[i] = pcv;
+                        st4(A.mic + 4 * i, self ? (F)((double)o1[jj] * pcv) : F(0),
+                            self ? (F)((double)o2[jj] * pcv) : F(0), self ? (F)pcv : F(0), nb_word(b, F(0)));
+                    } else {
+                        if (b & NB_SELF) {
+                            A.z[i] = res[jj];
+                            if (KIND == 2 && (b & NB_RED)) dot = fma((double)res[jj], (double)o4[jj], dot);
+                        }
+                    }
+                    if (producer) hstore(out + x, henc(res[jj]));
+                }
             }
         }
     }
@@ -628,9 +693,7 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     A.ax = S.ax;
     A.ay = S.ay;
     A.pc = S.pc;
-    A.pcf = S.pcf;
-    A.lx = S.lx;
-    A.ly = S.ly;
+    A.mic = S.mic;
     A.nb = S.nb;
     A.r = S.r;
     A.p = S.p;

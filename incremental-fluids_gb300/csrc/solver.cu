@@ -322,9 +322,7 @@ class SolverImpl final : public SolverBase {
         S_.adiag = c.take<F>(base, NS);
         S_.ax = c.take<F>(base, NS);
         S_.ay = c.take<F>(base, NS);
-        S_.lx = c.take<F>(base, NS);
-        S_.ly = c.take<F>(base, NS);
-        S_.pcf = c.take<F>(base, NS);
+        S_.mic = c.take<F>(base, 4 * NS);
         S_.pc = c.take<double>(base, NS);
         S_.nb = c.take<uint8_t>(base, NS);
         if (prm_.variant == IFL_VARDENS) {
