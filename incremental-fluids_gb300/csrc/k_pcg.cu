@@ -43,6 +43,10 @@ namespace ifl {
 
 namespace {
 
+// Dynamic shared memory of the PCG kernel, addressed through this symbol so
+// that every ring and halo access compiles to a shared-space instruction.
+extern __shared__ __align__(128) char g_smem[];
+
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
@@ -175,20 +179,36 @@ template <> __device__ __forceinline__ double hdec<double>(unsigned long long w)
 }
 template <> __device__ __forceinline__ float hdec<float>(unsigned long long w) { return __uint_as_float((unsigned)w); }
 
-__device__ __forceinline__ unsigned long long hload(const unsigned long long *p) {
-    return *(const volatile unsigned long long *)p;
+// Halo rows: shared memory (relaxed, CTA scope) inside a block, global memory
+// (relaxed, GPU scope) between blocks.  One 8-byte access is single-copy
+// atomic, so a reader sees either the sentinel or the whole value.
+struct Chan {
+    unsigned soff;             // byte offset in g_smem when shared
+    unsigned long long *g;     // global row when not shared
+    bool shared, valid;
+};
+__device__ __forceinline__ unsigned long long hload(const Chan &c, int x) {
+    unsigned long long v;
+    if (c.shared)
+        asm volatile("ld.relaxed.cta.shared.u64 %0, [%1];" : "=l"(v) : "r"(smem_u32(g_smem) + c.soff + 8u * x) : "memory");
+    else
+        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(c.g + x) : "memory");
+    return v;
 }
-__device__ __forceinline__ void hstore(unsigned long long *p, unsigned long long v) {
-    *(volatile unsigned long long *)p = v;
+__device__ __forceinline__ void hstore(const Chan &c, int x, unsigned long long v) {
+    if (c.shared)
+        asm volatile("st.relaxed.cta.shared.u64 [%0], %1;" ::"r"(smem_u32(g_smem) + c.soff + 8u * x), "l"(v) : "memory");
+    else
+        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(c.g + x), "l"(v) : "memory");
 }
 
 // Take a halo word (bounded poll), then put the sentinel back for the next sweep.
-__device__ __forceinline__ unsigned long long halo_take(unsigned long long *p, unsigned long long pre,
+__device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, unsigned long long pre,
                                                         unsigned *flags) {
     unsigned long long v = pre;
     long long n = 0;
     while (v == kSentinel) {
-        v = hload(p);
+        v = hload(c, x);
         if (v != kSentinel) break;
         if (++n > kWaitLimit || timed_out(flags)) {
             atomicOr(flags, FLAG_TIMEOUT);
@@ -196,7 +216,7 @@ __device__ __forceinline__ unsigned long long halo_take(unsigned long long *p, u
             break;
         }
     }
-    hstore(p, kSentinel);
+    hstore(c, x, kSentinel);
     return v;
 }
 
@@ -214,17 +234,18 @@ template <typename F>
 struct Ring {
     static constexpr unsigned kSlot = kB * 32 * sizeof(F);
     static constexpr unsigned kStageBytes = 6 * kSlot;
-    char *buf;
-    uint64_t *bars;
+    unsigned buf;   // byte offset of this warp's stages in g_smem
+    unsigned bars;  // byte offset of this warp's mbarriers in g_smem
     int stages;
     unsigned ii, ci;
+    __device__ __forceinline__ uint64_t *bar(unsigned st) const { return (uint64_t *)(g_smem + bars) + st; }
 };
 
 template <typename F>
 __device__ __forceinline__ void ring_wait(Ring<F> &R, unsigned *flags) {
     const unsigned st = R.ci % R.stages, parity = (R.ci / R.stages) & 1u;
     long long n = 0;
-    while (!mbar_try_wait(R.bars + st, parity)) {
+    while (!mbar_try_wait(R.bar(st), parity)) {
         if (++n > kMbarWaitLimit || timed_out(flags)) {
             atomicOr(flags, FLAG_TIMEOUT);
             break;
@@ -240,8 +261,8 @@ __device__ __forceinline__ void ring_issue(Ring<F> &R, const PcgArgs<F> &A, int 
     const int d0 = (KIND == 2) ? D - (blk + 1) * kB : blk * kB;
     const size_t off = ((size_t)s * D + d0) * 32;
     const unsigned st = R.ii % R.stages;
-    char *dst = R.buf + (size_t)st * Ring<F>::kStageBytes;
-    uint64_t *bar = R.bars + st;
+    char *dst = g_smem + R.buf + st * Ring<F>::kStageBytes;
+    uint64_t *bar = R.bar(st);
     if (KIND == 0) {
         mbar_expect_tx(bar, 3 * S1 + kB * 32);
         bulk_g2s(dst, A.adiag + off, S1, bar);
@@ -288,8 +309,7 @@ __device__ __forceinline__ double nb_word(unsigned b, double) { return __longlon
 // (registers and shuffles only), then issues its stores.  Returns the lane's
 // partial dot(z, r) for the backward solve.
 template <int KIND, typename F>
-__device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned long long *in,
-                              unsigned long long *out) {
+__device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan in, const Chan out) {
     using V = typename std::conditional<KIND == 0, double, F>::type;
     constexpr int kHB = sizeof(F) == 8 ? 4 : 8;
     constexpr bool bwd = KIND == 2;
@@ -300,8 +320,8 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
     const int y = s * 32 + lane;
     const bool rowok = y < H;
     const int nblk = D / kB;
-    const bool has_in = in != nullptr;
-    const bool producer = out != nullptr && lane == (bwd ? 0 : 31);
+    const bool has_in = in.valid;
+    const bool producer = out.valid && lane == (bwd ? 0 : 31);
     double dot = 0.0;
 
     V prev = V(0);                   // result of the previous cell in sweep order
@@ -317,7 +337,7 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
         if (has_in && lane < kHB) {
             const int xc = halo_col(t0 + lane);
             if (xc >= 0 && xc < W) {
-                hpre = hload(in + xc);
+                hpre = hload(in, xc);
                 if constexpr (KIND == 0) {
                     const size_t k = sd.slot(xc, s * 32 - 1);
                     spre_a = A.ax[k];
@@ -345,7 +365,7 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
         }
         const unsigned st = R.ci % R.stages;
         ring_wait(R, A.flags);
-        const char *sbuf = R.buf + (size_t)st * Ring<F>::kStageBytes;
+        const char *sbuf = g_smem + R.buf + st * Ring<F>::kStageBytes;
         const F *g0 = (const F *)sbuf;
         const F *g1 = (const F *)(sbuf + S1);
         const F *g2 = (const F *)(sbuf + 2 * S1);
@@ -358,7 +378,7 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
             if (has_in && lane < kHB) {
                 const int xc = halo_col(t0 + lane);
                 if (xc >= 0 && xc < W) {
-                    hv = hdec<V>(halo_take(in + xc, hpre, A.flags));
+                    hv = hdec<V>(halo_take(in, xc, hpre, A.flags));
                     ha = spre_a;
                     hb = spre_b;
                 }
@@ -474,7 +494,7 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
                             if (KIND == 2 && (b & NB_RED)) dot = fma((double)res[jj], (double)o4[jj], dot);
                         }
                     }
-                    if (producer) hstore(out + x, henc(res[jj]));
+                    if (producer) hstore(out, x, henc(res[jj]));
                 }
             }
         }
@@ -485,28 +505,30 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, unsigned l
 
 // Sweep of all strips of this block; the halo rows between its own warps live
 // in shared memory, those to neighbouring blocks in global memory.
+// hsm_off: byte offset in g_smem of the K-1 shared halo rows (D words each).
 template <int KIND, typename F>
-__device__ double sweep(const PcgArgs<F> &A, Ring<F> &R, unsigned long long *hsm, int nstrips_blk) {
+__device__ double sweep(const PcgArgs<F> &A, Ring<F> &R, unsigned hsm_off, int nstrips_blk) {
     const int w = threadIdx.x >> 5;
     if (w >= nstrips_blk) return 0.0;
     const SDIdx sd = A.sd;
     const int s = blockIdx.x * A.K + w;
     const size_t D = sd.D;
     unsigned long long *up = A.halo, *down = A.halo + (size_t)sd.S * D;
-    unsigned long long *in = nullptr, *out = nullptr;
+    auto smem_row = [&](int k) { return Chan{hsm_off + 8u * (unsigned)(k * D), nullptr, true, true}; };
+    auto glob_row = [&](unsigned long long *row) { return Chan{0u, row, false, true}; };
+    Chan in{0u, nullptr, false, false}, out{0u, nullptr, false, false};
     if (KIND != 2) {  // rows travel upward: strip s takes from s-1, gives to s+1
-        if (s > 0) in = (w > 0) ? hsm + (size_t)(w - 1) * D : up + (size_t)(s - 1) * D;
-        if (s + 1 < sd.S) out = (w + 1 < nstrips_blk) ? hsm + (size_t)w * D : up + (size_t)s * D;
+        if (s > 0) in = (w > 0) ? smem_row(w - 1) : glob_row(up + (size_t)(s - 1) * D);
+        if (s + 1 < sd.S) out = (w + 1 < nstrips_blk) ? smem_row(w) : glob_row(up + (size_t)s * D);
     } else {          // downward: strip s takes from s+1, gives to s-1
-        if (s + 1 < sd.S) in = (w + 1 < nstrips_blk) ? hsm + (size_t)w * D : down + (size_t)(s + 1) * D;
-        if (s > 0) out = (w > 0) ? hsm + (size_t)(w - 1) * D : down + (size_t)s * D;
+        if (s + 1 < sd.S) in = (w + 1 < nstrips_blk) ? smem_row(w) : glob_row(down + (size_t)(s + 1) * D);
+        if (s > 0) out = (w > 0) ? smem_row(w - 1) : glob_row(down + (size_t)s * D);
     }
     return sweep_strip<KIND, F>(A, s, R, in, out);
 }
 
 template <typename F>
 __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
-    extern __shared__ __align__(128) char smem_raw[];
     __shared__ double sm[kWarps + 1];
     const SDIdx sd = A.sd;
     const int W = sd.W, H = sd.H, D = sd.D;
@@ -519,23 +541,22 @@ __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
 
     // shared memory: mbarriers | halo rows between this block's strips | rings
     const size_t nh = (size_t)(A.K > 1 ? A.K - 1 : 0) * D;
-    uint64_t *bars = (uint64_t *)smem_raw;
-    unsigned long long *hsm = (unsigned long long *)(smem_raw + 32 * A.K);
-    char *rings = smem_raw + ((32 * A.K + nh * 8 + 127) / 128) * 128;
+    const unsigned hsm_off = 32u * A.K;
+    const unsigned rings = (unsigned)(((32 * A.K + nh * 8 + 127) / 128) * 128);
     Ring<F> R;
-    R.bars = bars + warp * 4;
-    R.buf = rings + (size_t)warp * A.stages * Ring<F>::kStageBytes;
+    R.bars = 32u * warp;
+    R.buf = rings + (unsigned)warp * A.stages * Ring<F>::kStageBytes;
     R.stages = A.stages;
     R.ii = R.ci = 0;
-    for (size_t k = threadIdx.x; k < nh; k += kThreads) hsm[k] = kSentinel;
+    for (size_t k = threadIdx.x; k < nh; k += kThreads) ((unsigned long long *)(g_smem + hsm_off))[k] = kSentinel;
     if (warp < nstrips_blk && lane == 0) {
-        for (int k = 0; k < R.stages; k++) mbar_init(R.bars + k, 1);
+        for (int k = 0; k < R.stages; k++) mbar_init(R.bar(k), 1);
         fence_mbar_init();
     }
     __syncthreads();
 
     if (A.mode & PCG_FACTOR) {
-        sweep<0, F>(A, R, hsm, nstrips_blk);
+        sweep<0, F>(A, R, hsm_off, nstrips_blk);
         grid_barrier(A.barrier, A.flags);
     }
     if (!(A.mode & PCG_SOLVE)) return;
@@ -551,9 +572,9 @@ __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
     block_store(mx, true, A.partials, 0, sm);
     if (kF32) grid_barrier(A.barrier, A.flags);  // FP32 copy of r complete
     // z = M^-1 r  (:351)
-    sweep<1, F>(A, R, hsm, nstrips_blk);
+    sweep<1, F>(A, R, hsm_off, nstrips_blk);
     grid_barrier(A.barrier, A.flags);
-    double d = sweep<2, F>(A, R, hsm, nstrips_blk);
+    double d = sweep<2, F>(A, R, hsm_off, nstrips_blk);
     block_store(d, false, A.partials, 2, sm);
     grid_barrier(A.barrier, A.flags);
 
@@ -623,9 +644,9 @@ __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
                 break;
             }
             // z = M^-1 r; sigmaNew = z.r  (:372-376)
-            sweep<1, F>(A, R, hsm, nstrips_blk);
+            sweep<1, F>(A, R, hsm_off, nstrips_blk);
             grid_barrier(A.barrier, A.flags);
-            d = sweep<2, F>(A, R, hsm, nstrips_blk);
+            d = sweep<2, F>(A, R, hsm_off, nstrips_blk);
             block_store(d, false, A.partials, 2, sm);
             grid_barrier(A.barrier, A.flags);
             const double sigmaNew = grid_reduce(A.partials, 2, false, sm);
