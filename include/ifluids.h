@@ -195,6 +195,35 @@ typedef struct {
 int ifl_set_timing(ifl_solver *s, int on);
 int ifl_get_timing(ifl_solver *s, ifl_timing *out);
 
+/* Pressure solve that allocates nothing.  This entry point has no counterpart
+ * in the reference: it serves callers that cannot allocate device memory
+ * while they run (code inside another framework's memory pool or under a
+ * fixed memory budget, real-time loops that must not enter the allocator,
+ * processes that forbid cudaMalloc after start-up).
+ *
+ * Solves the unmasked MIC(0)-preconditioned CG system of
+ * 3-conjugate-gradients (buildPreconditioner + project) for a w x h grid:
+ * adiag, aplusx, aplusy, rhs and p are DEVICE arrays, dense row-major
+ * (idx = x + y*w), FP64; `stats` is a DEVICE ifl_pcg_stats the solve writes
+ * its outcome into (status -1: a bounded device-side wait timed out).
+ * Work is enqueued on `stream` (NULL: the default stream); nothing is
+ * synchronised.
+ *
+ * Every intermediate array lives in one fixed device array inside the
+ * library (about 8.4 MB, held by every GPU that loads the library until the
+ * process exits).  Limit: the grid must fit 2304 strip-diagonals, i.e.
+ * ceil(h/32) * round_up(w + 31, 16) <= 2304 (for example 256 x 256); larger
+ * grids return IFL_ERR_UNSUPPORTED without touching the GPU.  It calls no
+ * cudaMalloc, cudaFree or other allocating routine.  All calls share that
+ * array, which keeps the last call's contents: calls whose work overlaps on
+ * the GPU (different streams, or different host threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture. */
+int ifl_pcg_solve_noalloc(int w, int h, const double *adiag, const double *aplusx,
+                          const double *aplusy, const double *rhs, double *p, int max_iter,
+                          ifl_pcg_stats *stats, void *stream);
+
 int ifl_synchronize(ifl_solver *s);
 void *ifl_stream(ifl_solver *s);
 /* Kernel launches of this library issued by the handle since creation. */

@@ -37,7 +37,7 @@ EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", 
            "ifl_advance_bodies", "ifl_add_inflow", "ifl_update", "ifl_run_phase", "ifl_ambient_t",
            "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_flip", "ifl_get_stats",
            "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
-           "ifl_set_timing", "ifl_get_timing",
+           "ifl_set_timing", "ifl_get_timing", "ifl_pcg_solve_noalloc",
            "ifl_last_error", "ifl_version")
 
 
@@ -118,6 +118,7 @@ def load_library(path: str = LIB_PATH):
     L.ifl_set_pinned_iterations.argtypes = [vp, i, i]
     L.ifl_synchronize.argtypes = [vp]
     L.ifl_set_timing.argtypes = [vp, i]
+    L.ifl_pcg_solve_noalloc.argtypes = [i, i, vp, vp, vp, vp, vp, i, vp, vp]
     L.ifl_get_timing.argtypes = [vp, C.POINTER(Timing)]
     L.ifl_stream.argtypes = [vp]
     L.ifl_stream.restype = vp
@@ -128,6 +129,13 @@ def load_library(path: str = LIB_PATH):
     L.ifl_version.restype = C.c_char_p
     _lib = L
     return L
+
+
+def pcg_solve_noalloc(w: int, h: int, adiag: int, aplusx: int, aplusy: int, rhs: int, p: int,
+                      max_iter: int, stats: int, stream: int = 0) -> int:
+    """ifl_pcg_solve_noalloc on device pointers (see include/ifluids.h); returns the status."""
+    return int(load_library().ifl_pcg_solve_noalloc(w, h, adiag, aplusx, aplusy, rhs, p, max_iter, stats,
+                                                    stream or None))
 
 
 class SolidBody:
