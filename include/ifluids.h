@@ -224,6 +224,77 @@ int ifl_pcg_solve_noalloc(int w, int h, const double *adiag, const double *aplus
                           const double *aplusy, const double *rhs, double *p, int max_iter,
                           ifl_pcg_stats *stats, void *stream);
 
+/* ------------------------------------------------------------------ batches
+ * Many independent scenes advanced together.  The reference runs one
+ * FluidSolver per process and has no batch; a batch replaces a loop of
+ * `solver.update(dt)` calls over many handles (3-conjugate-gradients/Fluid.cpp:433-447
+ * ... 7-variable-density/Fluid.cpp:995-1034, once per handle) by one step of
+ * batched launches: each phase runs for every scene in one launch and both
+ * PCG solves of every scene run in one persistent cooperative launch whose
+ * teams of blocks take scenes from work queues.  Results per scene equal
+ * ifl_update on that handle (same arithmetic; FP64 sums of the PCG in a
+ * different fixed order).
+ *
+ * Members are caller-owned handles of one device, variant and precision;
+ * they must outlive the batch and must not be used by other threads during
+ * ifl_batch_update.  Between batch steps each member remains a normal handle
+ * (read fields, set bodies, ...). */
+typedef struct ifl_batch ifl_batch;
+
+/* One inflow rectangle with the arguments of FluidSolver::addInflow. */
+typedef struct {
+    double x, y, w, h, d, t, u, v;
+} ifl_inflow;
+
+typedef struct {
+    /* Shape of the batched PCG launch: threads per block (64, 128 or 256),
+     * strips per block, bulk-copy ring stages.  threads = 0: autotune at the
+     * first update (each candidate shape runs a few pinned PCG iterations of
+     * the real system; the fastest is kept). */
+    int32_t threads, strips_per_block, stages;
+    int32_t use_graph;        /* 1: replay each step as one CUDA graph (default) */
+    int32_t tune_iterations;  /* PCG iterations per autotuning trial (default 8) */
+    int32_t pad_;
+} ifl_batch_options;
+
+typedef struct {
+    int32_t members;
+    int32_t threads, strips_per_block, stages;  /* PCG shape in use            */
+    int32_t grid;                               /* blocks of the PCG launch    */
+    int32_t graph;                              /* 1: steps replay a CUDA graph */
+    int32_t candidates;                         /* shapes tried by the autotuner */
+    int32_t pad_;
+    double candidate_ms[8];                     /* trial time of each candidate */
+    double last_step_ms;                        /* device time of the last step */
+    double last_pcg_ms;                         /* of which PCG launches        */
+    int64_t launches;                           /* kernels launched by the batch */
+    int64_t steps;
+} ifl_batch_info;
+
+void ifl_batch_default_options(ifl_batch_options *o);
+int ifl_batch_create(ifl_solver *const *members, int n, const ifl_batch_options *opt, ifl_batch **out);
+int ifl_batch_destroy(ifl_batch *b);
+/* Inflows applied at the start of every batch step, in order (the batched
+ * form of calling addInflow before each update); replaces the member's list. */
+int ifl_batch_set_inflows(ifl_batch *b, int member, const ifl_inflow *rects, int n);
+/* One update(dt) of every member; returns when the step has completed.  The
+ * members' current body tables are used (see ifl_set_bodies). */
+int ifl_batch_update(ifl_batch *b, double dt);
+/* Per-member PCG outcome of the last batch step (n = member count). */
+int ifl_batch_get_stats(ifl_batch *b, ifl_step_stats *out, int n);
+int ifl_batch_get_info(ifl_batch *b, ifl_batch_info *out);
+void *ifl_batch_stream(ifl_batch *b);
+/* Host-only preview of how a batched PCG launch of `grid` blocks splits into
+ * teams (no GPU work).  Scene i has strips[i] 32-row strips and estimated work
+ * work[i]; it is solved by a team of the smallest power-of-two block count that
+ * covers its strips.  teams[c] (c < 8) receives the number of teams of 2^c
+ * blocks.  Returns the blocks placed in teams, or IFL_ERR_UNSUPPORTED when
+ * the grid cannot hold one team of every size needed. */
+int ifl_batch_plan_teams(int grid, int strips_per_block, int n, const int *strips, const double *work,
+                         int *teams);
+/* NULL: why the last ifl_batch_create on this thread failed. */
+const char *ifl_batch_last_error(const ifl_batch *b);
+
 int ifl_synchronize(ifl_solver *s);
 void *ifl_stream(ifl_solver *s);
 /* Kernel launches of this library issued by the handle since creation. */

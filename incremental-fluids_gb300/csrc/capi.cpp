@@ -3,11 +3,16 @@
 // every failure into a status code; no exception crosses the ABI.
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "solver.h"
 
 struct ifl_solver {
     std::unique_ptr<ifl::SolverBase> impl;
+};
+
+struct ifl_batch {
+    std::unique_ptr<ifl::BatchBase> impl;
 };
 
 namespace {
@@ -25,6 +30,25 @@ int guarded(ifl_solver *s, Fn fn) {
         return IFL_ERR_NOMEM;
     } catch (...) {
         s->impl->set_error("internal error");
+        return IFL_ERR_ARG;
+    }
+}
+thread_local std::string g_batch_create_error;
+
+template <typename Fn>
+int bguarded(ifl_batch *b, Fn fn) {
+    if (!b || !b->impl) return IFL_ERR_ARG;
+    if (cudaSetDevice(b->impl->device()) != cudaSuccess) {
+        b->impl->set_error("cannot make the batch's device current");
+        return IFL_ERR_CUDA;
+    }
+    try {
+        return fn(*b->impl);
+    } catch (const std::bad_alloc &) {
+        b->impl->set_error("host allocation failed");
+        return IFL_ERR_NOMEM;
+    } catch (...) {
+        b->impl->set_error("internal error");
         return IFL_ERR_ARG;
     }
 }
@@ -182,6 +206,92 @@ const char *ifl_last_error(const ifl_solver *s) {
     return (s && s->impl) ? s->impl->error().c_str() : "invalid handle";
 }
 
-const char *ifl_version(void) { return "ifluids-gb300 0.1 (sm_103a)"; }
+const char *ifl_version(void) { return "ifluids-gb300 0.2 (sm_103a)"; }
+
+// ------------------------------------------------------------------ batches
+void ifl_batch_default_options(ifl_batch_options *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->use_graph = 1;
+    o->tune_iterations = 8;
+}
+
+int ifl_batch_create(ifl_solver *const *members, int n, const ifl_batch_options *opt, ifl_batch **out) {
+    if (!members || n <= 0 || !out) return IFL_ERR_ARG;
+    *out = nullptr;
+    ifl_batch_options o;
+    if (opt) o = *opt;
+    else ifl_batch_default_options(&o);
+    std::vector<ifl::SolverBase *> m(n);
+    for (int i = 0; i < n; i++) {
+        if (!members[i] || !members[i]->impl) return IFL_ERR_ARG;
+        m[i] = members[i]->impl.get();
+    }
+    ifl_batch *b = new (std::nothrow) ifl_batch;
+    if (!b) return IFL_ERR_NOMEM;
+    if (m[0]->activate() != 0) {
+        delete b;
+        return IFL_ERR_CUDA;
+    }
+    std::string err;
+    int e;
+    try {
+        e = ifl::make_batch(m.data(), n, o, &b->impl, &err);
+    } catch (...) {
+        e = IFL_ERR_NOMEM;
+        err = "host allocation failed";
+    }
+    if (e != IFL_OK) {
+        g_batch_create_error = err.empty() ? "invalid batch arguments" : err;
+        delete b;
+        return e;
+    }
+    *out = b;
+    return IFL_OK;
+}
+
+int ifl_batch_destroy(ifl_batch *b) {
+    if (!b) return IFL_ERR_ARG;
+    if (b->impl) cudaSetDevice(b->impl->device());
+    delete b;
+    return IFL_OK;
+}
+
+int ifl_batch_set_inflows(ifl_batch *b, int member, const ifl_inflow *rects, int n) {
+    return bguarded(b, [&](ifl::BatchBase &v) { return v.set_inflows(member, rects, n); });
+}
+
+int ifl_batch_update(ifl_batch *b, double dt) {
+    return bguarded(b, [&](ifl::BatchBase &v) { return v.update(dt); });
+}
+
+int ifl_batch_get_stats(ifl_batch *b, ifl_step_stats *out, int n) {
+    return bguarded(b, [&](ifl::BatchBase &v) { return v.get_stats(out, n); });
+}
+
+int ifl_batch_get_info(ifl_batch *b, ifl_batch_info *out) {
+    if (!out) return IFL_ERR_ARG;
+    return bguarded(b, [&](ifl::BatchBase &v) { return v.info(out); });
+}
+
+int ifl_batch_plan_teams(int grid, int strips_per_block, int n, const int *strips, const double *work,
+                         int *teams) {
+    if (grid <= 0 || strips_per_block <= 0 || n <= 0 || !strips || !work || !teams) return IFL_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (strips[i] <= 0 || !(work[i] >= 0.0)) return IFL_ERR_ARG;
+    try {
+        const int used = ifl::pcg_plan_teams(grid, strips_per_block, n, strips, work, teams, nullptr);
+        return used < 0 ? (int)IFL_ERR_UNSUPPORTED : used;
+    } catch (...) {
+        return IFL_ERR_NOMEM;
+    }
+}
+
+void *ifl_batch_stream(ifl_batch *b) { return (b && b->impl) ? (void *)b->impl->stream() : nullptr; }
+
+const char *ifl_batch_last_error(const ifl_batch *b) {
+    if (!b) return g_batch_create_error.c_str();  // why the last ifl_batch_create on this thread failed
+    return b->impl ? b->impl->error().c_str() : "invalid batch";
+}
 
 }  // extern "C"

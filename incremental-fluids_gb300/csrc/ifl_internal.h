@@ -19,6 +19,8 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -123,6 +125,13 @@ struct PcgConfig {
     int heat;  // 1: writes to the heat PcgOut slot
 };
 
+// Launch shape of the batched PCG kernel (chosen by the batch autotuner).
+struct PcgShape {
+    int threads;  // 64, 128 or 256 threads per block
+    int K;        // strips (sweeping warps) per block, <= threads / 32
+    int stages;   // bulk-copy ring stages per sweeping warp, 2..4
+};
+
 // Launchers (stream-ordered, no host synchronisation).
 template <typename F> void launch_inflow(const Scene<F> &S, int qi, double x0, double y0, double x1,
                                          double y1, double val, cudaStream_t st);
@@ -139,6 +148,55 @@ template <typename F> void launch_sd_to_rows(const Scene<F> &S, F *rows, const d
 template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
                                              cudaStream_t st, int *blocks_used);
 template <typename F> int pcg_max_blocks();
+
+// Batched PCG: many scenes in one cooperative launch (k_pcg.cu).  The plan
+// holds the per-scene job tables and the team/queue tables on the device.
+struct PcgBatchPlan;
+template <typename F>
+PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *const *scratch, int n,
+                               const PcgShape &shape, std::string *err);
+void pcg_batch_destroy(PcgBatchPlan *P);
+int pcg_batch_grid(const PcgBatchPlan *P);
+// Rebuilds teams and queues from the estimated work per scene (stream-ordered upload).
+int pcg_batch_schedule(PcgBatchPlan *P, const double *work, cudaStream_t st);
+// Team plan (host only): teams[c] = teams of 2^c blocks, c < 8; queues[c] =
+// scenes of class c by decreasing work.  Returns the blocks used, -1 if the grid is too small.
+int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work, int *teams,
+                   std::vector<std::vector<int>> *queues);
+// Device table of per-scene {pinned pressure, pinned heat, limit pressure, limit heat}.
+int4 *pcg_batch_ctl(PcgBatchPlan *P);
+template <typename F> cudaError_t launch_pcg_batch(PcgBatchPlan *P, const PcgConfig &cfg, cudaStream_t st);
+
+// ------------------------------------------------------------ batches
+// One inflow rectangle of one quantity (FluidQuantity::addInflow arguments).
+struct BatchInflow {
+    int q, pad_;
+    double x0, y0, x1, y1, val;
+};
+
+// Tiles of 32x8 threads that cover every grid of a w x h scene.
+inline int batch_tiles(int w, int h) { return ((w + 2 + 31) / 32) * ((h + 2 + 7) / 8); }
+
+// Device view of a batch of scenes for the batched phase launches.
+template <typename F>
+struct SceneBatch {
+    const Scene<F> *scenes;        // n scenes
+    const int *tile_start;         // n + 1 prefix sums of batch_tiles
+    const BatchInflow *inflows;    // inflows of all scenes, scene by scene
+    const int *inflow_start;       // n + 1 prefix sums
+    int n, tiles;
+};
+
+template <typename F> void launch_batch_inflow(const SceneBatch<F> &B, cudaStream_t st);
+template <typename F> void launch_batch_fill_solid(const SceneBatch<F> &B, int variant, int nq, cudaStream_t st);
+template <typename F> void launch_batch_bc(const SceneBatch<F> &B, cudaStream_t st);
+template <typename F> void launch_batch_buoyancy(const SceneBatch<F> &B, double dt, cudaStream_t st);
+template <typename F> void launch_batch_assemble(const SceneBatch<F> &B, double dt, int what, cudaStream_t st);
+template <typename F> void launch_batch_heat_assemble(const SceneBatch<F> &B, double dt, cudaStream_t st);
+template <typename F> void launch_batch_heat_to_rows(const SceneBatch<F> &B, cudaStream_t st);
+template <typename F> void launch_batch_apply_pressure(const SceneBatch<F> &B, double dt, cudaStream_t st);
+template <typename F> void launch_batch_extrapolate(const SceneBatch<F> &B, unsigned qmask, cudaStream_t st);
+template <typename F> void launch_batch_advect(const SceneBatch<F> &B, double dt, cudaStream_t st);
 
 // what-bits for launch_assemble
 enum { ASM_RHS = 1, ASM_MATRIX = 2, ASM_DENS = 4 };

@@ -25,8 +25,8 @@ template <typename F> __device__ __forceinline__ void stv(F *p, F v) { *(volatil
 // row two rectangle cells may hit one location, so the rectangle is then
 // walked by one thread in the reference's order.
 template <typename F>
-__global__ void inflow_kernel(Quant<F> Q, int P, double hx, double x0, double y0, double x1, double y1,
-                              double val) {
+__device__ __forceinline__ void inflow_body(const Quant<F> &Q, int P, double hx, double x0, double y0, double x1,
+                                            double y1, double val) {
     int ix0 = (int)(x0 / hx - Q.ox);
     int iy0 = (int)(y0 / hx - Q.oy);
     int ix1 = (int)(x1 / hx - Q.ox);
@@ -52,13 +52,18 @@ __global__ void inflow_kernel(Quant<F> Q, int P, double hx, double x0, double y0
         if (fabs((double)*c) < fabs(vi)) *c = (F)vi;
     }
 }
+template <typename F>
+__global__ void inflow_kernel(Quant<F> Q, int P, double hx, double x0, double y0, double x1, double y1,
+                              double val) {
+    inflow_body(Q, P, hx, x0, y0, x1, y1, val);
+}
 
 // ------------------------------------------------------------ solid fields
 // fillSolidFields, distance grid part (7-variable-density/Fluid.cpp:479-488)
 template <typename F>
-__global__ void phi_kernel(Scene<F> S) {
-    Quant<F> Q = S.q[qid_of(S.nq, blockIdx.z)];
-    int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void phi_body(const Scene<F> &S, const uint3 bid) {
+    Quant<F> Q = S.q[qid_of(S.nq, bid.z)];
+    int ix = bid.x * blockDim.x + threadIdx.x, iy = bid.y * blockDim.y + threadIdx.y;
     if (ix > Q.w || iy > Q.h) return;
     double x = (ix + Q.ox - 0.5) * S.hx;
     double y = (iy + Q.oy - 0.5) * S.hx;
@@ -66,13 +71,15 @@ __global__ void phi_kernel(Scene<F> S) {
     for (int i = 1; i < S.nbodies; i++) phi = smin(phi, body_distance(S.bodies[i], x, y));
     Q.phi[ix + (size_t)iy * S.P] = phi;
 }
+template <typename F>
+__global__ void phi_kernel(Scene<F> S) { phi_body(S, blockIdx); }
 
 // fillSolidFields, per-cell part (4-solid-boundaries/Fluid.cpp:453-479,
 // 7-variable-density/Fluid.cpp:490-521)
 template <typename F>
-__global__ void cell_kernel(Scene<F> S) {
-    Quant<F> Q = S.q[qid_of(S.nq, blockIdx.z)];
-    int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void cell_body(const Scene<F> &S, const uint3 bid) {
+    Quant<F> Q = S.q[qid_of(S.nq, bid.z)];
+    int ix = bid.x * blockDim.x + threadIdx.x, iy = bid.y * blockDim.y + threadIdx.y;
     if (ix >= Q.w || iy >= Q.h) return;
     size_t idx = ix + (size_t)iy * S.P;
     double x = (ix + Q.ox) * S.hx;
@@ -105,17 +112,19 @@ __global__ void cell_kernel(Scene<F> S) {
     if (cell != CELL_FLUID && (ix == 0 || iy == 0 || ix == Q.w - 1 || iy == Q.h - 1))
         atomicOr(S.flags, FLAG_RING_SOLID);
 }
+template <typename F>
+__global__ void cell_kernel(Scene<F> S) { cell_body(S, blockIdx); }
 
 // ------------------------------------------------------ boundary condition
 // setBoundaryCondition (4-solid-boundaries/Fluid.cpp:812-833): the later
 // (right / upper) solid cell's write wins, then the domain walls are zeroed.
 template <typename F>
-__global__ void bc_kernel(Scene<F> S) {
+__device__ __forceinline__ void bc_body(const Scene<F> &S, const uint3 bid) {
     const int w = S.w, h = S.h, P = S.P;
     const uint8_t *cell = S.q[0].cell, *body = S.q[0].body;
-    int fx = blockIdx.x * blockDim.x + threadIdx.x, fy = blockIdx.y * blockDim.y + threadIdx.y;
+    int fx = bid.x * blockDim.x + threadIdx.x, fy = bid.y * blockDim.y + threadIdx.y;
     const double hx = S.hx;
-    if (blockIdx.z == 0) {  // u faces (w+1) x h
+    if (bid.z == 0) {  // u faces (w+1) x h
         if (fx > w || fy >= h) return;
         F *u = S.q[2].src + fx + (size_t)fy * P;
         if (fx == 0 || fx == w) {
@@ -141,12 +150,14 @@ __global__ void bc_kernel(Scene<F> S) {
             *v = (F)body_vel_y(S.bodies[body[c - P]], (fx + 0.5) * hx, ((fy - 1) + 1.0) * hx);
     }
 }
+template <typename F>
+__global__ void bc_kernel(Scene<F> S) { bc_body(S, blockIdx); }
 
 // ---------------------------------------------------------------- buoyancy
 // addBuoyancy (7-variable-density/Fluid.cpp:908-919), gathered per v face.
 template <typename F>
-__global__ void buoyancy_kernel(Scene<F> S, double dt) {
-    int fx = blockIdx.x * blockDim.x + threadIdx.x, fy = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void buoyancy_body(const Scene<F> &S, double dt, const uint3 bid) {
+    int fx = bid.x * blockDim.x + threadIdx.x, fy = bid.y * blockDim.y + threadIdx.y;
     if (fx >= S.w || fy > S.h) return;
     const int P = S.P;
     const double alpha = (S.rho_soot - S.rho_air) / S.rho_air;
@@ -165,6 +176,8 @@ __global__ void buoyancy_kernel(Scene<F> S, double dt) {
     }
     *v = (F)val;
 }
+template <typename F>
+__global__ void buoyancy_kernel(Scene<F> S, double dt) { buoyancy_body(S, dt, blockIdx); }
 
 // ------------------------------------------------------------- assembly
 // Cell density of computeDensities (7-variable-density/Fluid.cpp:666-667).
@@ -227,9 +240,9 @@ __device__ __forceinline__ double yface_factor(const Scene<F> &S, double scale, 
 // in the reference's visiting order: lower face, left face, right face, upper
 // face.
 template <typename F>
-__global__ void assemble_kernel(Scene<F> S, double dt, int what) {
+__device__ __forceinline__ void assemble_body(const Scene<F> &S, double dt, int what, const uint3 bid) {
     const int w = S.w, h = S.h, P = S.P;
-    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    int x = bid.x * blockDim.x + threadIdx.x, y = bid.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
     const size_t c = x + (size_t)y * P;
     const size_t k = S.sd.slot(x, y);  // pressure-system arrays are strip-diagonal
@@ -315,13 +328,15 @@ __global__ void assemble_kernel(Scene<F> S, double dt, int what) {
         S.nb[k] = nb;
     }
 }
+template <typename F>
+__global__ void assemble_kernel(Scene<F> S, double dt, int what) { assemble_body(S, dt, what, blockIdx); }
 
 // r = T, buildHeatDiffusionMatrix (7-variable-density/Fluid.cpp:709-737,
 // 1001) and the neighbour bits.
 template <typename F>
-__global__ void heat_assemble_kernel(Scene<F> S, double dt) {
+__device__ __forceinline__ void heat_assemble_body(const Scene<F> &S, double dt, const uint3 bid) {
     const int w = S.w, h = S.h, P = S.P;
-    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    int x = bid.x * blockDim.x + threadIdx.x, y = bid.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
     const size_t c = x + (size_t)y * P;
     const size_t k = S.sd.slot(x, y);
@@ -348,18 +363,20 @@ __global__ void heat_assemble_kernel(Scene<F> S, double dt) {
     if (y < h - 1 && cell[c + P] == CELL_FLUID) nb |= NB_UP;
     S.nb[k] = nb;
 }
+template <typename F>
+__global__ void heat_assemble_kernel(Scene<F> S, double dt) { heat_assemble_body(S, dt, blockIdx); }
 
 // ---------------------------------------------------------- applyPressure
 // 3-conjugate-gradients/Fluid.cpp:382-398, 4-solid-boundaries/Fluid.cpp:794-809,
 // 7-variable-density/Fluid.cpp:891-906, gathered per face: first the
 // contribution of the lower/left cell (visited first), then the cell itself.
 template <typename F>
-__global__ void apply_pressure_kernel(Scene<F> S, double dt) {
+__device__ __forceinline__ void apply_pressure_body(const Scene<F> &S, double dt, const uint3 bid) {
     const int w = S.w, h = S.h, P = S.P, var = S.variant;
-    int fx = blockIdx.x * blockDim.x + threadIdx.x, fy = blockIdx.y * blockDim.y + threadIdx.y;
+    int fx = bid.x * blockDim.x + threadIdx.x, fy = bid.y * blockDim.y + threadIdx.y;
     const uint8_t *cell = S.q[0].cell;
     const double scale = (var == 7) ? dt / S.hx : dt / (S.rho_air * S.hx);
-    if (blockIdx.z == 0) {  // u faces
+    if (bid.z == 0) {  // u faces
         if (fx > w || fy >= h) return;
         size_t f = fx + (size_t)fy * P;
         F *u = S.q[2].src + f;
@@ -397,6 +414,8 @@ __global__ void apply_pressure_kernel(Scene<F> S, double dt) {
         *v = (F)val;
     }
 }
+template <typename F>
+__global__ void apply_pressure_kernel(Scene<F> S, double dt) { apply_pressure_body(S, dt, blockIdx); }
 
 // ------------------------------------------------------------ extrapolate
 // extrapolate / fillSolidMask / extrapolateNormal (4-solid-boundaries/Fluid.cpp:508-587).
@@ -405,11 +424,11 @@ __global__ void apply_pressure_kernel(Scene<F> S, double dt) {
 // a level-synchronous relaxation over the same DAG gives the same values.
 // Pass 1 (grid-wide): mask bits and the list of interior solid cells.
 template <typename F>
-__global__ void extrap_mask_kernel(Scene<F> S, unsigned qmask, int *counters) {
-    int qi = blockIdx.z;
+__device__ __forceinline__ void extrap_mask_body(const Scene<F> &S, unsigned qmask, int *counters, const uint3 bid) {
+    int qi = bid.z;
     if (!((qmask >> qi) & 1u)) return;
     Quant<F> Q = S.q[qi];
-    int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    int x = bid.x * blockDim.x + threadIdx.x, y = bid.y * blockDim.y + threadIdx.y;
     if (x >= Q.w || y >= Q.h) return;
     const int P = S.P;
     size_t idx = x + (size_t)y * P;
@@ -424,10 +443,14 @@ __global__ void extrap_mask_kernel(Scene<F> S, unsigned qmask, int *counters) {
     Q.list[slot] = (int)(idx * 4 + m);
 }
 
+template <typename F>
+__global__ void extrap_mask_kernel(Scene<F> S, unsigned qmask, int *counters) {
+    extrap_mask_body(S, qmask, counters, blockIdx);
+}
+
 // Pass 2: one CTA per quantity relaxes its list until nothing changes.
 template <typename F>
-__global__ void __launch_bounds__(1024) extrap_solve_kernel(Scene<F> S, unsigned qmask, const int *counters) {
-    int qi = blockIdx.x;
+__device__ __forceinline__ void extrap_solve_body(const Scene<F> &S, unsigned qmask, const int *counters, int qi) {
     if (!((qmask >> qi) & 1u)) return;
     Quant<F> Q = S.q[qi];
     const long P = S.P;
@@ -465,6 +488,10 @@ __global__ void __launch_bounds__(1024) extrap_solve_kernel(Scene<F> S, unsigned
         nxt = t;
         cnt = n2;
     }
+}
+template <typename F>
+__global__ void __launch_bounds__(1024) extrap_solve_kernel(Scene<F> S, unsigned qmask, const int *counters) {
+    extrap_solve_body(S, qmask, counters, blockIdx.x);
 }
 
 // -------------------------------------------------------------- advection
@@ -531,11 +558,11 @@ __device__ __forceinline__ F q_cerp(const F *__restrict__ src, int P, int w, int
 // backtrace), 1 = u, 2 = v.  Every quantity reads the u, v sources and writes
 // its own destination, so all of them advect in one launch.
 template <typename F>
-__global__ void advect_kernel(Scene<F> S, double dt) {
-    const int z = blockIdx.z;
+__device__ __forceinline__ void advect_body(const Scene<F> &S, double dt, const uint3 bid) {
+    const int z = bid.z;
     const int qi = z == 0 ? 0 : z + 1;
     const Quant<F> &Q = S.q[qi];
-    int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y * blockDim.y + threadIdx.y;
+    int ix = bid.x * blockDim.x + threadIdx.x, iy = bid.y * blockDim.y + threadIdx.y;
     if (ix >= Q.w || iy >= Q.h) return;
     const int P = S.P;
     const size_t idx = ix + (size_t)iy * P;
@@ -584,6 +611,8 @@ __global__ void advect_kernel(Scene<F> S, double dt) {
         T.dst[idx] = q_cerp(T.src, P, T.w, T.h, F(T.ox), F(T.oy), F(x), F(y));
     }
 }
+template <typename F>
+__global__ void advect_kernel(Scene<F> S, double dt) { advect_body(S, dt, blockIdx); }
 
 // Strip-diagonal FP64 array -> row-major field (T = p after the heat solve).
 template <typename F>
@@ -664,6 +693,175 @@ void launch_sd_to_rows(const Scene<F> &S, F *rows, const double *sd_arr, cudaStr
     dim3 b(32, 8);
     sd_to_rows_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S.sd, S.P, rows, sd_arr);
 }
+
+// ------------------------------------------------------------ batched phases
+// One launch runs a phase for every scene of a batch.  A scene covers
+// batch_tiles(w, h) tiles of 32x8 threads, enough for every grid of the scene
+// (the bodies bound-check their own grid); blockIdx.x enumerates the tiles of
+// all scenes through the prefix table tile_start, blockIdx.y is the phase's
+// third grid dimension (quantity or face kind).
+namespace {
+
+template <typename F>
+__device__ __forceinline__ int scene_of_tile(const SceneBatch<F> &B, int t) {
+    int lo = 0, hi = B.n;  // largest i with tile_start[i] <= t
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (B.tile_start[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <typename F, typename Op>
+__global__ void __launch_bounds__(256) batch_tiles_kernel(SceneBatch<F> B, Op op) {
+    const int i = scene_of_tile(B, blockIdx.x);
+    const Scene<F> &S = B.scenes[i];
+    const int tx = (S.w + 2 + 31) / 32;
+    const int local = blockIdx.x - B.tile_start[i];
+    op(S, make_uint3(local % tx, local / tx, blockIdx.y));
+}
+
+// fillSolidFields returns at once without bodies (4-solid-boundaries/Fluid.cpp:455)
+template <typename F> struct PhiOp {
+    __device__ void operator()(const Scene<F> &S, uint3 b) const {
+        if (S.nbodies > 0) phi_body(S, b);
+    }
+};
+template <typename F> struct CellOp {
+    __device__ void operator()(const Scene<F> &S, uint3 b) const {
+        if (S.nbodies > 0) cell_body(S, b);
+    }
+};
+template <typename F> struct BcOp {
+    __device__ void operator()(const Scene<F> &S, uint3 b) const { bc_body(S, b); }
+};
+template <typename F> struct BuoyancyOp {
+    double dt;
+    __device__ void operator()(const Scene<F> &S, uint3 b) const { buoyancy_body(S, dt, b); }
+};
+template <typename F> struct AssembleOp {
+    double dt;
+    int what;
+    __device__ void operator()(const Scene<F> &S, uint3 b) const { assemble_body(S, dt, what, b); }
+};
+template <typename F> struct HeatAssembleOp {
+    double dt;
+    __device__ void operator()(const Scene<F> &S, uint3 b) const { heat_assemble_body(S, dt, b); }
+};
+template <typename F> struct HeatToRowsOp {  // T = p (7-variable-density/Fluid.cpp:1005)
+    __device__ void operator()(const Scene<F> &S, uint3 b) const {
+        const int x = b.x * blockDim.x + threadIdx.x, y = b.y * blockDim.y + threadIdx.y;
+        if (x >= S.w || y >= S.h) return;
+        S.q[1].src[x + (size_t)y * S.P] = (F)S.p[S.sd.slot(x, y)];
+    }
+};
+template <typename F> struct ApplyOp {
+    double dt;
+    __device__ void operator()(const Scene<F> &S, uint3 b) const { apply_pressure_body(S, dt, b); }
+};
+template <typename F> struct MaskOp {
+    unsigned qmask;
+    __device__ void operator()(const Scene<F> &S, uint3 b) const {
+        extrap_mask_body(S, qmask, (int *)(S.flags + 4), b);
+    }
+};
+template <typename F> struct AdvectOp {
+    double dt;
+    __device__ void operator()(const Scene<F> &S, uint3 b) const { advect_body(S, dt, b); }
+};
+
+// The inflows of one scene, in call order, by one block.
+template <typename F>
+__global__ void batch_inflow_kernel(SceneBatch<F> B) {
+    const Scene<F> &S = B.scenes[blockIdx.x];
+    for (int r = B.inflow_start[blockIdx.x]; r < B.inflow_start[blockIdx.x + 1]; r++) {
+        const BatchInflow f = B.inflows[r];
+        inflow_body(S.q[f.q], S.P, S.hx, f.x0, f.y0, f.x1, f.y1, f.val);
+        __syncthreads();
+    }
+}
+
+// Extrapolation counters of every scene (Scene::flags[4..8)).
+template <typename F>
+__global__ void batch_zero_counters_kernel(SceneBatch<F> B) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.n) return;
+    int *c = (int *)(B.scenes[i].flags + 4);
+    c[0] = c[1] = c[2] = c[3] = 0;
+}
+
+template <typename F>
+__global__ void __launch_bounds__(1024) batch_extrap_solve_kernel(SceneBatch<F> B, unsigned qmask) {
+    const Scene<F> &S = B.scenes[blockIdx.x];
+    extrap_solve_body(S, qmask, (const int *)(S.flags + 4), blockIdx.y);
+}
+
+template <typename F, typename Op>
+void tiles(const SceneBatch<F> &B, int nz, Op op, cudaStream_t st) {
+    if (B.tiles > 0) batch_tiles_kernel<F, Op><<<dim3(B.tiles, nz), dim3(32, 8), 0, st>>>(B, op);
+}
+
+}  // namespace
+
+template <typename F>
+void launch_batch_inflow(const SceneBatch<F> &B, cudaStream_t st) {
+    if (B.n > 0) batch_inflow_kernel<F><<<B.n, 256, 0, st>>>(B);
+}
+template <typename F>
+void launch_batch_fill_solid(const SceneBatch<F> &B, int variant, int nq, cudaStream_t st) {
+    if (variant >= 5) tiles(B, nq, PhiOp<F>{}, st);
+    tiles(B, nq, CellOp<F>{}, st);
+}
+template <typename F>
+void launch_batch_bc(const SceneBatch<F> &B, cudaStream_t st) {
+    tiles(B, 2, BcOp<F>{}, st);
+}
+template <typename F>
+void launch_batch_buoyancy(const SceneBatch<F> &B, double dt, cudaStream_t st) {
+    tiles(B, 1, BuoyancyOp<F>{dt}, st);
+}
+template <typename F>
+void launch_batch_assemble(const SceneBatch<F> &B, double dt, int what, cudaStream_t st) {
+    tiles(B, 1, AssembleOp<F>{dt, what}, st);
+}
+template <typename F>
+void launch_batch_heat_assemble(const SceneBatch<F> &B, double dt, cudaStream_t st) {
+    tiles(B, 1, HeatAssembleOp<F>{dt}, st);
+}
+template <typename F>
+void launch_batch_heat_to_rows(const SceneBatch<F> &B, cudaStream_t st) {
+    tiles(B, 1, HeatToRowsOp<F>{}, st);
+}
+template <typename F>
+void launch_batch_apply_pressure(const SceneBatch<F> &B, double dt, cudaStream_t st) {
+    tiles(B, 2, ApplyOp<F>{dt}, st);
+}
+template <typename F>
+void launch_batch_extrapolate(const SceneBatch<F> &B, unsigned qmask, cudaStream_t st) {
+    if (B.n <= 0) return;
+    batch_zero_counters_kernel<F><<<(B.n + 255) / 256, 256, 0, st>>>(B);
+    tiles(B, 4, MaskOp<F>{qmask}, st);
+    batch_extrap_solve_kernel<F><<<dim3(B.n, 4), 1024, 0, st>>>(B, qmask);
+}
+template <typename F>
+void launch_batch_advect(const SceneBatch<F> &B, double dt, cudaStream_t st) {
+    tiles(B, 3, AdvectOp<F>{dt}, st);
+}
+
+#define IFL_BATCH_INST(F)                                                                                  \
+    template void launch_batch_inflow<F>(const SceneBatch<F> &, cudaStream_t);                              \
+    template void launch_batch_fill_solid<F>(const SceneBatch<F> &, int, int, cudaStream_t);                \
+    template void launch_batch_bc<F>(const SceneBatch<F> &, cudaStream_t);                                  \
+    template void launch_batch_buoyancy<F>(const SceneBatch<F> &, double, cudaStream_t);                    \
+    template void launch_batch_assemble<F>(const SceneBatch<F> &, double, int, cudaStream_t);               \
+    template void launch_batch_heat_assemble<F>(const SceneBatch<F> &, double, cudaStream_t);               \
+    template void launch_batch_heat_to_rows<F>(const SceneBatch<F> &, cudaStream_t);                        \
+    template void launch_batch_apply_pressure<F>(const SceneBatch<F> &, double, cudaStream_t);              \
+    template void launch_batch_extrapolate<F>(const SceneBatch<F> &, unsigned, cudaStream_t);               \
+    template void launch_batch_advect<F>(const SceneBatch<F> &, double, cudaStream_t);
+IFL_BATCH_INST(double)
+IFL_BATCH_INST(float)
 
 #define IFL_INST(F)                                                                                        \
     template void launch_inflow<F>(const Scene<F> &, int, double, double, double, double, double,           \

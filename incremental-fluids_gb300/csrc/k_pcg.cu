@@ -35,7 +35,10 @@
 //  * Phases are separated by a grid barrier of this file.
 // Every wait is bounded: on timeout the status word gets FLAG_TIMEOUT, later
 // waits stop waiting, the kernel runs to its end and the host reports an error.
+#include <algorithm>
+#include <cstring>
 #include <type_traits>
+#include <vector>
 
 #include "ifl_device.cuh"
 
@@ -47,14 +50,32 @@ namespace {
 // that every ring and halo access compiles to a shared-space instruction.
 extern __shared__ __align__(128) char g_smem[];
 
-constexpr int kThreads = 512;
-constexpr int kWarps = kThreads / 32;
+// Threads per block: 512 for a scene that has the GPU to itself, 256 in the
+// compact launch used when many scenes run concurrently.
+constexpr int kMaxWarps = 16;
+constexpr int kUnroll = 4;  // diagonals per warp and pass of the elementwise phases
 constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
 constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
 constexpr double kTau = 0.97, kSigma = 0.25, kTol = 1e-5;
 constexpr unsigned long long kSentinel = ~0ull;
 constexpr unsigned FULL = 0xffffffffu;
+
+// Status words a wait checks: the scene's own and one shared by every scene
+// of a batched launch (the same word for a single-scene launch).  A timed-out
+// wait marks both, so every later wait of the launch stops waiting.
+struct Flags {
+    unsigned *scene, *all;
+};
+
+// The blocks that solve one scene: ranks 0..size-1, their barrier words and
+// the per-block partial sums.  A single-scene launch is one team of the whole
+// grid.
+struct Team {
+    int rank, size;
+    unsigned *barrier;
+    double *partials;
+};
 
 template <typename F>
 struct PcgArgs {
@@ -67,7 +88,8 @@ struct PcgArgs {
     F *rf;  // r in storage precision for the substitutions (== r when F is double)
     F *z, *sa, *sb;
     double *partials;
-    unsigned *barrier, *flags;
+    unsigned *barrier;
+    Flags fl;
     unsigned long long *halo;  // [2][S][D]: [0] rows handed upward, [1] rows handed downward
     PcgOut *out;
     unsigned long long *iter_total;
@@ -104,24 +126,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
     return ok != 0;
 }
 
-__device__ __forceinline__ bool timed_out(const unsigned *flags) { return ld_volatile(flags) & FLAG_TIMEOUT; }
+__device__ __forceinline__ bool timed_out(const Flags &f) {
+    return (ld_volatile(f.scene) | ld_volatile(f.all)) & FLAG_TIMEOUT;
+}
+__device__ __forceinline__ void set_timeout(const Flags &f) {
+    atomicOr(f.scene, FLAG_TIMEOUT);
+    if (f.all != f.scene) atomicOr(f.all, FLAG_TIMEOUT);
+}
 
-// Grid barrier: arrival counter + generation word, bounded wait.
-__device__ void grid_barrier(unsigned *bar, unsigned *flags) {
+// Team barrier: arrival counter + generation word, bounded wait.
+__device__ void team_barrier(const Team &T, const Flags &fl) {
     __syncthreads();
     if (threadIdx.x == 0) {
+        unsigned *bar = T.barrier;
         unsigned g = ld_volatile(bar + 1);
         __threadfence();
         unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == (unsigned)T.size - 1) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
             long long n = 0;
             while (ld_volatile(bar + 1) == g) {
-                if (++n > kWaitLimit || timed_out(flags)) {
-                    atomicOr(flags, FLAG_TIMEOUT);
+                if (++n > kWaitLimit || timed_out(fl)) {
+                    set_timeout(fl);
                     break;
                 }
             }
@@ -140,8 +169,9 @@ __device__ __forceinline__ double warp_max(double v) {
     return v;
 }
 
-// Block partial -> partials[slot*G + block] (fixed order).
-__device__ void block_store(double v, bool is_max, double *partials, int slot, double *sm) {
+// Block partial -> partials[slot*size + rank] (fixed order).
+__device__ void block_store(double v, bool is_max, const Team &T, int slot, double *sm) {
+    const int kWarps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     v = is_max ? warp_max(v) : warp_sum(v);
     if (lane == 0) sm[warp] = v;
@@ -149,18 +179,19 @@ __device__ void block_store(double v, bool is_max, double *partials, int slot, d
     if (threadIdx.x == 0) {
         double acc = sm[0];
         for (int i = 1; i < kWarps; i++) acc = is_max ? smax(acc, sm[i]) : acc + sm[i];
-        partials[slot * gridDim.x + blockIdx.x] = acc;
+        T.partials[slot * T.size + T.rank] = acc;
     }
     __syncthreads();
 }
 
-// Every block reduces partials[slot][0..G) in the same fixed order.
-__device__ double grid_reduce(const double *partials, int slot, bool is_max, double *sm) {
+// Every block of the team reduces partials[slot][0..size) in the same fixed order.
+__device__ double team_reduce(const Team &T, int slot, bool is_max, double *sm) {
+    const int kWarps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31;
     if (threadIdx.x < 32) {
         double acc = 0.0;
-        const volatile double *p = partials + slot * gridDim.x;
-        for (int i = lane; i < (int)gridDim.x; i += 32) acc = is_max ? smax(acc, (double)p[i]) : acc + p[i];
+        const volatile double *p = T.partials + slot * T.size;
+        for (int i = lane; i < T.size; i += 32) acc = is_max ? smax(acc, (double)p[i]) : acc + p[i];
         acc = is_max ? warp_max(acc) : warp_sum(acc);
         if (lane == 0) sm[kWarps] = acc;
     }
@@ -181,7 +212,11 @@ template <> __device__ __forceinline__ float hdec<float>(unsigned long long w) {
 
 // Halo rows: shared memory (relaxed, CTA scope) inside a block, global memory
 // (relaxed, GPU scope) between blocks.  One 8-byte access is single-copy
-// atomic, so a reader sees either the sentinel or the whole value.
+// atomic, so a reader sees either the sentinel or the whole value.  A halo
+// word carries its value itself, so no other memory access has to be ordered
+// around it: the asm statements are volatile (kept, in program order) but do
+// not clobber memory, which would stop the compiler from keeping loaded
+// operands and pointers in registers across them.
 struct Chan {
     unsigned soff;             // byte offset in g_smem when shared
     unsigned long long *g;     // global row when not shared
@@ -190,28 +225,28 @@ struct Chan {
 __device__ __forceinline__ unsigned long long hload(const Chan &c, int x) {
     unsigned long long v;
     if (c.shared)
-        asm volatile("ld.relaxed.cta.shared.u64 %0, [%1];" : "=l"(v) : "r"(smem_u32(g_smem) + c.soff + 8u * x) : "memory");
+        asm volatile("ld.relaxed.cta.shared.u64 %0, [%1];" : "=l"(v) : "r"(smem_u32(g_smem) + c.soff + 8u * x));
     else
-        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(c.g + x) : "memory");
+        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(c.g + x));
     return v;
 }
 __device__ __forceinline__ void hstore(const Chan &c, int x, unsigned long long v) {
     if (c.shared)
-        asm volatile("st.relaxed.cta.shared.u64 [%0], %1;" ::"r"(smem_u32(g_smem) + c.soff + 8u * x), "l"(v) : "memory");
+        asm volatile("st.relaxed.cta.shared.u64 [%0], %1;" ::"r"(smem_u32(g_smem) + c.soff + 8u * x), "l"(v));
     else
-        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(c.g + x), "l"(v) : "memory");
+        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(c.g + x), "l"(v));
 }
 
 // Take a halo word (bounded poll), then put the sentinel back for the next sweep.
 __device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, unsigned long long pre,
-                                                        unsigned *flags) {
+                                                        const Flags &flags) {
     unsigned long long v = pre;
     long long n = 0;
     while (v == kSentinel) {
         v = hload(c, x);
         if (v != kSentinel) break;
         if (++n > kWaitLimit || timed_out(flags)) {
-            atomicOr(flags, FLAG_TIMEOUT);
+            set_timeout(flags);
             v = 0;
             break;
         }
@@ -225,7 +260,7 @@ __device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, un
 // (kB*32 slots) of the streams of one sweep kind, in three regions:
 //   factor:   [adiag][ax][ay | neighbour bits]
 //   forward:  [r]    [--][MIC record]
-//   backward: [z]    [r] [MIC record]
+//   backward: [z]    [--][MIC record]
 // A MIC record is {lx, ly, pc, neighbour bits} for one slot (lx = aPlusX*pc,
 // ly = aPlusY*pc, pc = precon, storage precision; written by the factor).
 // ii / ci count issued / consumed blocks over the whole kernel, so buffer =
@@ -242,12 +277,12 @@ struct Ring {
 };
 
 template <typename F>
-__device__ __forceinline__ void ring_wait(Ring<F> &R, unsigned *flags) {
+__device__ __forceinline__ void ring_wait(Ring<F> &R, const Flags &flags) {
     const unsigned st = R.ci % R.stages, parity = (R.ci / R.stages) & 1u;
     long long n = 0;
     while (!mbar_try_wait(R.bar(st), parity)) {
         if (++n > kMbarWaitLimit || timed_out(flags)) {
-            atomicOr(flags, FLAG_TIMEOUT);
+            set_timeout(flags);
             break;
         }
     }
@@ -274,9 +309,8 @@ __device__ __forceinline__ void ring_issue(Ring<F> &R, const PcgArgs<F> &A, int 
         bulk_g2s(dst, A.rf + off, S1, bar);
         bulk_g2s(dst + 2 * S1, A.mic + 4 * off, 4 * S1, bar);
     } else {
-        mbar_expect_tx(bar, 6 * S1);
+        mbar_expect_tx(bar, 5 * S1);
         bulk_g2s(dst, A.z + off, S1, bar);
-        bulk_g2s(dst + S1, A.rf + off, S1, bar);
         bulk_g2s(dst + 2 * S1, A.mic + 4 * off, 4 * S1, bar);
     }
     R.ii++;
@@ -297,6 +331,10 @@ __device__ __forceinline__ void st4(double *p, double a, double b, double c, dou
     *(double2 *)p = make_double2(a, b);
     *(double2 *)(p + 2) = make_double2(c, d);
 }
+// t - a*b: one fused multiply-add in the FP32 form; two roundings in FP64, as
+// the reference computes it (the FP64 path must stay bit-identical).
+__device__ __forceinline__ float msub(float t, float a, float b) { return fmaf(-a, b, t); }
+__device__ __forceinline__ double msub(double t, double a, double b) { return t - a * b; }
 __device__ __forceinline__ unsigned nb_of(float w) { return __float_as_uint(w); }
 __device__ __forceinline__ unsigned nb_of(double w) { return (unsigned)__double_as_longlong(w); }
 __device__ __forceinline__ float nb_word(unsigned b, float) { return __uint_as_float(b); }
@@ -306,10 +344,9 @@ __device__ __forceinline__ double nb_word(unsigned b, double) { return __longlon
 // neighbouring strip this one depends on (nullptr: none), `out` the row this
 // strip hands on (nullptr: none).  Each sub-block of kHB steps first stages
 // its operands from the ring into registers, then runs the dependency chain
-// (registers and shuffles only), then issues its stores.  Returns the lane's
-// partial dot(z, r) for the backward solve.
+// (registers and shuffles only), then issues its stores.
 template <int KIND, typename F>
-__device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan in, const Chan out) {
+__device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan in, const Chan out) {
     using V = typename std::conditional<KIND == 0, double, F>::type;
     constexpr int kHB = sizeof(F) == 8 ? 4 : 8;
     constexpr bool bwd = KIND == 2;
@@ -322,7 +359,12 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
     const int nblk = D / kB;
     const bool has_in = in.valid;
     const bool producer = out.valid && lane == (bwd ? 0 : 31);
-    double dot = 0.0;
+    // pointers in registers for the whole sweep
+    F *const zout = A.z;
+    F *const micp = A.mic;
+    double *const pcp = A.pc;
+    const F *const axp = A.ax;
+    const F *const ayp = A.ay;
 
     V prev = V(0);                   // result of the previous cell in sweep order
     F prev_a = F(0), prev_b = F(0);  // forward: lx, ly of that cell; factor: ax, ay
@@ -340,11 +382,11 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
                 hpre = hload(in, xc);
                 if constexpr (KIND == 0) {
                     const size_t k = sd.slot(xc, s * 32 - 1);
-                    spre_a = A.ax[k];
-                    spre_b = A.ay[k];
+                    spre_a = axp[k];
+                    spre_b = ayp[k];
                 } else if constexpr (KIND == 1) {
                     F a, b, c, d;
-                    ld4(A.mic + 4 * sd.slot(xc, s * 32 - 1), a, b, c, d);
+                    ld4(micp + 4 * sd.slot(xc, s * 32 - 1), a, b, c, d);
                     spre_b = b;  // ly of the cell below
                 }
             }
@@ -364,7 +406,7 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
             if (lane == 0) ring_issue<KIND, F>(R, A, s, blk + R.stages - 1);
         }
         const unsigned st = R.ci % R.stages;
-        ring_wait(R, A.flags);
+        ring_wait(R, A.fl);
         const char *sbuf = g_smem + R.buf + st * Ring<F>::kStageBytes;
         const F *g0 = (const F *)sbuf;
         const F *g1 = (const F *)(sbuf + S1);
@@ -378,14 +420,14 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
             if (has_in && lane < kHB) {
                 const int xc = halo_col(t0 + lane);
                 if (xc >= 0 && xc < W) {
-                    hv = hdec<V>(halo_take(in, xc, hpre, A.flags));
+                    hv = hdec<V>(halo_take(in, xc, hpre, A.fl));
                     ha = spre_a;
                     hb = spre_b;
                 }
             }
             prefetch(t0 + kHB);
             // stage this sub-block's operands in registers
-            F o0[kHB], o1[kHB], o2[kHB], o3[kHB], o4[kHB];
+            F o0[kHB], o1[kHB], o2[kHB], o3[kHB];
             unsigned ob[kHB];
             V hvv[kHB];
             F hav[kHB], hbv[kHB];
@@ -398,17 +440,15 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
                     o1[jj] = g1[e];
                     o2[jj] = g2[e];
                     ob[jj] = gnb[e];
-                    o3[jj] = o4[jj] = F(0);
+                    o3[jj] = F(0);
                 } else if constexpr (KIND == 1) {
                     F w3;
                     o0[jj] = g0[e];
                     ld4(g2 + 4 * e, o1[jj], o2[jj], o3[jj], w3);
                     ob[jj] = nb_of(w3);
-                    o4[jj] = F(0);
                 } else {
                     F w3;
                     o0[jj] = g0[e];
-                    o4[jj] = g1[e];
                     ld4(g2 + 4 * e, o1[jj], o2[jj], o3[jj], w3);
                     ob[jj] = nb_of(w3);
                 }
@@ -455,8 +495,8 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
                     const F q_d = lane == 0 ? hvv[jj] : q_sh;
                     const F ly_d = lane == 0 ? hbv[jj] : ly_sh;
                     F tt = o0[jj];
-                    tt = (b & NB_LEFT) ? tt - prev_a * prev : tt;
-                    tt = (b & NB_DOWN) ? tt - ly_d * q_d : tt;
+                    tt = (b & NB_LEFT) ? msub(tt, prev_a, prev) : tt;
+                    tt = (b & NB_DOWN) ? msub(tt, ly_d, q_d) : tt;
                     val = tt * o3[jj];
                     prev_a = o1[jj];
                     prev_b = o2[jj];
@@ -465,8 +505,8 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
                     const F z_sh = __shfl_down_sync(FULL, prev, 1);
                     const F z_u = lane == 31 ? hvv[jj] : z_sh;
                     F tt = o0[jj];
-                    tt = (b & NB_RIGHT) ? tt - o1[jj] * prev : tt;
-                    tt = (b & NB_UP) ? tt - o2[jj] * z_u : tt;
+                    tt = (b & NB_RIGHT) ? msub(tt, o1[jj], prev) : tt;
+                    tt = (b & NB_UP) ? msub(tt, o2[jj], z_u) : tt;
                     val = tt * o3[jj];
                 }
                 res[jj] = val;
@@ -485,14 +525,11 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
                     if constexpr (KIND == 0) {
                         const bool self = b & NB_SELF;
                         const double pcv = res[jj];
-                        if (self) A.pc[i] = pcv;
-                        st4(A.mic + 4 * i, self ? (F)((double)o1[jj] * pcv) : F(0),
+                        if (self) pcp[i] = pcv;
+                        st4(micp + 4 * i, self ? (F)((double)o1[jj] * pcv) : F(0),
                             self ? (F)((double)o2[jj] * pcv) : F(0), self ? (F)pcv : F(0), nb_word(b, F(0)));
                     } else {
-                        if (b & NB_SELF) {
-                            A.z[i] = res[jj];
-                            if (KIND == 2 && (b & NB_RED)) dot = fma((double)res[jj], (double)o4[jj], dot);
-                        }
+                        if (b & NB_SELF) zout[i] = res[jj];
                     }
                     if (producer) hstore(out, x, henc(res[jj]));
                 }
@@ -500,18 +537,17 @@ __device__ double sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan
         }
     }
     __syncwarp();
-    return dot;
 }
 
 // Sweep of all strips of this block; the halo rows between its own warps live
 // in shared memory, those to neighbouring blocks in global memory.
 // hsm_off: byte offset in g_smem of the K-1 shared halo rows (D words each).
 template <int KIND, typename F>
-__device__ double sweep(const PcgArgs<F> &A, Ring<F> &R, unsigned hsm_off, int nstrips_blk) {
+__device__ void sweep(const PcgArgs<F> &A, const Team &T, Ring<F> &R, unsigned hsm_off, int nstrips_blk) {
     const int w = threadIdx.x >> 5;
-    if (w >= nstrips_blk) return 0.0;
+    if (w >= nstrips_blk) return;
     const SDIdx sd = A.sd;
-    const int s = blockIdx.x * A.K + w;
+    const int s = T.rank * A.K + w;
     const size_t D = sd.D;
     unsigned long long *up = A.halo, *down = A.halo + (size_t)sd.S * D;
     auto smem_row = [&](int k) { return Chan{hsm_off + 8u * (unsigned)(k * D), nullptr, true, true}; };
@@ -524,40 +560,69 @@ __device__ double sweep(const PcgArgs<F> &A, Ring<F> &R, unsigned hsm_off, int n
         if (s + 1 < sd.S) in = (w + 1 < nstrips_blk) ? smem_row(w) : glob_row(down + (size_t)(s + 1) * D);
         if (s > 0) out = (w > 0) ? smem_row(w - 1) : glob_row(down + (size_t)s * D);
     }
-    return sweep_strip<KIND, F>(A, s, R, in, out);
+    sweep_strip<KIND, F>(A, s, R, in, out);
 }
 
+// Shared-memory layout of a PCG block: mbarriers (32 bytes per warp) | the
+// K-1 halo rows between its strips (D words each) | the per-warp rings.
+__device__ __forceinline__ unsigned halo_offset(int K) { return 32u * K; }
+__device__ __forceinline__ unsigned ring_offset(int K, int D) {
+    const size_t nh = (size_t)(K > 1 ? K - 1 : 0) * D;
+    return (unsigned)(((32 * (size_t)K + nh * 8 + 127) / 128) * 128);
+}
+
+// Per-warp ring state; the mbarriers are initialised once per launch.
 template <typename F>
-__global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
-    __shared__ double sm[kWarps + 1];
+__device__ void ring_init(Ring<F> &R, int K, int stages) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    R.bars = 32u * warp;
+    R.stages = stages;
+    R.ii = R.ci = 0;
+    if (warp < K && lane == 0) {
+        for (int k = 0; k < stages; k++) mbar_init(R.bar(k), 1);
+        fence_mbar_init();
+    }
+}
+
+// One complete solve (factor and/or PCG, by A.mode) of one scene by team T.
+// The shared halo rows must hold the sentinel on entry; they hold it again on
+// exit (every word a strip hands on is taken by its neighbour).
+template <typename F, int kThreads>
+__device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *sm) {
+    constexpr int kWarps = kThreads / 32;
     const SDIdx sd = A.sd;
     const int W = sd.W, H = sd.H, D = sd.D;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rows = sd.S * D;  // diagonals of all strips
-    const int gwarp = blockIdx.x * kWarps + warp, nwarps = gridDim.x * kWarps;
-    int nstrips_blk = sd.S - (int)blockIdx.x * A.K;
+    const int gwarp = T.rank * kWarps + warp, nwarps = T.size * kWarps;
+    int nstrips_blk = sd.S - T.rank * A.K;
     nstrips_blk = nstrips_blk < 0 ? 0 : (nstrips_blk > A.K ? A.K : nstrips_blk);
     constexpr bool kF32 = !std::is_same<F, double>::value;
+    const unsigned hsm_off = halo_offset(A.K);
+    R.buf = ring_offset(A.K, D) + (unsigned)warp * A.stages * Ring<F>::kStageBytes;
 
-    // shared memory: mbarriers | halo rows between this block's strips | rings
-    const size_t nh = (size_t)(A.K > 1 ? A.K - 1 : 0) * D;
-    const unsigned hsm_off = 32u * A.K;
-    const unsigned rings = (unsigned)(((32 * A.K + nh * 8 + 127) / 128) * 128);
-    Ring<F> R;
-    R.bars = 32u * warp;
-    R.buf = rings + (unsigned)warp * A.stages * Ring<F>::kStageBytes;
-    R.stages = A.stages;
-    R.ii = R.ci = 0;
-    for (size_t k = threadIdx.x; k < nh; k += kThreads) ((unsigned long long *)(g_smem + hsm_off))[k] = kSentinel;
-    if (warp < nstrips_blk && lane == 0) {
-        for (int k = 0; k < R.stages; k++) mbar_init(R.bar(k), 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
+    // sigma = z . r over the red cells (3-conjugate-gradients/Fluid.cpp:356, 376):
+    // a separate pass keeps the FP64 products off the backward sweep's chain.
+    auto dot_zr = [&]() {
+        double acc = 0.0;
+        const F *__restrict__ zp = A.z;
+        const double *__restrict__ rp = A.r;
+        const uint8_t *__restrict__ nbp = A.nb;
+        for (int row0 = gwarp; row0 < rows; row0 += kUnroll * nwarps) {
+#pragma unroll
+            for (int u = 0; u < kUnroll; u++) {
+                const int row = row0 + u * nwarps;
+                if (row >= rows) break;
+                const size_t i = (size_t)row * 32 + lane;
+                if (nbp[i] & NB_RED) acc += (double)zp[i] * rp[i];
+            }
+        }
+        return acc;
+    };
 
     if (A.mode & PCG_FACTOR) {
-        sweep<0, F>(A, R, hsm_off, nstrips_blk);
-        grid_barrier(A.barrier, A.flags);
+        sweep<0, F>(A, T, R, hsm_off, nstrips_blk);
+        team_barrier(T, A.fl);
     }
     if (!(A.mode & PCG_SOLVE)) return;
 
@@ -569,17 +634,18 @@ __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
         if (kF32) A.rf[i] = (F)A.r[i];
         if (A.nb[i] & NB_RED) mx = smax(mx, fabs(A.r[i]));
     }
-    block_store(mx, true, A.partials, 0, sm);
-    if (kF32) grid_barrier(A.barrier, A.flags);  // FP32 copy of r complete
+    block_store(mx, true, T, 0, sm);
+    if (kF32) team_barrier(T, A.fl);  // FP32 copy of r complete
     // z = M^-1 r  (:351)
-    sweep<1, F>(A, R, hsm_off, nstrips_blk);
-    grid_barrier(A.barrier, A.flags);
-    double d = sweep<2, F>(A, R, hsm_off, nstrips_blk);
-    block_store(d, false, A.partials, 2, sm);
-    grid_barrier(A.barrier, A.flags);
+    sweep<1, F>(A, T, R, hsm_off, nstrips_blk);
+    team_barrier(T, A.fl);
+    sweep<2, F>(A, T, R, hsm_off, nstrips_blk);
+    team_barrier(T, A.fl);
+    block_store(dot_zr(), false, T, 2, sm);
+    team_barrier(T, A.fl);
 
-    double maxError = grid_reduce(A.partials, 0, true, sm);
-    double sigma = grid_reduce(A.partials, 2, false, sm);
+    double maxError = team_reduce(T, 0, true, sm);
+    double sigma = team_reduce(T, 2, false, sm);
     int iterations = 0, status;
     if (A.pinned >= 0 ? A.pinned == 0 : maxError < kTol) {
         status = 1;
@@ -588,68 +654,99 @@ __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
         double beta = 0.0;
         F *s_old = A.sa, *s_new = A.sb;
         for (int iter = 0; iter < A.limit; iter++) {
-            if (timed_out(A.flags)) break;
+            // block-uniform: every thread of the block leaves together
+            if (__syncthreads_or(threadIdx.x == 0 && timed_out(A.fl))) break;
             // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
             double dacc = 0.0;
             const F fbeta = (F)beta;
-            for (int row = gwarp; row < rows; row += nwarps) {
-                const int s = row / D, dd = row - s * D;
-                const int x = dd - lane, y = s * 32 + lane;
-                const size_t i = (size_t)row * 32 + lane;
-                if (x < 0 || x >= W || y >= H) {
-                    s_new[i] = F(0);
-                    A.as[i] = 0.0;
-                    continue;
+            // Four diagonals per warp and pass, their loads issued together
+            // (the pointers do not alias), in the same per-lane order as a
+            // plain strided loop.
+            const F *__restrict__ zp = A.z;
+            const F *__restrict__ so = s_old;
+            const uint8_t *__restrict__ nbp = A.nb;
+            const F *__restrict__ adp = A.adiag;
+            const F *__restrict__ axp = A.ax;
+            const F *__restrict__ ayp = A.ay;
+            F *__restrict__ sn = s_new;
+            double *__restrict__ asp = A.as;
+            auto snew = [&](size_t k) -> F {
+                if (iter == 0) return zp[k];
+                return (nbp[k] & NB_RED) ? F(zp[k] + so[k] * fbeta) : so[k];
+            };
+            for (int row0 = gwarp; row0 < rows; row0 += kUnroll * nwarps) {
+#pragma unroll
+                for (int u = 0; u < kUnroll; u++) {
+                    const int row = row0 + u * nwarps;
+                    if (row >= rows) break;
+                    const int s = row / D, dd = row - s * D;
+                    const int x = dd - lane, y = s * 32 + lane;
+                    const size_t i = (size_t)row * 32 + lane;
+                    if (x < 0 || x >= W || y >= H) {
+                        sn[i] = F(0);
+                        asp[i] = 0.0;
+                        continue;
+                    }
+                    // FP64 accumulation: with FP32 storage every product is exact,
+                    // so the operator the recurrences see is the same every iteration.
+                    const F sc = snew(i);
+                    double t = (double)adp[i] * (double)sc;
+                    if (x > 0) t += (double)axp[i - 32] * (double)snew(i - 32);
+                    if (y > 0) {
+                        const size_t k = lane > 0 ? i - 33 : sd.slot(x, y - 1);
+                        t += (double)ayp[k] * (double)snew(k);
+                    }
+                    if (x < W - 1) t += (double)axp[i] * (double)snew(i + 32);
+                    if (y < H - 1) t += (double)ayp[i] * (double)snew(lane < 31 ? i + 33 : sd.slot(x, y + 1));
+                    sn[i] = sc;
+                    asp[i] = t;
+                    if (nbp[i] & NB_RED) dacc += t * (double)sc;
                 }
-                auto snew = [&](size_t k) -> F {
-                    if (iter == 0) return A.z[k];
-                    return (A.nb[k] & NB_RED) ? F(A.z[k] + s_old[k] * fbeta) : s_old[k];
-                };
-                // FP64 accumulation: with FP32 storage every product is exact,
-                // so the operator the recurrences see is the same every iteration.
-                const F sc = snew(i);
-                double t = (double)A.adiag[i] * (double)sc;
-                if (x > 0) t += (double)A.ax[i - 32] * (double)snew(i - 32);
-                if (y > 0) {
-                    const size_t k = lane > 0 ? i - 33 : sd.slot(x, y - 1);
-                    t += (double)A.ay[k] * (double)snew(k);
-                }
-                if (x < W - 1) t += (double)A.ax[i] * (double)snew(i + 32);
-                if (y < H - 1) t += (double)A.ay[i] * (double)snew(lane < 31 ? i + 33 : sd.slot(x, y + 1));
-                s_new[i] = sc;
-                A.as[i] = t;
-                if (A.nb[i] & NB_RED) dacc += t * (double)sc;
             }
-            block_store(dacc, false, A.partials, 1, sm);
-            grid_barrier(A.barrier, A.flags);
-            const double alpha = sigma / grid_reduce(A.partials, 1, false, sm);
+            block_store(dacc, false, T, 1, sm);
+            team_barrier(T, A.fl);
+            const double alpha = sigma / team_reduce(T, 1, false, sm);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
             mx = 0.0;
-            for (int row = gwarp; row < rows; row += nwarps) {
-                const size_t i = (size_t)row * 32 + lane;
-                if (A.nb[i] & NB_RED) {
-                    A.p[i] = A.p[i] + (double)s_new[i] * alpha;
-                    const double rn = A.r[i] + A.as[i] * -alpha;
-                    A.r[i] = rn;
-                    if (kF32) A.rf[i] = (F)rn;
-                    mx = smax(mx, fabs(rn));
+            {
+                double *__restrict__ pp = A.p;
+                double *__restrict__ rp = A.r;
+                const double *__restrict__ asp2 = A.as;
+                const F *__restrict__ sn2 = s_new;
+                const uint8_t *__restrict__ nbp2 = A.nb;
+                F *rfp = A.rf;  // aliases r in the FP64 form (not written there)
+                for (int row0 = gwarp; row0 < rows; row0 += kUnroll * nwarps) {
+#pragma unroll
+                    for (int u = 0; u < kUnroll; u++) {
+                        const int row = row0 + u * nwarps;
+                        if (row >= rows) break;
+                        const size_t i = (size_t)row * 32 + lane;
+                        if (nbp2[i] & NB_RED) {
+                            pp[i] = pp[i] + (double)sn2[i] * alpha;
+                            const double rn = rp[i] + asp2[i] * -alpha;
+                            rp[i] = rn;
+                            if (kF32) rfp[i] = (F)rn;
+                            mx = smax(mx, fabs(rn));
+                        }
+                    }
                 }
             }
-            block_store(mx, true, A.partials, 0, sm);
-            grid_barrier(A.barrier, A.flags);
-            maxError = grid_reduce(A.partials, 0, true, sm);
+            block_store(mx, true, T, 0, sm);
+            team_barrier(T, A.fl);
+            maxError = team_reduce(T, 0, true, sm);
             iterations = iter + 1;
             if (A.pinned >= 0 ? iterations >= A.pinned : maxError < kTol) {
                 status = 0;
                 break;
             }
             // z = M^-1 r; sigmaNew = z.r  (:372-376)
-            sweep<1, F>(A, R, hsm_off, nstrips_blk);
-            grid_barrier(A.barrier, A.flags);
-            d = sweep<2, F>(A, R, hsm_off, nstrips_blk);
-            block_store(d, false, A.partials, 2, sm);
-            grid_barrier(A.barrier, A.flags);
-            const double sigmaNew = grid_reduce(A.partials, 2, false, sm);
+            sweep<1, F>(A, T, R, hsm_off, nstrips_blk);
+            team_barrier(T, A.fl);
+            sweep<2, F>(A, T, R, hsm_off, nstrips_blk);
+            team_barrier(T, A.fl);
+            block_store(dot_zr(), false, T, 2, sm);
+            team_barrier(T, A.fl);
+            const double sigmaNew = team_reduce(T, 2, false, sm);
             beta = sigmaNew / sigma;
             sigma = sigmaNew;
             F *tmp = s_old;
@@ -658,11 +755,89 @@ __global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
         }
         if (status == 2) iterations = A.limit;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (T.rank == 0 && threadIdx.x == 0) {
         A.out->iterations = iterations;
         A.out->status = status;
         A.out->max_error = maxError;
         atomicAdd(A.iter_total, (unsigned long long)iterations);
+    }
+}
+
+template <typename F, int kThreads>
+__global__ void __launch_bounds__(kThreads, 1) pcg_kernel(PcgArgs<F> A) {
+    __shared__ double sm[kMaxWarps + 1];
+    const Team T{(int)blockIdx.x, (int)gridDim.x, A.barrier, A.partials};
+    Ring<F> R;
+    ring_init(R, A.K, A.stages);
+    const size_t nh = (size_t)(A.K > 1 ? A.K - 1 : 0) * A.sd.D;
+    for (size_t k = threadIdx.x; k < nh; k += kThreads)
+        ((unsigned long long *)(g_smem + halo_offset(A.K)))[k] = kSentinel;
+    __syncthreads();
+    pcg_job<F, kThreads>(A, T, R, sm);
+}
+
+// ------------------------------------------------------------ batched solves
+// Many independent scenes in one cooperative launch.  The grid is cut into
+// teams; a team of g blocks solves scenes of up to g*K strips.  Teams of one
+// size form a class and take that class's scenes from a shared queue (largest
+// estimated work first), so a team that finishes early takes the next scene.
+struct BatchTeams {
+    const int2 *block_team;   // per block: {team, rank in team}
+    const int2 *team;         // per team: {blocks, class}
+    const int2 *class_range;  // per class: {offset, count} into class_jobs
+    const int *class_jobs;    // job indices, each class in queue order
+    int *class_next;          // queue heads (zero at launch)
+    int *team_job;            // job taken by each team
+    unsigned *team_bar;       // two barrier words per team (zero at launch)
+    unsigned *all;            // launch-wide status word
+    const int4 *ctl;          // per job: {pinned pressure, pinned heat, limit pressure, limit heat}
+};
+
+// At most 128 registers per thread whatever the block size.
+template <typename F, int kThreads>
+__global__ void __launch_bounds__(kThreads, 512 / kThreads)
+    pcg_batch_kernel(const PcgArgs<F> *jobs, BatchTeams B, int mode, int heat, int pinned, int K, int stages) {
+    __shared__ double sm[kMaxWarps + 1];
+    __shared__ PcgArgs<F> sA;
+    const int2 bt = B.block_team[blockIdx.x];
+    const int2 tm = B.team[bt.x];
+    Team T{bt.y, tm.x, B.team_bar + 2 * bt.x, nullptr};
+    const Flags launch_fl{B.all, B.all};
+    Ring<F> R;
+    ring_init(R, K, stages);
+    __syncthreads();
+    for (;;) {
+        if (T.rank == 0 && threadIdx.x == 0) {
+            const int2 cr = B.class_range[tm.y];
+            const int k = atomicAdd(B.class_next + tm.y, 1);
+            *(volatile int *)(B.team_job + bt.x) = k < cr.y ? B.class_jobs[cr.x + k] : -1;
+        }
+        team_barrier(T, launch_fl);
+        const int j = *(volatile int *)(B.team_job + bt.x);
+        if (j < 0) break;
+        for (int k = threadIdx.x; k < (int)(sizeof(PcgArgs<F>) / 4); k += kThreads)
+            ((unsigned *)&sA)[k] = ((const unsigned *)(jobs + j))[k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int4 c = B.ctl[j];
+            sA.mode = mode;
+            sA.limit = heat ? c.w : c.z;
+            sA.pinned = pinned >= -1 ? pinned : (heat ? c.y : c.x);
+            sA.K = K;
+            sA.stages = stages;
+            sA.fl.all = B.all;
+        }
+        // halo rows start at the sentinel: the shared rows of this block
+        // (their length changes with the scene) and the scene's global rows
+        const size_t nh = (size_t)(K > 1 ? K - 1 : 0) * sA.sd.D;
+        for (size_t k = threadIdx.x; k < nh; k += kThreads)
+            ((unsigned long long *)(g_smem + halo_offset(K)))[k] = kSentinel;
+        const size_t ng = 2 * (size_t)sA.sd.S * sA.sd.D;
+        for (size_t k = (size_t)T.rank * kThreads + threadIdx.x; k < ng; k += (size_t)T.size * kThreads)
+            sA.halo[k] = kSentinel;
+        T.partials = sA.partials;
+        team_barrier(T, sA.fl);
+        pcg_job<F, kThreads>(sA, T, R, sm);
     }
 }
 
@@ -674,25 +849,19 @@ int strips_per_block() {
 }
 constexpr int kStages = 3;
 template <typename F>
-size_t smem_bytes(int K, int D) {
+size_t smem_bytes(int K, int D, int stages = kStages) {
     const size_t nh = (size_t)(K > 1 ? K - 1 : 0) * D;
-    return ((32 * (size_t)K + nh * 8 + 127) / 128) * 128 + (size_t)K * kStages * Ring<F>::kStageBytes;
+    return ((32 * (size_t)K + nh * 8 + 127) / 128) * 128 + (size_t)K * stages * Ring<F>::kStageBytes;
 }
 
-template <typename F>
+template <typename F, int kThreads>
 int max_coresident(size_t smem) {
-    static size_t cached_smem = 0;
-    static int cached = -1;
-    if (cached < 0 || cached_smem != smem) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaFuncSetAttribute(pcg_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel<F>, kThreads, smem);
-        cached = sms * (per > 2 ? 2 : per);
-        cached_smem = smem;
-    }
-    return cached;
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(pcg_kernel<F, kThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel<F, kThreads>, kThreads, smem);
+    return sms * (per > 2 ? 2 : per);
 }
 
 }  // namespace
@@ -705,10 +874,11 @@ int pcg_max_blocks() {
     return 2 * sms;
 }
 
+namespace {
 template <typename F>
-cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &cfg, cudaStream_t st,
-                       int *blocks_used) {
+PcgArgs<F> make_args(const Scene<F> &S, const PcgScratch &X, int heat) {
     PcgArgs<F> A;
+    std::memset(&A, 0, sizeof A);
     A.sd = S.sd;
     A.adiag = S.adiag;
     A.ax = S.ax;
@@ -726,9 +896,17 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     A.partials = X.partials;
     A.barrier = X.barrier;
     A.halo = X.halo;
-    A.flags = S.flags;
-    A.out = X.out + (cfg.heat ? 1 : 0);
+    A.fl = Flags{S.flags, S.flags};
+    A.out = X.out + (heat ? 1 : 0);
     A.iter_total = X.iter_total;
+    return A;
+}
+}  // namespace
+
+template <typename F>
+cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &cfg, cudaStream_t st,
+                       int *blocks_used) {
+    PcgArgs<F> A = make_args(S, X, cfg.heat);
     A.mode = cfg.mode;
     A.limit = cfg.limit;
     A.pinned = cfg.pinned;
@@ -736,20 +914,293 @@ cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &
     if (A.K > S.sd.S) A.K = S.sd.S;
     A.stages = kStages;
     const size_t smem = smem_bytes<F>(A.K, S.sd.D);
-    int maxb = max_coresident<F>(smem);
+    const int threads = 512;
+    const void *fn = (const void *)pcg_kernel<F, 512>;
+    int maxb = max_coresident<F, 512>(smem);
     if (maxb > X.max_blocks) maxb = X.max_blocks;
     const int need = (S.sd.S + A.K - 1) / A.K;  // blocks that own strips
     if (maxb < need) return cudaErrorInvalidConfiguration;
     const long long slots = (long long)S.sd.total();
-    int want = (int)((slots + kThreads * 4 - 1) / (kThreads * 4));
+    int want = (int)((slots + threads * 4 - 1) / (threads * 4));
     if (want < need) want = need;
     int G = want < maxb ? want : maxb;
     if (blocks_used) *blocks_used = G;
     cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
     cudaMemsetAsync(X.halo, 0xff, 2 * (size_t)S.sd.S * S.sd.D * sizeof(unsigned long long), st);
     void *args[] = {&A};
-    return cudaLaunchCooperativeKernel((const void *)pcg_kernel<F>, dim3(G), dim3(kThreads), args, smem, st);
+    return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(threads), args, smem, st);
 }
+
+// ------------------------------------------------------- batched solves, host
+struct PcgBatchPlan {
+    int precision = 0;  // sizeof(F)
+    int n = 0;
+    PcgShape shape{};
+    int grid = 0;      // co-resident blocks of the launch
+    size_t smem = 0;
+    std::vector<int> strips, diags, cells;
+    // device: [jobs pressure][jobs heat][block_team][team][class_range][class_jobs][team_job]
+    //         [zeroed at launch: class_next | team_bar | all]
+    char *dev = nullptr;
+    size_t dev_bytes = 0;
+    void *jobs[2] = {nullptr, nullptr};
+    int4 *ctl = nullptr;
+    BatchTeams B{};
+    size_t tab_off = 0, tab_bytes = 0;  // host-built tables copied each schedule
+    size_t zero_off = 0, zero_bytes = 0;
+    char *host = nullptr;  // pinned staging of the tables
+    cudaEvent_t uploaded = nullptr;
+    int nclass = 0;
+};
+
+namespace {
+constexpr int kMaxClasses = 8;  // team sizes 1, 2, 4, ... 128 blocks; class kMaxClasses: idle blocks
+size_t al256(size_t v) { return (v + 255) / 256 * 256; }
+
+template <typename F>
+const void *batch_fn(int threads) {
+    if (threads == 64) return (const void *)pcg_batch_kernel<F, 64>;
+    return threads == 128 ? (const void *)pcg_batch_kernel<F, 128> : (const void *)pcg_batch_kernel<F, 256>;
+}
+}  // namespace
+
+template <typename F>
+PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *const *scratch, int n,
+                               const PcgShape &shape, std::string *err) {
+    auto fail = [&](const std::string &m) -> PcgBatchPlan * {
+        if (err) *err = m;
+        return nullptr;
+    };
+    if (n <= 0) return fail("empty batch");
+    if ((shape.threads != 64 && shape.threads != 128 && shape.threads != 256) || shape.K < 1 ||
+        shape.K > shape.threads / 32 ||
+        shape.stages < 2 || shape.stages > 4)
+        return fail("unsupported batched PCG shape");
+    int dmax = 0, smax_ = 0;
+    for (int i = 0; i < n; i++) {
+        dmax = std::max(dmax, scenes[i]->sd.D);
+        smax_ = std::max(smax_, scenes[i]->sd.S);
+    }
+    const int need_max = (smax_ + shape.K - 1) / shape.K;
+    int cls = 0;
+    while ((1 << cls) < need_max) cls++;
+    if (cls >= kMaxClasses) return fail("scene too tall for the batched PCG shape");
+    const size_t smem = smem_bytes<F>(shape.K, dmax, shape.stages);
+    const void *fn = batch_fn<F>(shape.threads);
+    int dev = 0, sms = 0, per = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // the attribute stays at the device maximum, so a launch (or a graph
+    // replay) of any plan is valid whatever plan was created last
+    if (smem + sizeof(PcgArgs<F>) + 1024 > (size_t)optin ||
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 2048) != cudaSuccess) {
+        cudaGetLastError();
+        return fail("shared memory per block exceeds the device limit");
+    }
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, shape.threads, smem);
+    const int grid = sms * per;
+    for (int i = 0; i < n; i++)  // a scene's partial sums hold one entry per block of its team
+        if ((1 << cls) > scratch[i]->max_blocks) return fail("team larger than the scene's partial-sum buffer");
+    // every class may need a team of its size
+    int need_all = 0;
+    for (int c = 0; c <= cls; c++) need_all += 1 << c;
+    if (grid < need_all) return fail("too few co-resident blocks for the batched PCG shape");
+
+    PcgBatchPlan *P = new PcgBatchPlan;
+    P->precision = (int)sizeof(F);
+    P->n = n;
+    P->shape = shape;
+    P->grid = grid;
+    P->smem = smem;
+    for (int i = 0; i < n; i++) {
+        P->strips.push_back(scenes[i]->sd.S);
+        P->diags.push_back(scenes[i]->sd.D);
+        P->cells.push_back(scenes[i]->w * scenes[i]->h);
+    }
+    size_t off = 0;
+    const size_t o_jobs0 = off;
+    off = al256(off + n * sizeof(PcgArgs<F>));
+    const size_t o_jobs1 = off;
+    off = al256(off + n * sizeof(PcgArgs<F>));
+    P->tab_off = off;
+    const size_t o_bt = off;
+    off = al256(off + grid * sizeof(int2));
+    const size_t o_team = off;
+    off = al256(off + grid * sizeof(int2));
+    const size_t o_cr = off;
+    off = al256(off + (kMaxClasses + 1) * sizeof(int2));
+    const size_t o_cj = off;
+    off = al256(off + n * sizeof(int));
+    P->tab_bytes = off - P->tab_off;
+    const size_t o_ctl = off;
+    off = al256(off + n * sizeof(int4));
+    const size_t o_tj = off;
+    off = al256(off + grid * sizeof(int));
+    P->zero_off = off;
+    const size_t o_cn = off;
+    off += (kMaxClasses + 1) * sizeof(int);
+    const size_t o_tb = off;
+    off += 2 * grid * sizeof(unsigned);
+    const size_t o_all = off;
+    off += sizeof(unsigned);
+    P->zero_bytes = off - P->zero_off;
+    P->dev_bytes = al256(off);
+    if (cudaMalloc(&P->dev, P->dev_bytes) != cudaSuccess ||
+        cudaMallocHost(&P->host, P->tab_bytes) != cudaSuccess ||
+        cudaEventCreateWithFlags(&P->uploaded, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        pcg_batch_destroy(P);
+        return fail("device allocation for the batched PCG tables failed");
+    }
+    P->jobs[0] = P->dev + o_jobs0;
+    P->jobs[1] = P->dev + o_jobs1;
+    P->B.block_team = (const int2 *)(P->dev + o_bt);
+    P->B.team = (const int2 *)(P->dev + o_team);
+    P->B.class_range = (const int2 *)(P->dev + o_cr);
+    P->B.class_jobs = (const int *)(P->dev + o_cj);
+    P->B.team_job = (int *)(P->dev + o_tj);
+    P->B.class_next = (int *)(P->dev + o_cn);
+    P->B.team_bar = (unsigned *)(P->dev + o_tb);
+    P->B.all = (unsigned *)(P->dev + o_all);
+    P->ctl = (int4 *)(P->dev + o_ctl);
+    P->B.ctl = P->ctl;
+    std::vector<PcgArgs<F>> a0(n), a1(n);
+    for (int i = 0; i < n; i++) {
+        a0[i] = make_args(*scenes[i], *scratch[i], 0);
+        a1[i] = make_args(*scenes[i], *scratch[i], 1);
+    }
+    if (cudaMemcpy(P->jobs[0], a0.data(), n * sizeof(PcgArgs<F>), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(P->jobs[1], a1.data(), n * sizeof(PcgArgs<F>), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        pcg_batch_destroy(P);
+        return fail("upload of the batched PCG jobs failed");
+    }
+    return P;
+}
+
+void pcg_batch_destroy(PcgBatchPlan *P) {
+    if (!P) return;
+    if (P->uploaded) {
+        cudaEventSynchronize(P->uploaded);
+        cudaEventDestroy(P->uploaded);
+    }
+    if (P->host) cudaFreeHost(P->host);
+    if (P->dev) cudaFree(P->dev);
+    delete P;
+}
+
+int pcg_batch_grid(const PcgBatchPlan *P) { return P->grid; }
+
+// Teams and queues from the estimated work of each scene.  Scenes go to the
+// class of the smallest power-of-two team that covers their strips; every
+// non-empty class gets one team, then the remaining blocks go, one team at a
+// time, to the class whose estimated finish (work / teams, or its largest
+// scene) is latest, while that finish still improves.  Each queue is ordered
+// by work, largest first.  Returns the blocks in teams, or -1 when the
+// classes' first teams alone exceed the grid.
+int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work, int *teams,
+                   std::vector<std::vector<int>> *queues) {
+    std::vector<std::vector<int>> members(kMaxClasses);
+    for (int i = 0; i < n; i++) {
+        const int need = (strips[i] + K - 1) / K;
+        int c = 0;
+        while ((1 << c) < need) c++;
+        if (c >= kMaxClasses) return -1;
+        members[c].push_back(i);
+    }
+    double tot[kMaxClasses] = {0}, big[kMaxClasses] = {0};
+    for (int c = 0; c < kMaxClasses; c++) {
+        std::stable_sort(members[c].begin(), members[c].end(), [&](int a, int b) { return work[a] > work[b]; });
+        for (int i : members[c]) {
+            tot[c] += work[i];
+            big[c] = std::max(big[c], work[i]);
+        }
+    }
+    int left = grid;
+    for (int c = 0; c < kMaxClasses; c++) {
+        teams[c] = members[c].empty() ? 0 : 1;
+        left -= teams[c] << c;
+    }
+    if (left < 0) return -1;
+    for (;;) {
+        int best = -1;
+        double bt = -1.0;
+        for (int c = 0; c < kMaxClasses; c++) {
+            if (members[c].empty()) continue;
+            const double fin = std::max(tot[c] / teams[c], big[c]);
+            if (fin > bt) {
+                bt = fin;
+                best = c;
+            }
+        }
+        if (best < 0 || teams[best] >= (int)members[best].size() || (1 << best) > left ||
+            std::max(tot[best] / (teams[best] + 1), big[best]) >= bt)
+            break;
+        teams[best]++;
+        left -= 1 << best;
+    }
+    if (queues) *queues = std::move(members);
+    return grid - left;
+}
+
+int pcg_batch_schedule(PcgBatchPlan *P, const double *work, cudaStream_t st) {
+    int teams[kMaxClasses];
+    std::vector<std::vector<int>> members;
+    if (pcg_plan_teams(P->grid, P->shape.K, P->n, P->strips.data(), work, teams, &members) < 0) return -1;
+    // host tables
+    if (cudaEventSynchronize(P->uploaded) != cudaSuccess) return -2;  // staging free again
+    char *h = P->host;
+    const size_t base = P->tab_off;
+    auto at = [&](const void *devp) { return h + ((const char *)devp - (P->dev + base)); };
+    int2 *bt = (int2 *)at(P->B.block_team);
+    int2 *tm = (int2 *)at(P->B.team);
+    int2 *cr = (int2 *)at(P->B.class_range);
+    int *cj = (int *)at(P->B.class_jobs);
+    int blk = 0, team = 0, pos = 0;
+    for (int c = 0; c < kMaxClasses; c++) {
+        cr[c] = make_int2(pos, (int)members[c].size());
+        for (int i : members[c]) cj[pos++] = i;
+        for (int t = 0; t < teams[c]; t++, team++) {
+            tm[team] = make_int2(1 << c, c);
+            for (int r = 0; r < (1 << c); r++) bt[blk++] = make_int2(team, r);
+        }
+    }
+    // blocks left over form one-block teams of the empty idle class
+    cr[kMaxClasses] = make_int2(pos, 0);
+    for (; blk < P->grid; blk++, team++) {
+        tm[team] = make_int2(1, kMaxClasses);
+        bt[blk] = make_int2(team, 0);
+    }
+    if (cudaMemcpyAsync(P->dev + base, h, P->tab_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaEventRecord(P->uploaded, st) != cudaSuccess)
+        return -2;
+    return 0;
+}
+
+int4 *pcg_batch_ctl(PcgBatchPlan *P) { return P->ctl; }
+
+// cfg.pinned >= -1 applies to every scene; -2 takes each scene's entry of the
+// control table (cfg.limit is unused: limits come from the table).
+template <typename F>
+cudaError_t launch_pcg_batch(PcgBatchPlan *P, const PcgConfig &cfg, cudaStream_t st) {
+    if (P->precision != (int)sizeof(F)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(P->dev + P->zero_off, 0, P->zero_bytes, st);
+    if (e != cudaSuccess) return e;
+    const PcgArgs<F> *jobs = (const PcgArgs<F> *)P->jobs[cfg.heat ? 1 : 0];
+    BatchTeams B = P->B;
+    int mode = cfg.mode, heat = cfg.heat, pinned = cfg.pinned, K = P->shape.K, stages = P->shape.stages;
+    void *args[] = {&jobs, &B, &mode, &heat, &pinned, &K, &stages};
+    return cudaLaunchCooperativeKernel(batch_fn<F>(P->shape.threads), dim3(P->grid), dim3(P->shape.threads), args,
+                                       P->smem, st);
+}
+
+template PcgBatchPlan *pcg_batch_create<double>(const Scene<double> *const *, const PcgScratch *const *, int,
+                                                const PcgShape &, std::string *);
+template PcgBatchPlan *pcg_batch_create<float>(const Scene<float> *const *, const PcgScratch *const *, int,
+                                               const PcgShape &, std::string *);
+template cudaError_t launch_pcg_batch<double>(PcgBatchPlan *, const PcgConfig &, cudaStream_t);
+template cudaError_t launch_pcg_batch<float>(PcgBatchPlan *, const PcgConfig &, cudaStream_t);
 
 template cudaError_t launch_pcg<double>(const Scene<double> &, const PcgScratch &, const PcgConfig &,
                                         cudaStream_t, int *);

@@ -267,6 +267,9 @@ class SolverImpl final : public SolverBase {
 
     size_t pitch() const override { return (size_t)P_; }
     size_t device_bytes() const override { return arena_bytes_; }
+    void *scene_ptr() override { return &S_; }
+    void *scratch_ptr() override { return &scratch_; }
+    bool has_quantity(int q) const override { return q >= 0 && q < 4 && present(q); }
 
   private:
     bool present(int q) const { return q != 1 || nq_ == 4; }
@@ -353,23 +356,7 @@ class SolverImpl final : public SolverBase {
             return IFL_ERR_CUDA;  // the previous upload must have left the buffer
         }
         DevBody *db = staging_;
-        for (size_t i = 0; i < bodies_.size(); i++) {
-            const ifl_body &b = bodies_[i];
-            DevBody &d = db[i];
-            d.type = b.type;
-            d.pad_ = 0;
-            d.px = b.pos_x;
-            d.py = b.pos_y;
-            d.sx = b.scale_x;
-            d.sy = b.type == 0 ? b.scale_y : b.scale_x;  // SolidSphere(x, y, s, ...) sets both scales to s
-            d.vx = b.vel_x;
-            d.vy = b.vel_y;
-            d.vth = b.vel_theta;
-            d.cpos = std::cos(b.theta);
-            d.spos = std::sin(b.theta);
-            d.cneg = std::cos(-b.theta);
-            d.sneg = std::sin(-b.theta);
-        }
+        for (size_t i = 0; i < bodies_.size(); i++) to_dev_body(bodies_[i], db[i]);
         if (check(cudaMemcpyAsync(d_bodies_, db, bodies_.size() * sizeof(DevBody), cudaMemcpyHostToDevice,
                                   stream_),
                   "bodies") ||
@@ -450,6 +437,22 @@ class SolverImpl final : public SolverBase {
     size_t arena_bytes_ = 0;
     int P_ = 0, rows_ = 0, nq_ = 3, max_blocks_ = 1;
 };
+
+void to_dev_body(const ifl_body &b, DevBody &d) {
+    d.type = b.type;
+    d.pad_ = 0;
+    d.px = b.pos_x;
+    d.py = b.pos_y;
+    d.sx = b.scale_x;
+    d.sy = b.type == 0 ? b.scale_y : b.scale_x;  // SolidSphere(x, y, s, ...) sets both scales to s
+    d.vx = b.vel_x;
+    d.vy = b.vel_y;
+    d.vth = b.vel_theta;
+    d.cpos = std::cos(b.theta);
+    d.spos = std::sin(b.theta);
+    d.cneg = std::cos(-b.theta);
+    d.sneg = std::sin(-b.theta);
+}
 
 // ------------------------------------------------------------ SolverBase
 int SolverBase::tbegin(int group) {

@@ -26,6 +26,15 @@ class SolverBase {
     virtual size_t pitch() const = 0;
     virtual size_t device_bytes() const = 0;
 
+    // Access for the batch (batch.cu): Scene<F>* and PcgScratch* of this
+    // handle, F as its precision.
+    virtual void *scene_ptr() = 0;
+    virtual void *scratch_ptr() = 0;
+    virtual bool has_quantity(int q) const = 0;
+    void count_step() { steps_++; }
+    int pinned_pressure() const { return pinned_; }
+    int pinned_heat() const { return pinned_heat_; }
+
     int set_bodies(const ifl_body *b, int n);
     int advance_bodies(double dt);
     const std::vector<ifl_body> &bodies() const { return bodies_; }
@@ -73,5 +82,29 @@ class SolverBase {
 };
 
 std::unique_ptr<SolverBase> make_solver(const ifl_params &p);
+
+// Host-side conversion of a body to its device record (trigonometry by the C library).
+void to_dev_body(const ifl_body &b, DevBody &d);
+
+// A batch of handles stepped together (batch.cu).
+class BatchBase {
+  public:
+    virtual ~BatchBase() = default;
+    virtual int set_inflows(int member, const ifl_inflow *rects, int n) = 0;
+    virtual int update(double dt) = 0;
+    virtual int get_stats(ifl_step_stats *out, int n) = 0;
+    virtual int info(ifl_batch_info *out) = 0;
+    virtual cudaStream_t stream() const = 0;
+    virtual int device() const = 0;
+    const std::string &error() const { return err_; }
+    void set_error(const std::string &e) { err_ = e; }
+
+  protected:
+    std::string err_;
+};
+
+// Validates the members (one device, variant and precision) and builds the batch.
+int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, std::unique_ptr<BatchBase> *out,
+               std::string *err);
 
 }  // namespace ifl

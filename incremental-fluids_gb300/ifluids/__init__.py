@@ -38,7 +38,9 @@ EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", 
            "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_flip", "ifl_get_stats",
            "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
            "ifl_set_timing", "ifl_get_timing", "ifl_pcg_solve_noalloc",
-           "ifl_last_error", "ifl_version")
+           "ifl_batch_default_options", "ifl_batch_create", "ifl_batch_destroy", "ifl_batch_set_inflows",
+           "ifl_batch_update", "ifl_batch_get_stats", "ifl_batch_get_info", "ifl_batch_stream",
+           "ifl_batch_last_error", "ifl_batch_plan_teams", "ifl_last_error", "ifl_version")
 
 
 def field_id(quantity: int, array: int) -> int:
@@ -78,6 +80,22 @@ class PcgStats(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("pressure", PcgStats), ("heat", PcgStats), ("device_flags", C.c_uint32),
                 ("steps", C.c_uint32)]
+
+
+class Inflow(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("x", "y", "w", "h", "d", "t", "u", "v")]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("strips_per_block", C.c_int32), ("stages", C.c_int32),
+                ("use_graph", C.c_int32), ("tune_iterations", C.c_int32), ("pad_", C.c_int32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("members", C.c_int32), ("threads", C.c_int32), ("strips_per_block", C.c_int32),
+                ("stages", C.c_int32), ("grid", C.c_int32), ("graph", C.c_int32), ("candidates", C.c_int32),
+                ("pad_", C.c_int32), ("candidate_ms", C.c_double * 8), ("last_step_ms", C.c_double),
+                ("last_pcg_ms", C.c_double), ("launches", C.c_int64), ("steps", C.c_int64)]
 
 
 class IflError(RuntimeError):
@@ -127,6 +145,19 @@ def load_library(path: str = LIB_PATH):
     L.ifl_last_error.argtypes = [vp]
     L.ifl_last_error.restype = C.c_char_p
     L.ifl_version.restype = C.c_char_p
+    L.ifl_batch_default_options.argtypes = [C.POINTER(BatchOptions)]
+    L.ifl_batch_default_options.restype = None
+    L.ifl_batch_create.argtypes = [C.POINTER(vp), i, C.POINTER(BatchOptions), C.POINTER(vp)]
+    L.ifl_batch_destroy.argtypes = [vp]
+    L.ifl_batch_set_inflows.argtypes = [vp, i, C.POINTER(Inflow), i]
+    L.ifl_batch_update.argtypes = [vp, d]
+    L.ifl_batch_get_stats.argtypes = [vp, C.POINTER(StepStats), i]
+    L.ifl_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    L.ifl_batch_stream.argtypes = [vp]
+    L.ifl_batch_stream.restype = vp
+    L.ifl_batch_last_error.argtypes = [vp]
+    L.ifl_batch_last_error.restype = C.c_char_p
+    L.ifl_batch_plan_teams.argtypes = [i, i, i, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -360,3 +391,99 @@ class FluidSolver:
     def launch_count(self) -> int:
         """Kernel launches this solver has issued since it was created."""
         return int(self._L.ifl_launch_count(self._h))
+
+
+def plan_teams(grid: int, strips_per_block: int, strips, work):
+    """ifl_batch_plan_teams: (blocks used, teams per class c = teams of 2**c blocks)."""
+    L = load_library()
+    n = len(strips)
+    s_ = (C.c_int * n)(*[int(v) for v in strips])
+    w_ = (C.c_double * n)(*[float(v) for v in work])
+    t_ = (C.c_int * 8)()
+    rc = L.ifl_batch_plan_teams(int(grid), int(strips_per_block), n, s_, w_, t_)
+    if rc < 0:
+        raise IflError(rc, "ifl_batch_plan_teams failed")
+    return rc, list(t_)
+
+
+class Batch:
+    """Many FluidSolver handles advanced together (ifl_batch_*).
+
+    ``Batch(solvers)`` groups handles of one variant, precision and device;
+    ``set_inflows(i, [(x, y, w, h, d, u, v), ...])`` gives member i the
+    rectangles it receives before every step (addInflow arguments, with t
+    inserted for steps 6-7); ``update(dt)`` advances every member by one
+    update() and returns when the step is complete.  Members keep their own
+    bodies (moved with SolidBody.update between steps as usual) and stay
+    ordinary handles between steps.
+    """
+
+    def __init__(self, solvers: Sequence[FluidSolver], threads: int = 0, strips_per_block: int = 0,
+                 stages: int = 0, use_graph: bool = True, tune_iterations: int = 8):
+        self._L = load_library()
+        self.solvers = list(solvers)
+        o = BatchOptions()
+        self._L.ifl_batch_default_options(C.byref(o))
+        o.threads, o.strips_per_block, o.stages = int(threads), int(strips_per_block), int(stages)
+        o.use_graph = 1 if use_graph else 0
+        o.tune_iterations = int(tune_iterations)
+        arr = (C.c_void_p * len(self.solvers))(*[s._h for s in self.solvers])
+        h_ = C.c_void_p()
+        rc = self._L.ifl_batch_create(arr, len(self.solvers), C.byref(o), C.byref(h_))
+        if rc != OK:
+            msg = self._L.ifl_batch_last_error(None)
+            raise IflError(rc, f"ifl_batch_create failed: {msg.decode() if msg else ''}")
+        self._h = h_
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ifl_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            msg = self._L.ifl_batch_last_error(self._h)
+            raise IflError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def set_inflows(self, member: int, rects):
+        rs = list(rects)
+        arr = (Inflow * max(1, len(rs)))()
+        for k, r in enumerate(rs):
+            if len(r) == 7:
+                x, y, w, h, d, u, v = r
+                t = 0.0
+            else:
+                x, y, w, h, d, t, u, v = r
+            arr[k] = Inflow(x, y, w, h, d, t, u, v)
+        self._check(self._L.ifl_batch_set_inflows(self._h, int(member), arr, len(rs)), "set_inflows")
+
+    def update(self, timestep: float):
+        for s in self.solvers:
+            s._sync_bodies()
+        self._check(self._L.ifl_batch_update(self._h, float(timestep)), "batch update")
+
+    def stats(self):
+        n = len(self.solvers)
+        arr = (StepStats * n)()
+        self._check(self._L.ifl_batch_get_stats(self._h, arr, n), "batch stats")
+        return [((a.pressure.iterations, a.pressure.status, a.pressure.max_error),
+                 (a.heat.iterations, a.heat.status, a.heat.max_error), a.device_flags) for a in arr]
+
+    def info(self) -> dict:
+        o = BatchInfo()
+        self._check(self._L.ifl_batch_get_info(self._h, C.byref(o)), "batch info")
+        return {"members": o.members, "threads": o.threads, "strips_per_block": o.strips_per_block,
+                "stages": o.stages, "grid": o.grid, "graph": bool(o.graph),
+                "candidate_ms": [o.candidate_ms[k] for k in range(min(o.candidates, 8))],
+                "last_step_ms": o.last_step_ms, "last_pcg_ms": o.last_pcg_ms,
+                "launches": int(o.launches), "steps": int(o.steps)}
+
+    @property
+    def stream(self) -> int:
+        return self._L.ifl_batch_stream(self._h) or 0
