@@ -269,6 +269,8 @@ typedef struct {
     double last_pcg_ms;                         /* of which PCG launches        */
     int64_t launches;                           /* kernels launched by the batch */
     int64_t steps;
+    int64_t h2d_bytes_last_step;                /* host -> device bytes of the last step */
+    int64_t d2h_bytes_last_step;                /* device -> host bytes of the last step */
 } ifl_batch_info;
 
 void ifl_batch_default_options(ifl_batch_options *o);

@@ -244,6 +244,8 @@ class BatchImpl final : public BatchBase {
         o->last_pcg_ms = last_pcg_ms_;
         o->launches = launches_;
         o->steps = steps_;
+        o->h2d_bytes_last_step = h2d_bytes_;
+        o->d2h_bytes_last_step = (int64_t)(2 * n_ * sizeof(PcgOut) + n_ * sizeof(unsigned));
         return IFL_OK;
     }
 
@@ -309,6 +311,8 @@ class BatchImpl final : public BatchBase {
             h_ctl_[i] = make_int4(m_[i]->pinned_pressure(), m_[i]->pinned_heat(), p.max_iter_pressure,
                                   p.max_iter_heat);
         }
+        h2d_bytes_ = (int64_t)(n_ * sizeof(Scene<F>) + nb * sizeof(DevBody) + n_ * sizeof(int4)) +
+                     (plan_ ? pcg_batch_table_bytes(plan_) : 0);
         if (check(cudaMemcpyAsync(d_scenes_, h_scenes_, n_ * sizeof(Scene<F>), cudaMemcpyHostToDevice, st_),
                   "scene table") ||
             (nb && check(cudaMemcpyAsync(d_bodies_, h_bodies_, nb * sizeof(DevBody), cudaMemcpyHostToDevice, st_),
@@ -564,6 +568,7 @@ class BatchImpl final : public BatchBase {
     bool graph_ok_ = true, capturing_ = false;
     int64_t launches_ = 0, launches_per_step_ = 0, steps_ = 0;
     double last_step_ms_ = 0.0, last_pcg_ms_ = 0.0;
+    int64_t h2d_bytes_ = 0;
 };
 
 }  // namespace

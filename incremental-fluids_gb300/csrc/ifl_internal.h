@@ -157,6 +157,7 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
                                const PcgShape &shape, std::string *err);
 void pcg_batch_destroy(PcgBatchPlan *P);
 int pcg_batch_grid(const PcgBatchPlan *P);
+size_t pcg_batch_table_bytes(const PcgBatchPlan *P);  // team/queue tables uploaded per schedule
 // Rebuilds teams and queues from the estimated work per scene (stream-ordered upload).
 int pcg_batch_schedule(PcgBatchPlan *P, const double *work, cudaStream_t st);
 // Team plan (host only): teams[c] = teams of 2^c blocks, c < 8; queues[c] =

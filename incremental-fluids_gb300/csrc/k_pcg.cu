@@ -1091,6 +1091,7 @@ void pcg_batch_destroy(PcgBatchPlan *P) {
 }
 
 int pcg_batch_grid(const PcgBatchPlan *P) { return P->grid; }
+size_t pcg_batch_table_bytes(const PcgBatchPlan *P) { return P->tab_bytes; }
 
 // Teams and queues from the estimated work of each scene.  Scenes go to the
 // class of the smallest power-of-two team that covers their strips; every

@@ -95,7 +95,8 @@ class BatchInfo(C.Structure):
     _fields_ = [("members", C.c_int32), ("threads", C.c_int32), ("strips_per_block", C.c_int32),
                 ("stages", C.c_int32), ("grid", C.c_int32), ("graph", C.c_int32), ("candidates", C.c_int32),
                 ("pad_", C.c_int32), ("candidate_ms", C.c_double * 8), ("last_step_ms", C.c_double),
-                ("last_pcg_ms", C.c_double), ("launches", C.c_int64), ("steps", C.c_int64)]
+                ("last_pcg_ms", C.c_double), ("launches", C.c_int64), ("steps", C.c_int64),
+                ("h2d_bytes_last_step", C.c_int64), ("d2h_bytes_last_step", C.c_int64)]
 
 
 class IflError(RuntimeError):
@@ -482,7 +483,9 @@ class Batch:
                 "stages": o.stages, "grid": o.grid, "graph": bool(o.graph),
                 "candidate_ms": [o.candidate_ms[k] for k in range(min(o.candidates, 8))],
                 "last_step_ms": o.last_step_ms, "last_pcg_ms": o.last_pcg_ms,
-                "launches": int(o.launches), "steps": int(o.steps)}
+                "launches": int(o.launches), "steps": int(o.steps),
+                "h2d_bytes_last_step": int(o.h2d_bytes_last_step),
+                "d2h_bytes_last_step": int(o.d2h_bytes_last_step)}
 
     @property
     def stream(self) -> int:
