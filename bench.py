@@ -512,6 +512,86 @@ def run_batch(args, rank, world, local_rank):
                                            "candidate_ms")}}
 
 
+# ------------------------------------------------------------- serving
+def run_serve(args, local_rank):
+    """Open-loop Poisson arrivals of batch-generator scenes through ifl_server_*,
+    against the plain FP64 drop-in serving one request at a time (FCFS)."""
+    import torch
+    import ifluids as ifl
+    from ifluids import scenes
+
+    rng = np.random.default_rng(4)
+    scs = scenes.batch_scenes(count=args.serve_requests, seed=4)
+    steps = [max(1, int(round(int(rng.integers(50, 501)) * args.serve_steps_scale))) for _ in scs]
+    gaps = rng.exponential(1.0 / args.serve_rate, size=len(scs))
+    offsets = np.cumsum(gaps) - gaps[0]
+    prec = ifl.FP32 if args.precision == "fp32" else ifl.FP64
+    srv = ifl.Server(precision=prec, device=local_rank, hbm_budget_bytes=int(args.serve_budget_gb * 2**30))
+    t0 = srv.now() + 0.05
+    nxt, lat, cell_steps, finished, peak = 0, [], 0, 0, 0
+    while finished < len(scs):
+        now = srv.now()
+        while nxt < len(scs) and t0 + offsets[nxt] <= now:
+            sc = scs[nxt]
+            srv.submit(sc.w, sc.h, steps[nxt], sc.bodies, sc.inflows, arrival=t0 + offsets[nxt])
+            nxt += 1
+        a, q = srv.step()
+        peak = max(peak, a)
+        for c in srv.completions():
+            lat.append(c["finished"] - c["arrival"])
+            cell_steps += c["w"] * c["h"] * c["steps"]
+            srv.release(c["id"])
+            finished += 1
+        if a == 0 and q == 0 and nxt < len(scs):
+            time.sleep(max(0.0, t0 + offsets[nxt] - srv.now()))
+    wall = srv.now() - t0
+    info = srv.info()
+    srv.close()
+
+    # plain FP64 drop-in, one request at a time: measured time of one update of each
+    # request's scene (second update), FCFS queue over the same arrivals
+    per_step = []
+    dev = torch.device("cuda", local_rank)
+    for sc in scs:
+        bs = body_objs(ifl, sc)
+        g = ifl.FluidSolver(sc.w, sc.h, sc.density, bs, variant=sc.variant, precision=ifl.FP64, device=local_rank)
+        s0 = torch.cuda.ExternalStream(g.stream, device=dev)
+        for k in range(2):
+            for r in sc.inflows:
+                g.addInflow(*r[:5], *r[6:])
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s0):
+                e0.record(s0)
+            g.update(sc.dt)
+            with torch.cuda.stream(s0):
+                e1.record(s0)
+            g.synchronize()
+            for x in bs:
+                x.update(sc.dt)
+        per_step.append(e0.elapsed_time(e1) / 1e3)
+        g.close()
+    free, lat64 = 0.0, []
+    for k in range(len(scs)):
+        start = max(offsets[k], free)
+        free = start + steps[k] * per_step[k]
+        lat64.append(free - offsets[k])
+    work = sum(sc.cells * n for sc, n in zip(scs, steps))
+
+    def pct(v, q):
+        v = sorted(v)
+        return v[min(len(v) - 1, int(math.ceil(q * len(v))) - 1)]
+    return {"requests": len(scs), "arrival_rate_per_s": args.serve_rate,
+            "steps_per_request": f"U[50,500] x {args.serve_steps_scale}",
+            "p50_latency_s": round(pct(lat, 0.5), 3), "p99_latency_s": round(pct(lat, 0.99), 3),
+            "cell_steps_per_s": round(cell_steps / wall, 1), "wall_s": round(wall, 2), "peak_active": peak,
+            "batch_rebuilds": info["rebuilds"], "hbm_budget_gb": args.serve_budget_gb,
+            "fp64_one_at_a_time": {"p50_latency_s": round(pct(lat64, 0.5), 3),
+                                   "p99_latency_s": round(pct(lat64, 0.99), 3),
+                                   "cell_steps_per_s": round(work / (free - offsets[0]), 1),
+                                   "model": "FCFS over the same arrivals with each request's measured FP64 "
+                                            "drop-in update time (second update of its scene)"}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -525,6 +605,10 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--fp64-steps", type=int, default=3, help="single workload: FP64 drop-in steps")
     ap.add_argument("--fp64-sample", type=int, default=32, help="batch workload: scenes of the FP64 sample")
+    ap.add_argument("--serve-requests", type=int, default=32, help="batch workload: requests of the serving run")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-steps-scale", type=float, default=0.1, help="scale of the U[50,500] steps per request")
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget of the serving run")
     ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
@@ -590,6 +674,8 @@ def main():
     if batch:
         line["latency_ms"] = r["latency_ms"]
         line["batch"] = r["batch"]
+        if args.serve_requests > 0 and world == 1:
+            line["serving"] = run_serve(args, local_rank)
     else:
         line["pcg"] = {"iterations_last_step": r["pcg_iterations_last"], "status_last_step": r["pcg_status_last"]}
     print(json.dumps(line), flush=True)

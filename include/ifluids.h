@@ -297,6 +297,69 @@ int ifl_batch_plan_teams(int grid, int strips_per_block, int n, const int *strip
 /* NULL: why the last ifl_batch_create on this thread failed. */
 const char *ifl_batch_last_error(const ifl_batch *b);
 
+/* ------------------------------------------------------------------ serving
+ * Continuous batching of simulation requests (no counterpart in the
+ * reference, which runs one scene per process).  A request is a scene (grid
+ * size, bodies, inflow rectangles applied before every step) and a number of
+ * update() calls.  ifl_server_step admits waiting requests in arrival order
+ * while their device state fits the HBM budget and the member cap, then
+ * advances every admitted request by one update() in one batch step (see
+ * ifl_batch_update); requests that arrive while others run join at the next
+ * step.  A finished request keeps its device state until ifl_server_release.
+ * A request's results do not depend on the other requests in the batch
+ * (bit-identical alone and in any mix).  Times are seconds on the server's
+ * clock (ifl_server_now); `arrival` is supplied by the caller. */
+typedef struct ifl_server ifl_server;
+
+typedef struct {
+    int32_t variant, precision, device;
+    int32_t max_active;          /* scenes per batch step (default 1024)               */
+    double dt;                   /* time step of every request (0.0025)                */
+    int64_t hbm_budget_bytes;    /* device bytes for admitted requests; 0: no limit    */
+    int32_t dry_run;             /* 1: bookkeeping only, no device work (planning, tests) */
+    int32_t pad_;
+    ifl_batch_options batch;     /* PCG shape (threads = 0: autotuned once, then kept) */
+} ifl_server_params;
+
+typedef struct {
+    int32_t w, h, steps, n_bodies, n_inflows, pad_;
+    const ifl_body *bodies;
+    const ifl_inflow *inflows;
+    double arrival;
+} ifl_request;
+
+typedef struct {
+    int64_t id;
+    int32_t w, h, steps, pad_;
+    double arrival, admitted, finished;
+    int64_t device_bytes;
+} ifl_completion;
+
+typedef struct {
+    int32_t active, queued;
+    int64_t bytes_in_use, cell_steps, steps, rebuilds;
+    int32_t threads, strips_per_block, stages, pad_;
+} ifl_server_info;
+
+void ifl_server_default_params(ifl_server_params *p, int variant, int precision);
+int ifl_server_create(const ifl_server_params *p, ifl_server **out);
+int ifl_server_destroy(ifl_server *s);
+double ifl_server_now(const ifl_server *s);
+/* Queue a request; IFL_ERR_NOMEM when it alone exceeds the budget. */
+int ifl_server_submit(ifl_server *s, const ifl_request *r, int64_t *id);
+/* Admit, then one update() of every admitted request; returns when done. */
+int ifl_server_step(ifl_server *s, int *active, int *queued);
+/* Requests finished since the last call, in finishing order. */
+int ifl_server_completions(ifl_server *s, ifl_completion *out, int capacity, int *n);
+int ifl_server_field_shape(ifl_server *s, int64_t id, int field, int *w, int *h);
+int ifl_server_read_field(ifl_server *s, int64_t id, int field, void *host, size_t bytes, int dtype);
+int ifl_server_request_stats(ifl_server *s, int64_t id, ifl_step_stats *out);
+int ifl_server_release(ifl_server *s, int64_t id);
+int ifl_server_get_info(const ifl_server *s, ifl_server_info *out);
+const char *ifl_server_last_error(const ifl_server *s);
+/* Device bytes ifl_create allocates for these parameters (no GPU work). */
+int64_t ifl_device_bytes(const ifl_params *p);
+
 int ifl_synchronize(ifl_solver *s);
 void *ifl_stream(ifl_solver *s);
 /* Kernel launches of this library issued by the handle since creation. */

@@ -15,6 +15,12 @@ struct ifl_batch {
     std::unique_ptr<ifl::BatchBase> impl;
 };
 
+struct ifl_server {
+    ifl::Server *impl = nullptr;
+    bool dry = false;
+    ~ifl_server() { ifl::server_destroy(impl); }
+};
+
 namespace {
 template <typename Fn>
 int guarded(ifl_solver *s, Fn fn) {
@@ -53,6 +59,27 @@ int bguarded(ifl_batch *b, Fn fn) {
     }
 }
 }  // namespace
+
+namespace {
+template <typename Fn>
+int sguarded(ifl_server *s, Fn fn) {
+    if (!s || !s->impl) return IFL_ERR_ARG;
+    if (!s->dry && cudaSetDevice(ifl::server_device(s->impl)) != cudaSuccess) {
+        ifl::server_set_error(s->impl, "cannot make the server's device current");
+        return IFL_ERR_CUDA;
+    }
+    try {
+        return fn(s->impl);
+    } catch (const std::bad_alloc &) {
+        ifl::server_set_error(s->impl, "host allocation failed");
+        return IFL_ERR_NOMEM;
+    } catch (...) {
+        ifl::server_set_error(s->impl, "internal error");
+        return IFL_ERR_ARG;
+    }
+}
+}  // namespace
+
 
 extern "C" {
 
@@ -204,6 +231,99 @@ int64_t ifl_launch_count(const ifl_solver *s) { return (s && s->impl) ? s->impl-
 
 const char *ifl_last_error(const ifl_solver *s) {
     return (s && s->impl) ? s->impl->error().c_str() : "invalid handle";
+}
+
+// ------------------------------------------------------------------ serving
+void ifl_server_default_params(ifl_server_params *p, int variant, int precision) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->variant = variant;
+    p->precision = precision;
+    p->max_active = 1024;
+    p->dt = 0.0025;
+    ifl_batch_default_options(&p->batch);
+}
+
+int ifl_server_create(const ifl_server_params *p, ifl_server **out) {
+    if (!p || !out) return IFL_ERR_ARG;
+    *out = nullptr;
+    if (p->variant < IFL_PLAIN || p->variant > IFL_VARDENS || (p->precision != IFL_FP64 && p->precision != IFL_FP32) ||
+        p->device < 0 || p->max_active < 1 || !(p->dt > 0.0) || p->hbm_budget_bytes < 0)
+        return IFL_ERR_ARG;
+    if (!p->dry_run && cudaSetDevice(p->device) != cudaSuccess) {
+        cudaGetLastError();
+        return IFL_ERR_CUDA;
+    }
+    ifl_server *s = new (std::nothrow) ifl_server;
+    if (!s) return IFL_ERR_NOMEM;
+    try {
+        s->impl = ifl::server_create(*p);
+    } catch (...) {
+        delete s;
+        return IFL_ERR_NOMEM;
+    }
+    s->dry = p->dry_run != 0;
+    *out = s;
+    return IFL_OK;
+}
+
+int ifl_server_destroy(ifl_server *s) {
+    if (!s) return IFL_ERR_ARG;
+    if (!s->dry) cudaSetDevice(ifl::server_device(s->impl));
+    delete s;
+    return IFL_OK;
+}
+
+double ifl_server_now(const ifl_server *s) { return (s && s->impl) ? ifl::server_now(s->impl) : 0.0; }
+
+int ifl_server_submit(ifl_server *s, const ifl_request *r, int64_t *id) {
+    if (!r) return IFL_ERR_ARG;
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_submit(v, *r, id); });
+}
+
+int ifl_server_step(ifl_server *s, int *active, int *queued) {
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_step(v, active, queued); });
+}
+
+int ifl_server_completions(ifl_server *s, ifl_completion *out, int capacity, int *n) {
+    if (capacity < 0 || (capacity > 0 && !out)) return IFL_ERR_ARG;
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_completions(v, out, capacity, n); });
+}
+
+int ifl_server_read_field(ifl_server *s, int64_t id, int field, void *host, size_t bytes, int dtype) {
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_read_field(v, id, field, host, bytes, dtype); });
+}
+
+int ifl_server_field_shape(ifl_server *s, int64_t id, int field, int *w, int *h) {
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_field_shape(v, id, field, w, h); });
+}
+
+int ifl_server_request_stats(ifl_server *s, int64_t id, ifl_step_stats *out) {
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_stats(v, id, out); });
+}
+
+int ifl_server_release(ifl_server *s, int64_t id) {
+    return sguarded(s, [&](ifl::Server *v) { return ifl::server_release(v, id); });
+}
+
+int ifl_server_get_info(const ifl_server *s, ifl_server_info *out) {
+    if (!s || !s->impl || !out) return IFL_ERR_ARG;
+    ifl::server_info(s->impl, out);
+    return IFL_OK;
+}
+
+const char *ifl_server_last_error(const ifl_server *s) {
+    return (s && s->impl) ? ifl::server_error(s->impl).c_str() : "invalid server";
+}
+
+int64_t ifl_device_bytes(const ifl_params *p) {
+    if (!p || p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768 || p->variant < IFL_PLAIN ||
+        p->variant > IFL_VARDENS || (p->precision != IFL_FP64 && p->precision != IFL_FP32))
+        return IFL_ERR_ARG;
+    int sms = 152, dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    return (int64_t)ifl::solver_device_bytes(*p, 2 * sms);
 }
 
 const char *ifl_version(void) { return "ifluids-gb300 0.2 (sm_103a)"; }

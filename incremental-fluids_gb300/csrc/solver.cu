@@ -40,6 +40,18 @@ class SolverImpl final : public SolverBase {
     explicit SolverImpl(const ifl_params &prm) : SolverBase(prm) {}
     ~SolverImpl() override { release(); }
 
+    // Device bytes init() allocates for these parameters (no GPU work).
+    static size_t arena_size(const ifl_params &prm, int max_blocks) {
+        SolverImpl s(prm);
+        s.P_ = (int)align_up((size_t)prm.w + 2, 32);
+        s.rows_ = prm.h + 2;
+        s.nq_ = prm.variant >= IFL_HEAT ? 4 : 3;
+        s.max_blocks_ = max_blocks;
+        Carver c;
+        s.carve(nullptr, c);
+        return c.off;
+    }
+
     int init() override {
         const int w = prm_.w, h = prm_.h;
         if (check(cudaSetDevice(prm_.device), "set device")) return IFL_ERR_CUDA;
@@ -631,6 +643,11 @@ int SolverBase::write_field(int field, const void *host, size_t bytes, int dtype
         check(cudaStreamSynchronize(stream()), "write sync"))
         return IFL_ERR_CUDA;
     return IFL_OK;
+}
+
+size_t solver_device_bytes(const ifl_params &p, int max_blocks) {
+    if (p.precision == IFL_FP32) return SolverImpl<float>::arena_size(p, max_blocks);
+    return SolverImpl<double>::arena_size(p, max_blocks);
 }
 
 std::unique_ptr<SolverBase> make_solver(const ifl_params &p) {

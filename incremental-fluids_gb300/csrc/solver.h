@@ -82,6 +82,9 @@ class SolverBase {
 };
 
 std::unique_ptr<SolverBase> make_solver(const ifl_params &p);
+// Device bytes a handle of these parameters allocates (max_blocks: PCG partial
+// sums per scene, 2 x the SM count on the device).
+size_t solver_device_bytes(const ifl_params &p, int max_blocks);
 
 // Host-side conversion of a body to its device record (trigonometry by the C library).
 void to_dev_body(const ifl_body &b, DevBody &d);
@@ -102,6 +105,23 @@ class BatchBase {
   protected:
     std::string err_;
 };
+
+// Continuous-batching request loop (server.cpp).
+class Server;
+Server *server_create(const ifl_server_params &p);
+void server_destroy(Server *s);
+double server_now(const Server *s);
+int server_submit(Server *s, const ifl_request &r, int64_t *id);
+int server_step(Server *s, int *active, int *queued);
+int server_completions(Server *s, ifl_completion *out, int capacity, int *n);
+int server_read_field(Server *s, int64_t id, int field, void *host, size_t bytes, int dtype);
+int server_stats(Server *s, int64_t id, ifl_step_stats *st);
+int server_field_shape(Server *s, int64_t id, int field, int *w, int *h);
+int server_release(Server *s, int64_t id);
+void server_info(const Server *s, ifl_server_info *out);
+const std::string &server_error(const Server *s);
+void server_set_error(Server *s, const std::string &e);
+int server_device(const Server *s);
 
 // Validates the members (one device, variant and precision) and builds the batch.
 int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, std::unique_ptr<BatchBase> *out,

@@ -40,7 +40,10 @@ EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", 
            "ifl_set_timing", "ifl_get_timing", "ifl_pcg_solve_noalloc",
            "ifl_batch_default_options", "ifl_batch_create", "ifl_batch_destroy", "ifl_batch_set_inflows",
            "ifl_batch_update", "ifl_batch_get_stats", "ifl_batch_get_info", "ifl_batch_stream",
-           "ifl_batch_last_error", "ifl_batch_plan_teams", "ifl_last_error", "ifl_version")
+           "ifl_batch_last_error", "ifl_batch_plan_teams", "ifl_server_default_params", "ifl_server_create",
+           "ifl_server_destroy", "ifl_server_now", "ifl_server_submit", "ifl_server_step",
+           "ifl_server_completions", "ifl_server_field_shape", "ifl_server_read_field", "ifl_server_request_stats", "ifl_server_release",
+           "ifl_server_get_info", "ifl_server_last_error", "ifl_device_bytes", "ifl_last_error", "ifl_version")
 
 
 def field_id(quantity: int, array: int) -> int:
@@ -97,6 +100,30 @@ class BatchInfo(C.Structure):
                 ("pad_", C.c_int32), ("candidate_ms", C.c_double * 8), ("last_step_ms", C.c_double),
                 ("last_pcg_ms", C.c_double), ("launches", C.c_int64), ("steps", C.c_int64),
                 ("h2d_bytes_last_step", C.c_int64), ("d2h_bytes_last_step", C.c_int64)]
+
+
+class ServerParams(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32), ("max_active", C.c_int32),
+                ("dt", C.c_double), ("hbm_budget_bytes", C.c_int64), ("dry_run", C.c_int32), ("pad_", C.c_int32),
+                ("batch", BatchOptions)]
+
+
+class Request(C.Structure):
+    _fields_ = [("w", C.c_int32), ("h", C.c_int32), ("steps", C.c_int32), ("n_bodies", C.c_int32),
+                ("n_inflows", C.c_int32), ("pad_", C.c_int32), ("bodies", C.c_void_p), ("inflows", C.c_void_p),
+                ("arrival", C.c_double)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("id", C.c_int64), ("w", C.c_int32), ("h", C.c_int32), ("steps", C.c_int32), ("pad_", C.c_int32),
+                ("arrival", C.c_double), ("admitted", C.c_double), ("finished", C.c_double),
+                ("device_bytes", C.c_int64)]
+
+
+class ServerInfo(C.Structure):
+    _fields_ = [("active", C.c_int32), ("queued", C.c_int32), ("bytes_in_use", C.c_int64),
+                ("cell_steps", C.c_int64), ("steps", C.c_int64), ("rebuilds", C.c_int64), ("threads", C.c_int32),
+                ("strips_per_block", C.c_int32), ("stages", C.c_int32), ("pad_", C.c_int32)]
 
 
 class IflError(RuntimeError):
@@ -159,6 +186,24 @@ def load_library(path: str = LIB_PATH):
     L.ifl_batch_last_error.argtypes = [vp]
     L.ifl_batch_last_error.restype = C.c_char_p
     L.ifl_batch_plan_teams.argtypes = [i, i, i, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.ifl_server_default_params.argtypes = [C.POINTER(ServerParams), i, i]
+    L.ifl_server_default_params.restype = None
+    L.ifl_server_create.argtypes = [C.POINTER(ServerParams), C.POINTER(vp)]
+    L.ifl_server_destroy.argtypes = [vp]
+    L.ifl_server_now.argtypes = [vp]
+    L.ifl_server_now.restype = d
+    L.ifl_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_int64)]
+    L.ifl_server_step.argtypes = [vp, C.POINTER(i), C.POINTER(i)]
+    L.ifl_server_completions.argtypes = [vp, C.POINTER(Completion), i, C.POINTER(i)]
+    L.ifl_server_read_field.argtypes = [vp, C.c_int64, i, vp, sz, i]
+    L.ifl_server_field_shape.argtypes = [vp, C.c_int64, i, C.POINTER(i), C.POINTER(i)]
+    L.ifl_server_request_stats.argtypes = [vp, C.c_int64, C.POINTER(StepStats)]
+    L.ifl_server_release.argtypes = [vp, C.c_int64]
+    L.ifl_server_get_info.argtypes = [vp, C.POINTER(ServerInfo)]
+    L.ifl_server_last_error.argtypes = [vp]
+    L.ifl_server_last_error.restype = C.c_char_p
+    L.ifl_device_bytes.argtypes = [C.POINTER(Params)]
+    L.ifl_device_bytes.restype = C.c_int64
     _lib = L
     return L
 
@@ -490,3 +535,125 @@ class Batch:
     @property
     def stream(self) -> int:
         return self._L.ifl_batch_stream(self._h) or 0
+
+
+def device_bytes(variant: int, w: int, h: int, precision: int = FP64) -> int:
+    """Device bytes a FluidSolver of this variant, size and precision allocates."""
+    L = load_library()
+    p = Params()
+    L.ifl_default_params(C.byref(p), variant, int(w), int(h))
+    p.precision = precision
+    n = int(L.ifl_device_bytes(C.byref(p)))
+    if n < 0:
+        raise IflError(n, "ifl_device_bytes failed")
+    return n
+
+
+class Server:
+    """Continuous-batching request loop (ifl_server_*).
+
+    ``submit(w, h, steps, bodies=(), inflows=(), arrival=None)`` queues a
+    scene; ``step()`` admits what fits and advances every admitted request by
+    one update(); ``completions()`` lists requests finished since the last
+    call; ``read_field(id, name)`` reads a finished request's field and
+    ``release(id)`` frees its device state.
+    """
+
+    def __init__(self, variant: int = SOLID, precision: int = FP32, device: int = 0, dt: float = 0.0025,
+                 hbm_budget_bytes: int = 0, max_active: int = 1024, dry_run: bool = False, threads: int = 0,
+                 strips_per_block: int = 0, stages: int = 0, use_graph: bool = True):
+        self._L = load_library()
+        p = ServerParams()
+        self._L.ifl_server_default_params(C.byref(p), variant, precision)
+        p.device, p.dt, p.hbm_budget_bytes, p.max_active = int(device), float(dt), int(hbm_budget_bytes), int(max_active)
+        p.dry_run = 1 if dry_run else 0
+        p.batch.threads, p.batch.strips_per_block, p.batch.stages = int(threads), int(strips_per_block), int(stages)
+        p.batch.use_graph = 1 if use_graph else 0
+        h_ = C.c_void_p()
+        rc = self._L.ifl_server_create(C.byref(p), C.byref(h_))
+        if rc != OK:
+            raise IflError(rc, "ifl_server_create failed")
+        self._h = h_
+        self.variant, self.precision = variant, precision
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ifl_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            msg = self._L.ifl_server_last_error(self._h)
+            raise IflError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def now(self) -> float:
+        return float(self._L.ifl_server_now(self._h))
+
+    def submit(self, w: int, h: int, steps: int, bodies=(), inflows=(), arrival=None) -> int:
+        bl = [_body_tuple(b) for b in bodies]
+        barr = (_CBody * max(1, len(bl)))()
+        for k, b in enumerate(bl):
+            barr[k].type = int(b[0])
+            (barr[k].pos_x, barr[k].pos_y, barr[k].scale_x, barr[k].scale_y, barr[k].theta, barr[k].vel_x,
+             barr[k].vel_y, barr[k].vel_theta) = [float(x) for x in b[1:9]]
+        il = list(inflows)
+        iarr = (Inflow * max(1, len(il)))()
+        for k, r in enumerate(il):
+            if len(r) == 7:
+                x, y, ww, hh, dd, u, v = r
+                t = 0.0
+            else:
+                x, y, ww, hh, dd, t, u, v = r
+            iarr[k] = Inflow(x, y, ww, hh, dd, t, u, v)
+        r = Request(int(w), int(h), int(steps), len(bl), len(il), 0, C.cast(barr, C.c_void_p),
+                    C.cast(iarr, C.c_void_p), float(self.now() if arrival is None else arrival))
+        rid = C.c_int64(0)
+        self._check(self._L.ifl_server_submit(self._h, C.byref(r), C.byref(rid)), "submit")
+        return int(rid.value)
+
+    def step(self):
+        a, q = C.c_int(0), C.c_int(0)
+        self._check(self._L.ifl_server_step(self._h, C.byref(a), C.byref(q)), "step")
+        return a.value, q.value
+
+    def completions(self):
+        out = []
+        buf = (Completion * 256)()
+        while True:
+            n = C.c_int(0)
+            self._check(self._L.ifl_server_completions(self._h, buf, 256, C.byref(n)), "completions")
+            out += [{"id": c.id, "w": c.w, "h": c.h, "steps": c.steps, "arrival": c.arrival,
+                     "admitted": c.admitted, "finished": c.finished, "device_bytes": c.device_bytes}
+                    for c in buf[:n.value]]
+            if n.value < 256:
+                return out
+
+    def read_field(self, rid: int, field, dtype=np.float64) -> np.ndarray:
+        """Copy a field of an admitted or finished request to the host."""
+        f = _NAMED[field] if isinstance(field, str) else int(field)
+        w, h = C.c_int(), C.c_int()
+        self._check(self._L.ifl_server_field_shape(self._h, rid, f, C.byref(w), C.byref(h)), "field_shape")
+        out = np.empty((h.value, w.value), dtype=dtype)
+        code = {np.dtype(np.float64): DT_F64, np.dtype(np.float32): DT_F32, np.dtype(np.uint8): DT_U8}[np.dtype(dtype)]
+        self._check(self._L.ifl_server_read_field(self._h, rid, f, out.ctypes.data, out.nbytes, code), "read_field")
+        return out
+
+    def stats(self, rid: int):
+        st = StepStats()
+        self._check(self._L.ifl_server_request_stats(self._h, rid, C.byref(st)), "stats")
+        return ((st.pressure.iterations, st.pressure.status, st.pressure.max_error),
+                (st.heat.iterations, st.heat.status, st.heat.max_error), st.device_flags)
+
+    def release(self, rid: int):
+        self._check(self._L.ifl_server_release(self._h, rid), "release")
+
+    def info(self) -> dict:
+        o = ServerInfo()
+        self._check(self._L.ifl_server_get_info(self._h, C.byref(o)), "info")
+        return {k: getattr(o, k) for k, _ in ServerInfo._fields_ if k != "pad_"}
