@@ -51,29 +51,48 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "cell-steps/s"
-# Algorithmic bytes per cell of the PCG kernels (strip-diagonal arrays; F =
-# storage width of the matrix, z, s and the MIC record {lx, ly, pc, nb}; r, p
-# and A*s are FP64; nb = 1 byte of neighbour bits; the FP32 form keeps an F
-# copy of r for the substitutions):
-#   factor     adiag, ax, ay, nb -> pc (8 B), MIC record                7F + 9
-#   setup      r, nb -> p = 0 [, r copy]; |r|_inf                       17 [+ F]
-#   forward    r copy, MIC -> z                                          6F
-#   backward   z, MIC -> z                                               6F
-#   z.r        z, r, nb                                                  F + 9
-#   s-update + matvec + dot  z, s, nb, adiag, ax, ay -> s, As            6F + 9
-#   AXPYs + norm  nb, p, s, r, As -> p, r [, r copy]                     41 + F [+ F]
-# per solve: factor + setup + forward + backward + z.r; per iteration: the last
-# two lines, and forward + backward + z.r for every iteration but the last
-# (which stops after the AXPYs).
-
-
+# Algorithmic bytes of the PCG solves, per cell, from the fused-schedule word
+# counts of the hot-path scope table (a lower bound: every array read or
+# written once per pass), with the FP32 form's storage widths: F for the
+# matrix, the MIC(0) apply operands, z and s; 8 bytes for r, p, A*s and the
+# MIC(0) factor.
+#   per iteration   s = z + beta s, A s, z.s   R z s aDiag aX aY, W s As        6F + 8
+#                   p, r AXPYs + |r|_inf       R p s r As, W p r               40 + F
+#                   forward MIC(0)             R r aX aY precon, W q            5F
+#                   backward MIC(0) + z.r      R q aX aY precon r, W z          5F + 8
+#                                                                     total   16F + 56
+#   per solve       factor                     R aDiag aX aY, W precon          3F + 8
+#                   setup                      W p, |r|_inf, first M^-1 r       10F + 24
 def pcg_bytes_per_cell(F: int, iterations: int) -> float:
     """Algorithmic bytes per cell of one solve that ran `iterations` iterations."""
+    return (3 * F + 8) + (10 * F + 24) + iterations * (16 * F + 56)
+
+
+# Bytes per cell the kernels of this library actually move for one solve (its
+# own layout: 1-byte neighbour bits, the 4-word MIC(0) record, an FP32 copy of
+# r, a separate z.r pass); reported beside the algorithmic figure.
+def pcg_kernel_bytes_per_cell(F: int, iterations: int) -> float:
     copy = F if F == 4 else 0
     factor, setup = 7 * F + 9, 17 + copy
     sweeps = 6 * F + 6 * F + F + 9
     per_iter = (6 * F + 9) + (41 + F + copy)
     return factor + setup + sweeps + iterations * per_iter + max(iterations - 1, 0) * sweeps
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """Largest value over all ranks (identity for one rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, steps: int, world: int, t_max_ms: float) -> float:
+    """Units per second over all ranks: every rank does the same work (replicas)."""
+    return world * units_per_rank * steps / (t_max_ms / 1e3)
 
 
 def load_peaks():
@@ -411,7 +430,7 @@ def run_batch(args, rank, world, local_rank):
         step(b, bodies, dt)
         step(be, bodies_e, dt)
     info0 = b.info()
-    step_ms, pcg_ms, pcg_bytes = [], [], 0.0
+    step_ms, pcg_ms, pcg_bytes, kernel_bytes = [], [], 0.0, 0.0
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
@@ -427,17 +446,14 @@ def run_batch(args, rank, world, local_rank):
                 if x[2] & 1:
                     raise RuntimeError("device-side wait timed out during the benchmark")
                 pcg_bytes += sc.cells * pcg_bytes_per_cell(fbytes, x[0][0])
+                kernel_bytes += sc.cells * pcg_kernel_bytes_per_cell(fbytes, x[0][0])
     torch.cuda.synchronize(dev)
     info = b.info()
     launches = info["launches"] - launches0
     iters = [x[0][0] for x in b.stats()]
     dev_ms = sum(step_ms)
-    t_max = dev_ms
-    if world > 1:
-        t = torch.tensor([dev_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * cells * args.steps / (t_max / 1e3)
+    t_max = max_over_ranks(dev_ms, world, dev)
+    value = whole_job_rate(cells, args.steps, world, t_max)
 
     # ---- end to end through the public API: pinned density readback of every scene
     host = [torch.empty((sc.h, sc.w), dtype=torch.float32, pin_memory=True).numpy() for sc in scs]
@@ -450,12 +466,8 @@ def run_batch(args, rank, world, local_rank):
         h2d += be.info()["h2d_bytes_last_step"]
         for m, hb in zip(members_e, host):
             m.read_field("d", dtype=np.float32, out=hb)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * cells * args.steps / e2e_s, "unit": METRIC,
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e = {"value": whole_job_rate(cells, args.steps, world, e2e_s * 1e3), "unit": METRIC,
            "h2d_bytes_per_step": int(h2d / args.steps),
            "d2h_bytes_per_step": int(cells * 4 + be.info()["d2h_bytes_last_step"])}
     be.close()
@@ -467,6 +479,8 @@ def run_batch(args, rank, world, local_rank):
     roof = {"bound": "hbm", "kernel": "pcg_batch_kernel", "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": f"of {peak_kind}",
             "traffic": None, "algorithmic_bytes_per_step": round(pcg_bytes / args.steps),
+            "kernel_bytes_per_step": round(kernel_bytes / args.steps),
+            "kernel_bytes_gbs": round(kernel_bytes / (sum(pcg_ms) / 1e3) / 1e9, 1) if sum(pcg_ms) > 0 else 0.0,
             "pcg_ms_per_step": round(sum(pcg_ms) / args.steps, 2),
             "share_of_step": round(sum(pcg_ms) / max(dev_ms, 1e-9), 4),
             "pcg_iterations": {"max": max(iters), "mean": round(sum(iters) / len(iters), 1),
