@@ -53,7 +53,6 @@ extern __shared__ __align__(128) char g_smem[];
 // Threads per block: 512 for a scene that has the GPU to itself, 256 in the
 // compact launch used when many scenes run concurrently.
 constexpr int kMaxWarps = 16;
-constexpr int kUnroll = 4;  // diagonals per warp and pass of the elementwise phases
 constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
 constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
@@ -331,6 +330,25 @@ __device__ __forceinline__ void st4(double *p, double a, double b, double c, dou
     *(double2 *)p = make_double2(a, b);
     *(double2 *)(p + 2) = make_double2(c, d);
 }
+// Float-float numbers (hi + lo, |lo| <= ulp(hi)/2): an exact product of two
+// floats and a sum with an error-free two-sum of the high parts (Knuth's
+// TwoSum; the library is compiled without contraction, so these stay exact).
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+    const float p = a * b;
+    return FF{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+    const float s = x.hi + y.hi;
+    const float bb = s - x.hi;
+    const float err = (x.hi - (s - bb)) + (y.hi - bb);
+    const float lo = err + x.lo + y.lo;
+    const float hi = s + lo;
+    return FF{hi, lo - (hi - s)};
+}
+
 // t - a*b: one fused multiply-add in the FP32 form; two roundings in FP64, as
 // the reference computes it (the FP64 path must stay bit-identical).
 __device__ __forceinline__ float msub(float t, float a, float b) { return fmaf(-a, b, t); }
@@ -595,6 +613,10 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rows = sd.S * D;  // diagonals of all strips
     const int gwarp = T.rank * kWarps + warp, nwarps = T.size * kWarps;
+    // Elementwise phases: each warp takes one contiguous run of diagonals, so
+    // the neighbouring diagonals a cell reads are mostly its own (L1 hits).
+    const int r_chunk = (rows + nwarps - 1) / nwarps;
+    const int r_begin = min(rows, gwarp * r_chunk), r_end = min(rows, r_begin + r_chunk);
     int nstrips_blk = sd.S - T.rank * A.K;
     nstrips_blk = nstrips_blk < 0 ? 0 : (nstrips_blk > A.K ? A.K : nstrips_blk);
     constexpr bool kF32 = !std::is_same<F, double>::value;
@@ -608,14 +630,22 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
         const F *__restrict__ zp = A.z;
         const double *__restrict__ rp = A.r;
         const uint8_t *__restrict__ nbp = A.nb;
-        for (int row0 = gwarp; row0 < rows; row0 += kUnroll * nwarps) {
+        constexpr int kUD = kF32 ? 16 : 8;
+        for (int row0 = r_begin; row0 < r_end; row0 += kUD) {
+            F vz[kUD];
+            double vr[kUD];
+            unsigned vn[kUD];
 #pragma unroll
-            for (int u = 0; u < kUnroll; u++) {
-                const int row = row0 + u * nwarps;
-                if (row >= rows) break;
+            for (int u = 0; u < kUD; u++) {
+                const int row = row0 + u < r_end ? row0 + u : row0;
                 const size_t i = (size_t)row * 32 + lane;
-                if (nbp[i] & NB_RED) acc += (double)zp[i] * rp[i];
+                vn[u] = row0 + u < r_end ? nbp[i] : 0u;
+                vz[u] = zp[i];
+                vr[u] = rp[i];
             }
+#pragma unroll
+            for (int u = 0; u < kUD; u++)
+                if (vn[u] & NB_RED) acc += (double)vz[u] * vr[u];
         }
         return acc;
     };
@@ -628,7 +658,7 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
 
     // p = 0; maxError = |r|_inf   (3-conjugate-gradients/Fluid.cpp:350, 354)
     double mx = 0.0;
-    for (int row = gwarp; row < rows; row += nwarps) {
+    for (int row = r_begin; row < r_end; row++) {
         const size_t i = (size_t)row * 32 + lane;
         A.p[i] = 0.0;
         if (kF32) A.rf[i] = (F)A.r[i];
@@ -670,37 +700,71 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             const F *__restrict__ ayp = A.ay;
             F *__restrict__ sn = s_new;
             double *__restrict__ asp = A.as;
-            auto snew = [&](size_t k) -> F {
-                if (iter == 0) return zp[k];
-                return (nbp[k] & NB_RED) ? F(zp[k] + so[k] * fbeta) : so[k];
-            };
-            for (int row0 = gwarp; row0 < rows; row0 += kUnroll * nwarps) {
+            // Groups of kUA diagonals: all loads of a group first, then the
+            // arithmetic and the stores, so one memory latency covers the group.
+            constexpr int kUA = 2;
+            for (int row0 = r_begin; row0 < r_end; row0 += kUA) {
+                F vz[kUA][5], vs[kUA][5], va[kUA][5];
+                unsigned vn[kUA][5];
+                unsigned fl[kUA];
+                size_t vi[kUA];
 #pragma unroll
-                for (int u = 0; u < kUnroll; u++) {
-                    const int row = row0 + u * nwarps;
-                    if (row >= rows) break;
+                for (int u = 0; u < kUA; u++) {
+                    const bool valid = row0 + u < r_end;
+                    const int row = valid ? row0 + u : row0;
                     const int s = row / D, dd = row - s * D;
                     const int x = dd - lane, y = s * 32 + lane;
                     const size_t i = (size_t)row * 32 + lane;
-                    if (x < 0 || x >= W || y >= H) {
-                        sn[i] = F(0);
-                        asp[i] = 0.0;
-                        continue;
+                    const bool in = valid && x >= 0 && x < W && y < H;
+                    const bool hl = in && x > 0, hd = in && y > 0, hr = in && x < W - 1, hu = in && y < H - 1;
+                    // a missing neighbour reads the cell itself and is not used
+                    const size_t idx[5] = {i, hl ? i - 32 : i, hd ? (lane > 0 ? i - 33 : sd.slot(x, y - 1)) : i,
+                                           hr ? i + 32 : i, hu ? (lane < 31 ? i + 33 : sd.slot(x, y + 1)) : i};
+#pragma unroll
+                    for (int c = 0; c < 5; c++) {
+                        vz[u][c] = zp[idx[c]];
+                        vs[u][c] = so[idx[c]];
+                        vn[u][c] = nbp[idx[c]];
                     }
-                    // FP64 accumulation: with FP32 storage every product is exact,
-                    // so the operator the recurrences see is the same every iteration.
-                    const F sc = snew(i);
-                    double t = (double)adp[i] * (double)sc;
-                    if (x > 0) t += (double)axp[i - 32] * (double)snew(i - 32);
-                    if (y > 0) {
-                        const size_t k = lane > 0 ? i - 33 : sd.slot(x, y - 1);
-                        t += (double)ayp[k] * (double)snew(k);
+                    va[u][0] = adp[i];
+                    va[u][1] = axp[idx[1]];
+                    va[u][2] = ayp[idx[2]];
+                    va[u][3] = axp[i];
+                    va[u][4] = ayp[i];
+                    vi[u] = i;
+                    fl[u] = (valid ? 1u : 0u) | (in ? 2u : 0u) | (hl ? 4u : 0u) | (hd ? 8u : 0u) | (hr ? 16u : 0u) |
+                            (hu ? 32u : 0u);
+                }
+#pragma unroll
+                for (int u = 0; u < kUA; u++) {
+                    if (!(fl[u] & 1u)) continue;
+                    const size_t i = vi[u];
+                    const bool in = fl[u] & 2u;
+                    F sv[5];
+#pragma unroll
+                    for (int c = 0; c < 5; c++)
+                        sv[c] = iter == 0 ? vz[u][c] : ((vn[u][c] & NB_RED) ? F(vz[u][c] + vs[u][c] * fbeta) : vs[u][c]);
+                    // The operator the CG recurrences see must be the same every
+                    // iteration (an FP32 matvec made the FP32 form stagnate): FP64
+                    // accumulation in the FP64 form (the reference's order); in the
+                    // FP32 form an error-free float-float sum of the exact products
+                    // on the FP32 pipes (GB300 runs FP64 at 1/64 of the FP32 rate).
+                    double t;
+                    if constexpr (kF32) {
+                        FF acc = ff_prod(va[u][0], sv[0]);
+#pragma unroll
+                        for (int c = 1; c < 5; c++)
+                            if (fl[u] & (2u << c)) acc = ff_add(acc, ff_prod(va[u][c], sv[c]));
+                        t = (double)acc.hi + (double)acc.lo;
+                    } else {
+                        t = (double)va[u][0] * (double)sv[0];
+#pragma unroll
+                        for (int c = 1; c < 5; c++)
+                            t = (fl[u] & (2u << c)) ? t + (double)va[u][c] * (double)sv[c] : t;
                     }
-                    if (x < W - 1) t += (double)axp[i] * (double)snew(i + 32);
-                    if (y < H - 1) t += (double)ayp[i] * (double)snew(lane < 31 ? i + 33 : sd.slot(x, y + 1));
-                    sn[i] = sc;
-                    asp[i] = t;
-                    if (nbp[i] & NB_RED) dacc += t * (double)sc;
+                    sn[i] = in ? sv[0] : F(0);
+                    asp[i] = in ? t : 0.0;
+                    if (in && (vn[u][0] & NB_RED)) dacc += t * (double)sv[0];
                 }
             }
             block_store(dacc, false, T, 1, sm);
@@ -715,15 +779,27 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 const F *__restrict__ sn2 = s_new;
                 const uint8_t *__restrict__ nbp2 = A.nb;
                 F *rfp = A.rf;  // aliases r in the FP64 form (not written there)
-                for (int row0 = gwarp; row0 < rows; row0 += kUnroll * nwarps) {
+                constexpr int kUB = kF32 ? 8 : 4;
+                for (int row0 = r_begin; row0 < r_end; row0 += kUB) {
+                    double vp[kUB], vr[kUB], vas[kUB];
+                    F vsn[kUB];
+                    unsigned vnb[kUB];
 #pragma unroll
-                    for (int u = 0; u < kUnroll; u++) {
-                        const int row = row0 + u * nwarps;
-                        if (row >= rows) break;
+                    for (int u = 0; u < kUB; u++) {
+                        const int row = row0 + u < r_end ? row0 + u : row0;
                         const size_t i = (size_t)row * 32 + lane;
-                        if (nbp2[i] & NB_RED) {
-                            pp[i] = pp[i] + (double)sn2[i] * alpha;
-                            const double rn = rp[i] + asp2[i] * -alpha;
+                        vnb[u] = row0 + u < r_end ? nbp2[i] : 0u;
+                        vp[u] = pp[i];
+                        vr[u] = rp[i];
+                        vas[u] = asp2[i];
+                        vsn[u] = sn2[i];
+                    }
+#pragma unroll
+                    for (int u = 0; u < kUB; u++) {
+                        const size_t i = (size_t)(row0 + u) * 32 + lane;
+                        if (vnb[u] & NB_RED) {
+                            pp[i] = vp[u] + (double)vsn[u] * alpha;
+                            const double rn = vr[u] + vas[u] * -alpha;
                             rp[i] = rn;
                             if (kF32) rfp[i] = (F)rn;
                             mx = smax(mx, fabs(rn));
@@ -791,6 +867,16 @@ struct BatchTeams {
     unsigned *team_bar;       // two barrier words per team (zero at launch)
     unsigned *all;            // launch-wide status word
     const int4 *ctl;          // per job: {pinned pressure, pinned heat, limit pressure, limit heat}
+    // Placement of teams across SMs: the hardware puts consecutive blocks of a
+    // launch on the same few SMs, so a team of consecutive block indices would
+    // share those SMs' pipes.  Each block instead takes the slot
+    // (its rank on its SM) x nsm + (its SM's dense index), and teams are built
+    // from consecutive slots, i.e. from blocks on different SMs.
+    const short *sm_dense;    // %smid -> dense SM index (-1: unknown); 1024 entries
+    int *sm_fill;             // blocks placed per SM (zero at launch)
+    unsigned *grid_bar;       // two barrier words over the whole grid (zero at launch)
+    unsigned *remap_fail;     // set when a block could not be placed (zero at launch)
+    int nsm, per, remap;
 };
 
 // At most 128 registers per thread whatever the block size.
@@ -799,10 +885,30 @@ __global__ void __launch_bounds__(kThreads, 512 / kThreads)
     pcg_batch_kernel(const PcgArgs<F> *jobs, BatchTeams B, int mode, int heat, int pinned, int K, int stages) {
     __shared__ double sm[kMaxWarps + 1];
     __shared__ PcgArgs<F> sA;
-    const int2 bt = B.block_team[blockIdx.x];
+    __shared__ int s_slot;
+    const Flags launch_fl{B.all, B.all};
+    if (threadIdx.x == 0) {
+        int slot = (int)blockIdx.x;
+        if (B.remap) {
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            const int d = smid < 1024u ? B.sm_dense[smid] : -1;
+            const int k = d >= 0 ? atomicAdd(B.sm_fill + d, 1) : B.per;
+            if (d >= 0 && k < B.per) slot = k * B.nsm + d;
+            else atomicOr(B.remap_fail, 1u);
+        }
+        s_slot = slot;
+    }
+    if (B.remap) {
+        // every block learns whether all of them were placed, then all follow the same rule
+        const Team G{(int)blockIdx.x, (int)gridDim.x, B.grid_bar, nullptr};
+        team_barrier(G, launch_fl);
+        if (threadIdx.x == 0 && ld_volatile(B.remap_fail)) s_slot = (int)blockIdx.x;
+    }
+    __syncthreads();
+    const int2 bt = B.block_team[s_slot];
     const int2 tm = B.team[bt.x];
     Team T{bt.y, tm.x, B.team_bar + 2 * bt.x, nullptr};
-    const Flags launch_fl{B.all, B.all};
     Ring<F> R;
     ring_init(R, K, stages);
     __syncthreads();
@@ -955,6 +1061,14 @@ struct PcgBatchPlan {
 
 namespace {
 constexpr int kMaxClasses = 8;  // team sizes 1, 2, 4, ... 128 blocks; class kMaxClasses: idle blocks
+constexpr int kMaxSmid = 1024;
+
+// Which %smid values this device's blocks run on.
+__global__ void smid_probe_kernel(int *seen) {
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    if (threadIdx.x == 0 && smid < (unsigned)kMaxSmid) seen[smid] = 1;
+}
 size_t al256(size_t v) { return (v + 255) / 256 * 256; }
 
 template <typename F>
@@ -1044,7 +1158,16 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
     off += 2 * grid * sizeof(unsigned);
     const size_t o_all = off;
     off += sizeof(unsigned);
+    const size_t o_fill = off;
+    off += sms * sizeof(int);
+    const size_t o_gbar = off;
+    off += 2 * sizeof(unsigned);
+    const size_t o_rfail = off;
+    off += sizeof(unsigned);
     P->zero_bytes = off - P->zero_off;
+    off = al256(off);
+    const size_t o_dense = off;
+    off += kMaxSmid * sizeof(short);
     P->dev_bytes = al256(off);
     if (cudaMalloc(&P->dev, P->dev_bytes) != cudaSuccess ||
         cudaMallocHost(&P->host, P->tab_bytes) != cudaSuccess ||
@@ -1065,6 +1188,38 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
     P->B.all = (unsigned *)(P->dev + o_all);
     P->ctl = (int4 *)(P->dev + o_ctl);
     P->B.ctl = P->ctl;
+    P->B.sm_fill = (int *)(P->dev + o_fill);
+    P->B.grid_bar = (unsigned *)(P->dev + o_gbar);
+    P->B.remap_fail = (unsigned *)(P->dev + o_rfail);
+    P->B.sm_dense = (const short *)(P->dev + o_dense);
+    P->B.nsm = sms;
+    P->B.per = per;
+    P->B.remap = 0;
+    {
+        // dense SM indices from a probe launch with many small blocks
+        int *seen = (int *)(P->dev + o_fill);  // scratch before first use
+        std::vector<int> hs(kMaxSmid, 0);
+        std::vector<short> dense(kMaxSmid, -1);
+        int *dseen = nullptr;
+        if (cudaMalloc(&dseen, kMaxSmid * sizeof(int)) == cudaSuccess &&
+            cudaMemset(dseen, 0, kMaxSmid * sizeof(int)) == cudaSuccess) {
+            smid_probe_kernel<<<sms * 16, 32>>>(dseen);
+            if (cudaMemcpy(hs.data(), dseen, kMaxSmid * sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess) {
+                int n = 0;
+                for (int i = 0; i < kMaxSmid; i++)
+                    if (hs[i]) dense[i] = (short)n++;
+                if (n == sms) P->B.remap = 1;
+            }
+        }
+        cudaGetLastError();
+        if (dseen) cudaFree(dseen);
+        (void)seen;
+        if (cudaMemcpy((void *)P->B.sm_dense, dense.data(), kMaxSmid * sizeof(short), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            cudaGetLastError();
+            P->B.remap = 0;
+        }
+    }
     std::vector<PcgArgs<F>> a0(n), a1(n);
     for (int i = 0; i < n; i++) {
         a0[i] = make_args(*scenes[i], *scratch[i], 0);
