@@ -329,17 +329,18 @@ class BatchImpl final : public BatchBase {
     }
 
     // Estimated PCG time of each scene: iterations x (two wavefront sweeps,
-    // D + lag per strip steps each, plus the elementwise passes over its team).
+    // D + lag per strip steps each; the elementwise passes over its team).
     int schedule() {
-        std::vector<double> work(n_);
+        std::vector<double> ws(n_), we(n_);
         for (int i = 0; i < n_; i++) {
             const Scene<F> &S = scene(i);
             const int g = pow2ceil((S.sd.S + shape_.K - 1) / shape_.K);
-            const double sweep = 2.0 * (S.sd.D + 48.0 * (S.sd.S - 1));
-            const double elem = 8.0 * (double)S.w * S.h / ((double)g * shape_.threads);
-            work[i] = iters_[i] * (sweep + elem);
+            // wavefront steps of both sweeps (D plus ~48 steps per strip hand-over)
+            // and elementwise rows per thread of the smallest team, in comparable units
+            ws[i] = iters_[i] * 2.0 * (S.sd.D + 48.0 * (S.sd.S - 1));
+            we[i] = iters_[i] * 4.0 * (double)S.w * S.h / ((double)g * shape_.threads);
         }
-        if (pcg_batch_schedule(plan_, work.data(), st_) != 0) {
+        if (pcg_batch_schedule(plan_, ws.data(), we.data(), st_) != 0) {
             err_ = "batched PCG schedule failed";
             return IFL_ERR_CUDA;
         }

@@ -400,7 +400,8 @@ int ifl_batch_plan_teams(int grid, int strips_per_block, int n, const int *strip
     for (int i = 0; i < n; i++)
         if (strips[i] <= 0 || !(work[i] >= 0.0)) return IFL_ERR_ARG;
     try {
-        const int used = ifl::pcg_plan_teams(grid, strips_per_block, n, strips, work, teams, nullptr);
+        int tsize[8];
+        const int used = ifl::pcg_plan_teams(grid, strips_per_block, n, strips, work, nullptr, teams, tsize, nullptr);
         return used < 0 ? (int)IFL_ERR_UNSUPPORTED : used;
     } catch (...) {
         return IFL_ERR_NOMEM;

@@ -106,9 +106,13 @@ struct PcgOut {
     double max_error;
 };
 
+// Diagonals per reduction chunk of the PCG's elementwise phases.
+constexpr int kPcgChunk = 64;
+inline size_t pcg_chunks(const SDIdx &sd) { return ((size_t)sd.S * sd.D + kPcgChunk - 1) / kPcgChunk; }
+
 // Scratch for the persistent PCG kernel.
 struct PcgScratch {
-    double *partials;    // 4 * max_blocks
+    double *partials;    // 4 reduction slots x pcg_chunks(sd)
     unsigned *barrier;   // 2 words
     unsigned long long *halo;  // 2 x S x D boundary rows handed between strips (sentinel protocol)
     PcgOut *out;
@@ -158,12 +162,15 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
 void pcg_batch_destroy(PcgBatchPlan *P);
 int pcg_batch_grid(const PcgBatchPlan *P);
 size_t pcg_batch_table_bytes(const PcgBatchPlan *P);  // team/queue tables uploaded per schedule
-// Rebuilds teams and queues from the estimated work per scene (stream-ordered upload).
-int pcg_batch_schedule(PcgBatchPlan *P, const double *work, cudaStream_t st);
-// Team plan (host only): teams[c] = teams of 2^c blocks, c < 8; queues[c] =
-// scenes of class c by decreasing work.  Returns the blocks used, -1 if the grid is too small.
-int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work, int *teams,
-                   std::vector<std::vector<int>> *queues);
+// Rebuilds teams and queues from the estimated work per scene: the wavefront
+// part and the elementwise part at the smallest team (stream-ordered upload).
+int pcg_batch_schedule(PcgBatchPlan *P, const double *work_sweep, const double *work_elem, cudaStream_t st);
+// Team plan (host only): class c holds the scenes whose strips need 2^c
+// blocks; teams[c] teams of tsize[c] blocks serve it; queues[c] = its scenes by
+// decreasing work.  work_elem may be null.  Returns the blocks used, -1 if the
+// grid is too small.
+int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
+                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues);
 // Device table of per-scene {pinned pressure, pinned heat, limit pressure, limit heat}.
 int4 *pcg_batch_ctl(PcgBatchPlan *P);
 template <typename F> cudaError_t launch_pcg_batch(PcgBatchPlan *P, const PcgConfig &cfg, cudaStream_t st);

@@ -53,6 +53,7 @@ extern __shared__ __align__(128) char g_smem[];
 // Threads per block: 512 for a scene that has the GPU to itself, 256 in the
 // compact launch used when many scenes run concurrently.
 constexpr int kMaxWarps = 16;
+constexpr int kChunk = kPcgChunk;  // diagonals per reduction chunk of the elementwise phases
 constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
 constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
@@ -94,6 +95,7 @@ struct PcgArgs {
     unsigned long long *iter_total;
     int mode, limit, pinned;
     int K, stages;
+    int rowsum_zero;  // 1: pressure matrix (rows sum to zero), 0: heat matrix
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -166,38 +168,6 @@ __device__ __forceinline__ double warp_sum(double v) {
 __device__ __forceinline__ double warp_max(double v) {
     for (int o = 16; o > 0; o >>= 1) v = smax(v, __shfl_down_sync(FULL, v, o));
     return v;
-}
-
-// Block partial -> partials[slot*size + rank] (fixed order).
-__device__ void block_store(double v, bool is_max, const Team &T, int slot, double *sm) {
-    const int kWarps = blockDim.x >> 5;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    v = is_max ? warp_max(v) : warp_sum(v);
-    if (lane == 0) sm[warp] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double acc = sm[0];
-        for (int i = 1; i < kWarps; i++) acc = is_max ? smax(acc, sm[i]) : acc + sm[i];
-        T.partials[slot * T.size + T.rank] = acc;
-    }
-    __syncthreads();
-}
-
-// Every block of the team reduces partials[slot][0..size) in the same fixed order.
-__device__ double team_reduce(const Team &T, int slot, bool is_max, double *sm) {
-    const int kWarps = blockDim.x >> 5;
-    const int lane = threadIdx.x & 31;
-    if (threadIdx.x < 32) {
-        double acc = 0.0;
-        const volatile double *p = T.partials + slot * T.size;
-        for (int i = lane; i < T.size; i += 32) acc = is_max ? smax(acc, (double)p[i]) : acc + p[i];
-        acc = is_max ? warp_max(acc) : warp_sum(acc);
-        if (lane == 0) sm[kWarps] = acc;
-    }
-    __syncthreads();
-    double r = sm[kWarps];
-    __syncthreads();
-    return r;
 }
 
 // ------------------------------------------------------------ halo words
@@ -613,10 +583,33 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rows = sd.S * D;  // diagonals of all strips
     const int gwarp = T.rank * kWarps + warp, nwarps = T.size * kWarps;
-    // Elementwise phases: each warp takes one contiguous run of diagonals, so
-    // the neighbouring diagonals a cell reads are mostly its own (L1 hits).
-    const int r_chunk = (rows + nwarps - 1) / nwarps;
-    const int r_begin = min(rows, gwarp * r_chunk), r_end = min(rows, r_begin + r_chunk);
+    // Elementwise phases work on chunks of kChunk diagonals; each warp takes a
+    // contiguous run of chunks (the neighbouring diagonals a cell reads are then
+    // mostly its own: L1 hits).  Every reduction is summed per chunk (lanes in
+    // diagonal order, then a fixed shuffle tree) and the chunk partials in
+    // chunk order, so the result depends on the scene alone, not on the number
+    // of blocks or warps that solve it: a scene gives bit-identical results in
+    // a single-scene launch, in any batch and with any launch shape.
+    const int nchunk = (rows + kChunk - 1) / kChunk;
+    const int c_per = (nchunk + nwarps - 1) / nwarps;
+    const int c_begin = min(nchunk, gwarp * c_per), c_end = min(nchunk, c_begin + c_per);
+    auto chunk_put = [&](int slot, int c, double v, bool is_max) {
+        v = is_max ? warp_max(v) : warp_sum(v);
+        if (lane == 0) A.partials[(size_t)slot * nchunk + c] = v;
+    };
+    auto chunk_total = [&](int slot, bool is_max) -> double {
+        if (threadIdx.x < 32) {
+            double acc = 0.0;
+            const volatile double *pt = A.partials + (size_t)slot * nchunk;
+            for (int c = lane; c < nchunk; c += 32) acc = is_max ? smax(acc, (double)pt[c]) : acc + pt[c];
+            acc = is_max ? warp_max(acc) : warp_sum(acc);
+            if (lane == 0) sm[kMaxWarps] = acc;
+        }
+        __syncthreads();
+        const double r = sm[kMaxWarps];
+        __syncthreads();
+        return r;
+    };
     int nstrips_blk = sd.S - T.rank * A.K;
     nstrips_blk = nstrips_blk < 0 ? 0 : (nstrips_blk > A.K ? A.K : nstrips_blk);
     constexpr bool kF32 = !std::is_same<F, double>::value;
@@ -626,28 +619,31 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     // sigma = z . r over the red cells (3-conjugate-gradients/Fluid.cpp:356, 376):
     // a separate pass keeps the FP64 products off the backward sweep's chain.
     auto dot_zr = [&]() {
-        double acc = 0.0;
         const F *__restrict__ zp = A.z;
         const double *__restrict__ rp = A.r;
         const uint8_t *__restrict__ nbp = A.nb;
         constexpr int kUD = kF32 ? 16 : 8;
-        for (int row0 = r_begin; row0 < r_end; row0 += kUD) {
-            F vz[kUD];
-            double vr[kUD];
-            unsigned vn[kUD];
+        for (int c = c_begin; c < c_end; c++) {
+            const int cb = c * kChunk, ce = min(rows, cb + kChunk);
+            double acc = 0.0;
+            for (int row0 = cb; row0 < ce; row0 += kUD) {
+                F vz[kUD];
+                double vr[kUD];
+                unsigned vn[kUD];
 #pragma unroll
-            for (int u = 0; u < kUD; u++) {
-                const int row = row0 + u < r_end ? row0 + u : row0;
-                const size_t i = (size_t)row * 32 + lane;
-                vn[u] = row0 + u < r_end ? nbp[i] : 0u;
-                vz[u] = zp[i];
-                vr[u] = rp[i];
+                for (int u = 0; u < kUD; u++) {
+                    const int row = row0 + u < ce ? row0 + u : row0;
+                    const size_t i = (size_t)row * 32 + lane;
+                    vn[u] = row0 + u < ce ? nbp[i] : 0u;
+                    vz[u] = zp[i];
+                    vr[u] = rp[i];
+                }
+#pragma unroll
+                for (int u = 0; u < kUD; u++)
+                    if (vn[u] & NB_RED) acc += (double)vz[u] * vr[u];
             }
-#pragma unroll
-            for (int u = 0; u < kUD; u++)
-                if (vn[u] & NB_RED) acc += (double)vz[u] * vr[u];
+            chunk_put(2, c, acc, false);
         }
-        return acc;
     };
 
     if (A.mode & PCG_FACTOR) {
@@ -657,25 +653,27 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     if (!(A.mode & PCG_SOLVE)) return;
 
     // p = 0; maxError = |r|_inf   (3-conjugate-gradients/Fluid.cpp:350, 354)
-    double mx = 0.0;
-    for (int row = r_begin; row < r_end; row++) {
-        const size_t i = (size_t)row * 32 + lane;
-        A.p[i] = 0.0;
-        if (kF32) A.rf[i] = (F)A.r[i];
-        if (A.nb[i] & NB_RED) mx = smax(mx, fabs(A.r[i]));
+    for (int c = c_begin; c < c_end; c++) {
+        double mx = 0.0;
+        for (int row = c * kChunk; row < min(rows, (c + 1) * kChunk); row++) {
+            const size_t i = (size_t)row * 32 + lane;
+            A.p[i] = 0.0;
+            if (kF32) A.rf[i] = (F)A.r[i];
+            if (A.nb[i] & NB_RED) mx = smax(mx, fabs(A.r[i]));
+        }
+        chunk_put(0, c, mx, true);
     }
-    block_store(mx, true, T, 0, sm);
     if (kF32) team_barrier(T, A.fl);  // FP32 copy of r complete
     // z = M^-1 r  (:351)
     sweep<1, F>(A, T, R, hsm_off, nstrips_blk);
     team_barrier(T, A.fl);
     sweep<2, F>(A, T, R, hsm_off, nstrips_blk);
     team_barrier(T, A.fl);
-    block_store(dot_zr(), false, T, 2, sm);
+    dot_zr();
     team_barrier(T, A.fl);
 
-    double maxError = team_reduce(T, 0, true, sm);
-    double sigma = team_reduce(T, 2, false, sm);
+    double maxError = chunk_total(0, true);
+    double sigma = chunk_total(2, false);
     int iterations = 0, status;
     if (A.pinned >= 0 ? A.pinned == 0 : maxError < kTol) {
         status = 1;
@@ -687,7 +685,6 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             // block-uniform: every thread of the block leaves together
             if (__syncthreads_or(threadIdx.x == 0 && timed_out(A.fl))) break;
             // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
-            double dacc = 0.0;
             const F fbeta = (F)beta;
             // Four diagonals per warp and pass, their loads issued together
             // (the pointers do not alias), in the same per-lane order as a
@@ -703,14 +700,17 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             // Groups of kUA diagonals: all loads of a group first, then the
             // arithmetic and the stores, so one memory latency covers the group.
             constexpr int kUA = 2;
-            for (int row0 = r_begin; row0 < r_end; row0 += kUA) {
+            for (int c = c_begin; c < c_end; c++) {
+            const int cb = c * kChunk, ce = min(rows, cb + kChunk);
+            double dacc = 0.0;
+            for (int row0 = cb; row0 < ce; row0 += kUA) {
                 F vz[kUA][5], vs[kUA][5], va[kUA][5];
                 unsigned vn[kUA][5];
                 unsigned fl[kUA];
                 size_t vi[kUA];
 #pragma unroll
                 for (int u = 0; u < kUA; u++) {
-                    const bool valid = row0 + u < r_end;
+                    const bool valid = row0 + u < ce;
                     const int row = valid ? row0 + u : row0;
                     const int s = row / D, dd = row - s * D;
                     const int x = dd - lane, y = s * 32 + lane;
@@ -744,17 +744,29 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
 #pragma unroll
                     for (int c = 0; c < 5; c++)
                         sv[c] = iter == 0 ? vz[u][c] : ((vn[u][c] & NB_RED) ? F(vz[u][c] + vs[u][c] * fbeta) : vs[u][c]);
-                    // The operator the CG recurrences see must be the same every
-                    // iteration (an FP32 matvec made the FP32 form stagnate): FP64
-                    // accumulation in the FP64 form (the reference's order); in the
-                    // FP32 form an error-free float-float sum of the exact products
-                    // on the FP32 pipes (GB300 runs FP64 at 1/64 of the FP32 rate).
+                    // FP64 form: FP64 accumulation in the reference's order.  FP32
+                    // form: an error-free float-float sum on the FP32 pipes (GB300
+                    // runs FP64 at 1/64 of the FP32 rate), and for the pressure
+                    // matrices, whose rows sum to zero in the reference
+                    // (aDiag = sum of the face factors, each off-diagonal = -factor),
+                    // the form sum_j a_ij (s_j - s_i), which keeps that property
+                    // exactly: the FP32-rounded aDiag no longer matches its
+                    // off-diagonals, and the resulting tiny, non-zero eigenvalue made
+                    // CG stagnate on some scenes (up to the 2000-iteration cap).
                     double t;
                     if constexpr (kF32) {
-                        FF acc = ff_prod(va[u][0], sv[0]);
+                        FF acc;
+                        if (A.rowsum_zero) {
+                            acc = FF{0.f, 0.f};
 #pragma unroll
-                        for (int c = 1; c < 5; c++)
-                            if (fl[u] & (2u << c)) acc = ff_add(acc, ff_prod(va[u][c], sv[c]));
+                            for (int c = 1; c < 5; c++)
+                                if (fl[u] & (2u << c)) acc = ff_add(acc, ff_prod(va[u][c], sv[c] - sv[0]));
+                        } else {
+                            acc = ff_prod(va[u][0], sv[0]);
+#pragma unroll
+                            for (int c = 1; c < 5; c++)
+                                if (fl[u] & (2u << c)) acc = ff_add(acc, ff_prod(va[u][c], sv[c]));
+                        }
                         t = (double)acc.hi + (double)acc.lo;
                     } else {
                         t = (double)va[u][0] * (double)sv[0];
@@ -767,11 +779,11 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                     if (in && (vn[u][0] & NB_RED)) dacc += t * (double)sv[0];
                 }
             }
-            block_store(dacc, false, T, 1, sm);
+            chunk_put(1, c, dacc, false);
+            }
             team_barrier(T, A.fl);
-            const double alpha = sigma / team_reduce(T, 1, false, sm);
+            const double alpha = sigma / chunk_total(1, false);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
-            mx = 0.0;
             {
                 double *__restrict__ pp = A.p;
                 double *__restrict__ rp = A.r;
@@ -780,15 +792,18 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 const uint8_t *__restrict__ nbp2 = A.nb;
                 F *rfp = A.rf;  // aliases r in the FP64 form (not written there)
                 constexpr int kUB = kF32 ? 8 : 4;
-                for (int row0 = r_begin; row0 < r_end; row0 += kUB) {
+                for (int c = c_begin; c < c_end; c++) {
+                const int cb = c * kChunk, ce = min(rows, cb + kChunk);
+                double mx = 0.0;
+                for (int row0 = cb; row0 < ce; row0 += kUB) {
                     double vp[kUB], vr[kUB], vas[kUB];
                     F vsn[kUB];
                     unsigned vnb[kUB];
 #pragma unroll
                     for (int u = 0; u < kUB; u++) {
-                        const int row = row0 + u < r_end ? row0 + u : row0;
+                        const int row = row0 + u < ce ? row0 + u : row0;
                         const size_t i = (size_t)row * 32 + lane;
-                        vnb[u] = row0 + u < r_end ? nbp2[i] : 0u;
+                        vnb[u] = row0 + u < ce ? nbp2[i] : 0u;
                         vp[u] = pp[i];
                         vr[u] = rp[i];
                         vas[u] = asp2[i];
@@ -806,10 +821,11 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                         }
                     }
                 }
+                chunk_put(0, c, mx, true);
+                }
             }
-            block_store(mx, true, T, 0, sm);
             team_barrier(T, A.fl);
-            maxError = team_reduce(T, 0, true, sm);
+            maxError = chunk_total(0, true);
             iterations = iter + 1;
             if (A.pinned >= 0 ? iterations >= A.pinned : maxError < kTol) {
                 status = 0;
@@ -820,9 +836,9 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             team_barrier(T, A.fl);
             sweep<2, F>(A, T, R, hsm_off, nstrips_blk);
             team_barrier(T, A.fl);
-            block_store(dot_zr(), false, T, 2, sm);
+            dot_zr();
             team_barrier(T, A.fl);
-            const double sigmaNew = team_reduce(T, 2, false, sm);
+            const double sigmaNew = chunk_total(2, false);
             beta = sigmaNew / sigma;
             sigma = sigmaNew;
             F *tmp = s_old;
@@ -1005,6 +1021,7 @@ PcgArgs<F> make_args(const Scene<F> &S, const PcgScratch &X, int heat) {
     A.fl = Flags{S.flags, S.flags};
     A.out = X.out + (heat ? 1 : 0);
     A.iter_total = X.iter_total;
+    A.rowsum_zero = heat ? 0 : 1;
     return A;
 }
 }  // namespace
@@ -1114,8 +1131,6 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, shape.threads, smem);
     const int grid = sms * per;
-    for (int i = 0; i < n; i++)  // a scene's partial sums hold one entry per block of its team
-        if ((1 << cls) > scratch[i]->max_blocks) return fail("team larger than the scene's partial-sum buffer");
     // every class may need a team of its size
     int need_all = 0;
     for (int c = 0; c <= cls; c++) need_all += 1 << c;
@@ -1248,15 +1263,19 @@ void pcg_batch_destroy(PcgBatchPlan *P) {
 int pcg_batch_grid(const PcgBatchPlan *P) { return P->grid; }
 size_t pcg_batch_table_bytes(const PcgBatchPlan *P) { return P->tab_bytes; }
 
-// Teams and queues from the estimated work of each scene.  Scenes go to the
-// class of the smallest power-of-two team that covers their strips; every
-// non-empty class gets one team, then the remaining blocks go, one team at a
-// time, to the class whose estimated finish (work / teams, or its largest
-// scene) is latest, while that finish still improves.  Each queue is ordered
-// by work, largest first.  Returns the blocks in teams, or -1 when the
-// classes' first teams alone exceed the grid.
-int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work, int *teams,
-                   std::vector<std::vector<int>> *queues) {
+// Teams and queues from the estimated work of each scene: work_sweep (the
+// wavefront part, which more blocks do not shorten) and work_elem (the
+// elementwise part at the smallest team, which shrinks with the team).
+// Scenes go to the class of the smallest power-of-two team that covers their
+// strips; every non-empty class gets one team.  Then, while blocks are left,
+// the class with the latest estimated finish (its work over its teams, or its
+// largest scene) gets one more team or teams twice as large (up to 128
+// blocks), whichever shortens that finish most per block spent, as long as it
+// improves.  Each queue is ordered by work, largest first.  teams[c] and
+// tsize[c] give the teams of class c; returns the blocks in teams, or -1 when
+// the classes' first teams alone exceed the grid.
+int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
+                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues) {
     std::vector<std::vector<int>> members(kMaxClasses);
     for (int i = 0; i < n; i++) {
         const int need = (strips[i] + K - 1) / K;
@@ -1265,13 +1284,21 @@ int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work
         if (c >= kMaxClasses) return -1;
         members[c].push_back(i);
     }
-    double tot[kMaxClasses] = {0}, big[kMaxClasses] = {0};
-    for (int c = 0; c < kMaxClasses; c++) {
-        std::stable_sort(members[c].begin(), members[c].end(), [&](int a, int b) { return work[a] > work[b]; });
+    auto w = [&](int i, int mult) { return work_sweep[i] + (work_elem ? work_elem[i] / mult : 0.0); };
+    int mult[kMaxClasses];
+    double tot[kMaxClasses], big[kMaxClasses];
+    auto account = [&](int c) {
+        tot[c] = big[c] = 0.0;
         for (int i : members[c]) {
-            tot[c] += work[i];
-            big[c] = std::max(big[c], work[i]);
+            tot[c] += w(i, mult[c]);
+            big[c] = std::max(big[c], w(i, mult[c]));
         }
+    };
+    for (int c = 0; c < kMaxClasses; c++) {
+        mult[c] = 1;
+        std::stable_sort(members[c].begin(), members[c].end(),
+                         [&](int a, int b) { return w(a, 1) > w(b, 1); });
+        account(c);
     }
     int left = grid;
     for (int c = 0; c < kMaxClasses; c++) {
@@ -1290,20 +1317,46 @@ int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work
                 best = c;
             }
         }
-        if (best < 0 || teams[best] >= (int)members[best].size() || (1 << best) > left ||
-            std::max(tot[best] / (teams[best] + 1), big[best]) >= bt)
+        if (best < 0) break;
+        const int c = best, size = (1 << c) * mult[c];
+        // one more team of the current size
+        const bool can_add = teams[c] < (int)members[c].size() && size <= left;
+        const double fin_add = can_add ? std::max(tot[c] / (teams[c] + 1), big[c]) : bt;
+        // every team of the class twice as large
+        const bool can_grow = work_elem && size * 2 <= 128 && teams[c] * size <= left;
+        double fin_grow = bt;
+        if (can_grow) {
+            mult[c] *= 2;
+            account(c);
+            fin_grow = std::max(tot[c] / teams[c], big[c]);
+            mult[c] /= 2;
+            account(c);
+        }
+        // the option that shortens the finish most per block spent
+        const double gain_add = can_add ? (bt - fin_add) / size : 0.0;
+        const double gain_grow = can_grow ? (bt - fin_grow) / ((double)teams[c] * size) : 0.0;
+        if (gain_add > 0.0 && gain_add >= gain_grow) {
+            teams[c]++;
+            left -= size;
+        } else if (gain_grow > 0.0) {
+            left -= teams[c] * size;
+            mult[c] *= 2;
+            account(c);
+        } else {
             break;
-        teams[best]++;
-        left -= 1 << best;
+        }
     }
+    for (int c = 0; c < kMaxClasses; c++) tsize[c] = (1 << c) * mult[c];
     if (queues) *queues = std::move(members);
     return grid - left;
 }
 
-int pcg_batch_schedule(PcgBatchPlan *P, const double *work, cudaStream_t st) {
-    int teams[kMaxClasses];
+int pcg_batch_schedule(PcgBatchPlan *P, const double *work_sweep, const double *work_elem, cudaStream_t st) {
+    int teams[kMaxClasses], tsize[kMaxClasses];
     std::vector<std::vector<int>> members;
-    if (pcg_plan_teams(P->grid, P->shape.K, P->n, P->strips.data(), work, teams, &members) < 0) return -1;
+    if (pcg_plan_teams(P->grid, P->shape.K, P->n, P->strips.data(), work_sweep, work_elem, teams, tsize, &members) <
+        0)
+        return -1;
     // host tables
     if (cudaEventSynchronize(P->uploaded) != cudaSuccess) return -2;  // staging free again
     char *h = P->host;
@@ -1318,8 +1371,8 @@ int pcg_batch_schedule(PcgBatchPlan *P, const double *work, cudaStream_t st) {
         cr[c] = make_int2(pos, (int)members[c].size());
         for (int i : members[c]) cj[pos++] = i;
         for (int t = 0; t < teams[c]; t++, team++) {
-            tm[team] = make_int2(1 << c, c);
-            for (int r = 0; r < (1 << c); r++) bt[blk++] = make_int2(team, r);
+            tm[team] = make_int2(tsize[c], c);
+            for (int r = 0; r < tsize[c]; r++) bt[blk++] = make_int2(team, r);
         }
     }
     // blocks left over form one-block teams of the empty idle class

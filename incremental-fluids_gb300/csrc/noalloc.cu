@@ -123,7 +123,7 @@ extern "C" int ifl_pcg_solve_noalloc(int w, int h, const double *adiag, const do
     S.flags = take<unsigned>(cur, 8);
     PcgScratch X{};
     X.halo = take<unsigned long long>(cur, 2 * (size_t)sd.S * sd.D);
-    X.partials = take<double>(cur, 4 * kMaxBlocks);
+    X.partials = take<double>(cur, 4 * pcg_chunks(sd));
     X.barrier = take<unsigned>(cur, 2);
     X.iter_total = take<unsigned long long>(cur, 1);
     X.out = (PcgOut *)stats;  // the solve writes its outcome straight into the caller's struct

@@ -351,7 +351,7 @@ class SolverImpl final : public SolverBase {
         S_.nbodies = 0;
         S_.flags = c.take<unsigned>(base, 8);
         scratch_.max_blocks = max_blocks_;
-        scratch_.partials = c.take<double>(base, 4 * (size_t)std::max(max_blocks_, 1));
+        scratch_.partials = c.take<double>(base, 4 * pcg_chunks(S_.sd));
         scratch_.barrier = c.take<unsigned>(base, 2);
         scratch_.halo = c.take<unsigned long long>(base, 2 * (size_t)S_.sd.S * S_.sd.D);
         scratch_.out = c.take<PcgOut>(base, 2);

@@ -10,7 +10,8 @@ Bars:
 * FP32 batch from the oracle's state: pressure (fluid cells, mean-free) and
   velocity within 1e-4 relative of the FP64 oracle after one step.
 * Replaying a step as a CUDA graph gives bit-identical fields to issuing its
-  launches directly; two identical batches give bit-identical fields.
+  launches directly; two identical batches give bit-identical fields; a
+  batched scene is bit-identical to the same scene stepped alone.
 """
 import numpy as np
 import pytest
@@ -203,18 +204,21 @@ def test_autotuner_tries_shapes_and_keeps_one(ifl):
     info = b.info()
     tried = [t for t in info["candidate_ms"] if t > 0]
     assert len(tried) >= 2
-    assert info["threads"] in (128, 256) and 1 <= info["strips_per_block"] <= info["threads"] // 32
+    assert info["threads"] in (64, 128, 256) and 1 <= info["strips_per_block"] <= info["threads"] // 32
     assert info["grid"] > 0 and info["steps"] == 2 and info["launches"] > 0
 
 
-def test_batch_matches_single_handles_on_generated_scenes(ifl):
-    """Ragged generated scenes (sides 64..320, 0-4 bodies, 1-3 inflows): the
-    FP32 batch against each scene run alone through ifl_update with the same
-    iteration counts."""
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_batch_equals_single_handles_bit_for_bit(ifl, precision):
+    """Ragged generated scenes (sides 64..320, 0-4 bodies, 1-3 inflows): every
+    PCG reduction is summed in per-scene chunks, so a scene's batched step is
+    bit-identical to the same scene stepped alone through ifl_update, whatever
+    the batch's launch shape."""
     from ifluids import scenes as SC
     sc = SC.batch_scenes(count=12, seed=7, lo=64, hi=320)
+
     def member(s):
-        return ifl.FluidSolver(s.w, s.h, 0.1, list(s.bodies), precision=ifl.FP32)
+        return ifl.FluidSolver(s.w, s.h, 0.1, list(s.bodies), precision=precision)
     batch_m = [member(s) for s in sc]
     alone = [member(s) for s in sc]
     b = ifl.Batch(batch_m)
@@ -227,16 +231,14 @@ def test_batch_matches_single_handles_on_generated_scenes(ifl):
         for i, s in enumerate(sc):
             for r in s.inflows:
                 alone[i].addInflow(*r[:5], *r[6:])
-            alone[i].set_pinned_iterations(st[i][0][0], -1)
             alone[i].update(dt)
             assert st[i][2] & 1 == 0
-            assert alone[i].stats()[0][0] == st[i][0][0]
+            assert alone[i].stats()[0][0] == st[i][0][0], (step, i)
         for m in batch_m + alone:
             m.set_bodies([_moved(bd, dt) for bd in m.bodies])
     for i in range(len(sc)):
-        for n in ("d", "u", "v"):
-            ref = alone[i].read_field(n)
-            assert rel_err(batch_m[i].read_field(n), ref) < 1e-4, (i, n)
+        for n in ("d", "u", "v", "p"):
+            assert np.array_equal(batch_m[i].read_field(n), alone[i].read_field(n)), (i, n)
 
 
 def _moved(b, dt):
