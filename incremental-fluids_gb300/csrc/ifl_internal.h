@@ -107,7 +107,7 @@ struct PcgOut {
 };
 
 // Diagonals per reduction chunk of the PCG's elementwise phases.
-constexpr int kPcgChunk = 64;
+constexpr int kPcgChunk = 16;
 inline size_t pcg_chunks(const SDIdx &sd) { return ((size_t)sd.S * sd.D + kPcgChunk - 1) / kPcgChunk; }
 
 // Scratch for the persistent PCG kernel.

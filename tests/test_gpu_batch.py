@@ -241,6 +241,27 @@ def test_batch_equals_single_handles_bit_for_bit(ifl, precision):
             assert np.array_equal(batch_m[i].read_field(n), alone[i].read_field(n)), (i, n)
 
 
+def test_fp32_form_converges_like_fp64(ifl):
+    """The FP32 form's pressure solves need about as many iterations as the
+    FP64 ones and never reach the cap: its matvec keeps the reference's exact
+    zero row sums (an FP32-rounded diagonal made CG stagnate on some scenes)."""
+    from ifluids import scenes as SC
+    sc = SC.batch_scenes(count=24, seed=11, lo=128, hi=640)
+    runs = {}
+    for prec in (ifl.FP64, ifl.FP32):
+        ms = [ifl.FluidSolver(s.w, s.h, 0.1, list(s.bodies), precision=prec) for s in sc]
+        b = ifl.Batch(ms)
+        for i, s in enumerate(sc):
+            b.set_inflows(i, s.inflows)
+        its = []
+        for _ in range(4):
+            b.update(sc[0].dt)
+            its.append([x[0][0] for x in b.stats()])
+            assert all(x[0][1] == 0 or x[0][0] == 0 for x in b.stats())  # converged (or nothing to solve)
+        runs[prec] = np.array(its)
+    assert (runs[ifl.FP32] <= 1.15 * runs[ifl.FP64] + 5).all(), (runs[ifl.FP32] - runs[ifl.FP64])
+
+
 def _moved(b, dt):
     t, x, y, sx, sy, th, vx, vy, vt = b
     return (t, x + vx * dt, y + vy * dt, sx, sy, th + vt * dt, vx, vy, vt)
