@@ -196,6 +196,9 @@ def cpu_baseline(n: int, steps: int, procs: int, seed: int):
 
 # ----------------------------------------------------------------- GPU arm
 def make_solver(ifl, sc, precision, device, bodies):
+    if sc.variant >= 6:
+        return ifl.FluidSolver(sc.w, sc.h, sc.density, sc.density_soot, sc.diffusion, bodies, variant=sc.variant,
+                               precision=precision, device=device)
     return ifl.FluidSolver(sc.w, sc.h, sc.density, bodies, variant=sc.variant, precision=precision,
                            device=device)
 
@@ -209,7 +212,10 @@ def body_objs(ifl, sc):
 
 def step_host(g, sc, bodies):
     x, y, w, h, d, t, u, v = sc.inflows[0]
-    g.addInflow(x, y, w, h, d, u, v)
+    if sc.variant >= 6:
+        g.addInflow(x, y, w, h, d, t, u, v)
+    else:
+        g.addInflow(x, y, w, h, d, u, v)
     g.update(sc.dt)
     for b in bodies:
         b.update(sc.dt)
@@ -224,7 +230,7 @@ def run_gpu(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     prec = ifl.FP32 if args.precision == "fp32" else ifl.FP64
     fbytes = 4 if prec == ifl.FP32 else 8
-    sc = scenes.config1(n=args.size, seed=args.seed)
+    sc = scenes.config3(n=args.size) if args.workload == "c3" else scenes.config1(n=args.size, seed=args.seed)
     cells = sc.cells
     # two identical solvers: one for the device-timed pass, one for the end-to-end
     # pass, so that both time the same steps (the PCG iteration count varies with
@@ -612,9 +618,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=("batch", "single"), default="batch")
+    ap.add_argument("--workload", choices=("batch", "single", "c3"), default="batch")
     ap.add_argument("--count", type=int, default=BATCH_COUNT, help="scenes of the batched workload")
-    ap.add_argument("--size", type=int, default=1024, help="side of the single-scene workload")
+    ap.add_argument("--size", type=int, default=0, help="side of the single-scene workload (1024; c3: 2048)")
     ap.add_argument("--precision", choices=("fp32", "fp64"), default="fp32")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--fp64-steps", type=int, default=3, help="single workload: FP64 drop-in steps")
@@ -626,6 +632,8 @@ def main():
     ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
+    if not args.size:
+        args.size = 2048 if args.workload == "c3" else 1024
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -639,6 +647,12 @@ def main():
                   "variant": "4-solid-boundaries", "scenes": args.count, "seed": BATCH_SEED,
                   "precision_form": args.precision,
                   "l2": "inputs larger than L2 (about 6 GB of scene state)", "scene_data": "seeded synthetic scenes"}
+    elif args.workload == "c3":
+        config = {"workload": f"heat + variable density scene {args.size}x{args.size} (7-variable-density), "
+                              f"ambient 294 K, inflow d=1 T=700 K, the reference main's box, dt=0.001 (configs[3])",
+                  "variant": "7-variable-density", "grid": [args.size, args.size], "precision_form": args.precision,
+                  "l2": "flushed between timed steps (512 MiB write)", "scene_data": "seeded synthetic scene"}
+        args.no_cpu = True  # one oracle update of this scene takes minutes: no bounded CPU sample
     else:
         config = {"workload": f"solid-boundary scene {args.size}x{args.size}, 3 seeded bodies, "
                               f"dt=0.0025, config-0 inflow (configs[1])",

@@ -247,7 +247,7 @@ typedef struct {
 } ifl_inflow;
 
 typedef struct {
-    /* Shape of the batched PCG launch: threads per block (64, 128 or 256),
+    /* Shape of the batched PCG launch: threads per block (32, 64, 128 or 256),
      * strips per block, bulk-copy ring stages.  threads = 0: autotune at the
      * first update (each candidate shape runs a few pinned PCG iterations of
      * the real system; the fastest is kept). */

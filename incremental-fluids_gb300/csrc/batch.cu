@@ -45,8 +45,8 @@ int pow2ceil(int v) {
 template <typename F>
 std::vector<PcgShape> candidate_shapes() {
     if (sizeof(F) == 4)
-        return {{256, 4, 3}, {128, 2, 2}, {128, 1, 3}, {128, 1, 2}, {64, 2, 2}, {64, 1, 3}, {64, 1, 2}};
-    return {{256, 2, 3}, {128, 2, 2}, {128, 1, 3}, {128, 1, 2}, {64, 1, 3}, {64, 1, 2}};
+        return {{256, 4, 3}, {128, 2, 2}, {128, 1, 2}, {64, 2, 2}, {64, 1, 3}, {64, 1, 2}, {32, 1, 2}, {32, 1, 3}};
+    return {{256, 2, 3}, {128, 2, 2}, {128, 1, 2}, {64, 1, 3}, {64, 1, 2}, {32, 1, 2}, {32, 1, 3}};
 }
 
 template <typename F>
@@ -591,7 +591,8 @@ int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, 
                 return IFL_ERR_ARG;
             }
     }
-    if (opt.threads != 0 && opt.threads != 64 && opt.threads != 128 && opt.threads != 256) return IFL_ERR_ARG;
+    if (opt.threads != 0 && opt.threads != 32 && opt.threads != 64 && opt.threads != 128 && opt.threads != 256)
+        return IFL_ERR_ARG;
     std::vector<SolverBase *> m(members, members + n);
     int e;
     if (p0.precision == IFL_FP32) {

@@ -131,7 +131,7 @@ struct PcgConfig {
 
 // Launch shape of the batched PCG kernel (chosen by the batch autotuner).
 struct PcgShape {
-    int threads;  // 64, 128 or 256 threads per block
+    int threads;  // 32, 64, 128 or 256 threads per block
     int K;        // strips (sweeping warps) per block, <= threads / 32
     int stages;   // bulk-copy ring stages per sweeping warp, 2..4
 };

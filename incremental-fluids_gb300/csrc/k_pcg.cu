@@ -1090,6 +1090,7 @@ size_t al256(size_t v) { return (v + 255) / 256 * 256; }
 
 template <typename F>
 const void *batch_fn(int threads) {
+    if (threads == 32) return (const void *)pcg_batch_kernel<F, 32>;
     if (threads == 64) return (const void *)pcg_batch_kernel<F, 64>;
     return threads == 128 ? (const void *)pcg_batch_kernel<F, 128> : (const void *)pcg_batch_kernel<F, 256>;
 }
@@ -1103,7 +1104,7 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
         return nullptr;
     };
     if (n <= 0) return fail("empty batch");
-    if ((shape.threads != 64 && shape.threads != 128 && shape.threads != 256) || shape.K < 1 ||
+    if ((shape.threads != 32 && shape.threads != 64 && shape.threads != 128 && shape.threads != 256) || shape.K < 1 ||
         shape.K > shape.threads / 32 ||
         shape.stages < 2 || shape.stages > 4)
         return fail("unsupported batched PCG shape");

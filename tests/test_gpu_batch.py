@@ -204,7 +204,7 @@ def test_autotuner_tries_shapes_and_keeps_one(ifl):
     info = b.info()
     tried = [t for t in info["candidate_ms"] if t > 0]
     assert len(tried) >= 2
-    assert info["threads"] in (64, 128, 256) and 1 <= info["strips_per_block"] <= info["threads"] // 32
+    assert info["threads"] in (32, 64, 128, 256) and 1 <= info["strips_per_block"] <= info["threads"] // 32
     assert info["grid"] > 0 and info["steps"] == 2 and info["launches"] > 0
 
 
