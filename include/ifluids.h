@@ -165,6 +165,16 @@ double ifl_ambient_t(const ifl_solver *s);
 int ifl_field_shape(const ifl_solver *s, int field, int *w, int *h);
 int ifl_read_field(ifl_solver *s, int field, void *host, size_t bytes, int dtype);
 int ifl_write_field(ifl_solver *s, int field, const void *host, size_t bytes, int dtype);
+/* FluidSolver::toImage (3-conjugate-gradients/Fluid.cpp:455-465,
+ * 4-solid-boundaries/Fluid.cpp:903-916, 5-curved-boundaries/Fluid.cpp:961-972,
+ * 7-variable-density/Fluid.cpp:1047-1081): 8-bit RGBA, w x h pixels, pixel
+ * (x, y) at 4*(x + y*width); with heat != 0 in steps 6-7 the image is 2w wide
+ * (heat colours left, density shade right) as renderHeat in the reference.
+ * on_device = 0: `rgba` is host memory and the call synchronises; 1: `rgba`
+ * is device memory, written asynchronously on the handle's stream (a headless
+ * frame for GPU-side consumers).  The reference encodes PNGs with lodepng;
+ * the Python package writes them (ifluids.write_png). */
+int ifl_render(ifl_solver *s, int heat, void *rgba, size_t bytes, int on_device);
 /* FluidQuantity::flip for one quantity (tests). */
 int ifl_flip(ifl_solver *s, int quantity);
 

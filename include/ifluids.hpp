@@ -111,6 +111,13 @@ class FluidSolver {
         if (h) *h = fh;
         return out;
     }
+    // FluidSolver::toImage: rgba holds w*h*4 bytes (2*w*h*4 with renderHeat in steps 6-7).
+    void toImage(unsigned char *rgba, bool renderHeat = false) {
+        int w = 0, h = 0;
+        check(ifl_field_shape(h_, IFL_FIELD(IFL_Q_D, IFL_A_SRC), &w, &h), "field shape");
+        const bool wide = renderHeat && variant_ >= IFL_HEAT;
+        check(ifl_render(h_, renderHeat ? 1 : 0, rgba, (size_t)(wide ? 2 : 1) * w * h * 4, 0), "toImage");
+    }
     ifl_step_stats stats() {
         ifl_step_stats st;
         check(ifl_get_stats(h_, &st), "stats");
@@ -126,6 +133,7 @@ class FluidSolver {
         p.density_soot = rs;
         p.diffusion = diff;
         p.precision = precision;
+        variant_ = variant;
         check(ifl_create(&p, &h_), "create");
     }
     void check(int rc, const char *what) {
@@ -134,6 +142,7 @@ class FluidSolver {
                                      "): " + (h_ ? ifl_last_error(h_) : ""));
     }
     ifl_solver *h_ = nullptr;
+    int variant_ = IFL_PLAIN;
     const std::vector<const SolidBody *> *bodies_ = nullptr;
 };
 

@@ -182,6 +182,10 @@ int ifl_write_field(ifl_solver *s, int field, const void *host, size_t bytes, in
     return guarded(s, [&](ifl::SolverBase &v) { return v.write_field(field, host, bytes, dtype); });
 }
 
+int ifl_render(ifl_solver *s, int heat, void *rgba, size_t bytes, int on_device) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.render(heat, rgba, bytes, on_device != 0); });
+}
+
 int ifl_flip(ifl_solver *s, int quantity) {
     return guarded(s, [&](ifl::SolverBase &v) { return v.flip(quantity); });
 }

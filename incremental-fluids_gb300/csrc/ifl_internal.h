@@ -149,6 +149,8 @@ template <typename F> void launch_extrapolate(const Scene<F> &S, unsigned qmask,
 template <typename F> void launch_advect(const Scene<F> &S, double dt, cudaStream_t st);
 // strip-diagonal FP64 array -> row-major field (T = p after the heat solve)
 template <typename F> void launch_sd_to_rows(const Scene<F> &S, F *rows, const double *sd_arr, cudaStream_t st);
+// toImage: 8-bit RGBA of the density (and, heat != 0, the temperature) into a device buffer
+template <typename F> void launch_render(const Scene<F> &S, unsigned char *rgba, int heat, cudaStream_t st);
 template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
                                              cudaStream_t st, int *blocks_used);
 template <typename F> int pcg_max_blocks();

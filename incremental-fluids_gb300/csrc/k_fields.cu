@@ -622,6 +622,48 @@ __global__ void sd_to_rows_kernel(SDIdx sd, int P, F *rows, const double *sd_arr
     rows[x + (size_t)y * P] = (F)sd_arr[sd.slot(x, y)];
 }
 
+// ------------------------------------------------------------------ image
+// FluidSolver::toImage (3-conjugate-gradients/Fluid.cpp:455-465,
+// 4-solid-boundaries/Fluid.cpp:903-916, 5-curved-boundaries/Fluid.cpp:961-972,
+// 7-variable-density/Fluid.cpp:1047-1081): 8-bit RGBA, row y at y*width; with
+// heat (steps 6-7) the image is 2w wide, heat colours left, shade right.
+template <typename F>
+__global__ void render_kernel(Scene<F> S, unsigned char *rgba, int heat) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int w = S.w, h = S.h;
+    if (x >= w || y >= h) return;
+    const size_t c = x + (size_t)y * S.P;
+    const double d = (double)S.q[0].src[c];
+    if (S.variant <= 5) {
+        int shade = S.variant == 5 ? (int)((1.0 - d) * S.q[0].vol[c] * 255.0) : (int)((1.0 - d) * 255.0);
+        shade = shade < 255 ? shade : 255;  // max(min(shade, 255), 0)
+        shade = shade < 0 ? 0 : shade;
+        if (S.variant == 4 && S.q[0].cell[c] == CELL_SOLID) shade = 0;
+        const size_t o = 4 * (x + (size_t)y * w);
+        rgba[o] = rgba[o + 1] = rgba[o + 2] = (unsigned char)shade;
+        rgba[o + 3] = 0xFF;
+        return;
+    }
+    const double volume = S.q[0].vol[c];
+    double shade = (1.0 - d) * volume;
+    shade = smin(smax(shade, 0.0), 1.0);
+    const size_t oright = heat ? 4 * (x + (size_t)y * w * 2 + w) : 4 * (x + (size_t)y * w);
+    rgba[oright] = rgba[oright + 1] = rgba[oright + 2] = (unsigned char)(int)(shade * 255.0);
+    rgba[oright + 3] = 0xFF;
+    if (heat) {
+        double t = ((double)S.q[1].src[c] - S.t_amb) / 700.0;
+        t = smin(smax(t, 0.0), 1.0);
+        const double r = 1.0 + volume * (smin(t * 4.0, 1.0) - 1.0);
+        const double g = 1.0 + volume * (smin(t * 2.0, 1.0) - 1.0);
+        const double b = 1.0 + volume * (smax(smin(t * 4.0 - 3.0, 1.0), 0.0) - 1.0);
+        const size_t ol = 4 * (x + (size_t)y * w * 2);
+        rgba[ol] = (unsigned char)(int)(r * 255.0);
+        rgba[ol + 1] = (unsigned char)(int)(g * 255.0);
+        rgba[ol + 2] = (unsigned char)(int)(b * 255.0);
+        rgba[ol + 3] = 0xFF;
+    }
+}
+
 inline dim3 grid2(int nx, int ny, int nz, dim3 b) {
     return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y, nz);
 }
@@ -686,6 +728,12 @@ template <typename F>
 void launch_advect(const Scene<F> &S, double dt, cudaStream_t st) {
     dim3 b(32, 8);
     advect_kernel<F><<<grid2(S.w + 1, S.h + 1, 3, b), b, 0, st>>>(S, dt);
+}
+
+template <typename F>
+void launch_render(const Scene<F> &S, unsigned char *rgba, int heat, cudaStream_t st) {
+    dim3 b(32, 8);
+    render_kernel<F><<<grid2(S.w, S.h, 1, b), b, 0, st>>>(S, rgba, heat);
 }
 
 template <typename F>
@@ -874,7 +922,8 @@ IFL_BATCH_INST(float)
     template void launch_apply_pressure<F>(const Scene<F> &, double, cudaStream_t);                         \
     template void launch_extrapolate<F>(const Scene<F> &, unsigned, cudaStream_t);                          \
     template void launch_advect<F>(const Scene<F> &, double, cudaStream_t);                                 \
-    template void launch_sd_to_rows<F>(const Scene<F> &, F *, const double *, cudaStream_t);
+    template void launch_sd_to_rows<F>(const Scene<F> &, F *, const double *, cudaStream_t);                 \
+    template void launch_render<F>(const Scene<F> &, unsigned char *, int, cudaStream_t);
 IFL_INST(double)
 IFL_INST(float)
 

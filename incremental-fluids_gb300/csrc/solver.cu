@@ -279,6 +279,31 @@ class SolverImpl final : public SolverBase {
 
     size_t pitch() const override { return (size_t)P_; }
     size_t device_bytes() const override { return arena_bytes_; }
+    int render(int heat, void *rgba, size_t bytes, bool on_device) override {
+        const bool wide = heat && prm_.variant >= IFL_HEAT;
+        const size_t need = (size_t)(wide ? 2 : 1) * prm_.w * prm_.h * 4;
+        if (!rgba || bytes < need) return IFL_ERR_ARG;
+        unsigned char *dst = (unsigned char *)rgba;
+        if (!on_device) {
+            if (image_bytes_ < need) {
+                if (image_) cudaFree(image_);
+                image_ = nullptr;
+                image_bytes_ = 0;
+                if (check(cudaMalloc(&image_, need), "image buffer")) return IFL_ERR_NOMEM;
+                image_bytes_ = need;
+            }
+            dst = image_;
+        }
+        launch_render<F>(S_, dst, wide ? 1 : 0, stream_);
+        launches_++;
+        if (int e = launch_check("render")) return e;
+        if (!on_device &&
+            (check(cudaMemcpyAsync(rgba, image_, need, cudaMemcpyDeviceToHost, stream_), "image readback") ||
+             check(cudaStreamSynchronize(stream_), "image sync")))
+            return IFL_ERR_CUDA;
+        return IFL_OK;
+    }
+
     void *scene_ptr() override { return &S_; }
     void *scratch_ptr() override { return &scratch_; }
     bool has_quantity(int q) const override { return q >= 0 && q < 4 && present(q); }
@@ -436,6 +461,8 @@ class SolverImpl final : public SolverBase {
         staging_done_ = nullptr;
         if (arena_) cudaFree(arena_);
         arena_ = nullptr;
+        if (image_) cudaFree(image_);
+        image_ = nullptr;
         if (own_stream_ && stream_) cudaStreamDestroy(stream_);
         stream_ = nullptr;
     }
@@ -447,6 +474,8 @@ class SolverImpl final : public SolverBase {
     cudaEvent_t staging_done_ = nullptr;
     void *arena_ = nullptr;
     size_t arena_bytes_ = 0;
+    unsigned char *image_ = nullptr;  // device staging of toImage for host readback
+    size_t image_bytes_ = 0;
     int P_ = 0, rows_ = 0, nq_ = 3, max_blocks_ = 1;
 };
 

@@ -25,6 +25,8 @@ class SolverBase {
     virtual int read_pcg(ifl_step_stats *st) = 0;
     virtual size_t pitch() const = 0;
     virtual size_t device_bytes() const = 0;
+    // toImage into a host buffer (synchronising) or a device buffer (async).
+    virtual int render(int heat, void *rgba, size_t bytes, bool on_device) = 0;
 
     // Access for the batch (batch.cu): Scene<F>* and PcgScratch* of this
     // handle, F as its precision.

@@ -35,7 +35,7 @@ PCG_CONVERGED, PCG_INITIAL, PCG_CAP = 0, 1, 2
 
 EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", "ifl_get_bodies",
            "ifl_advance_bodies", "ifl_add_inflow", "ifl_update", "ifl_run_phase", "ifl_ambient_t",
-           "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_flip", "ifl_get_stats",
+           "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_render", "ifl_flip", "ifl_get_stats",
            "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
            "ifl_set_timing", "ifl_get_timing", "ifl_pcg_solve_noalloc",
            "ifl_batch_default_options", "ifl_batch_create", "ifl_batch_destroy", "ifl_batch_set_inflows",
@@ -160,6 +160,7 @@ def load_library(path: str = LIB_PATH):
     L.ifl_read_field.argtypes = [vp, i, vp, sz, i]
     L.ifl_write_field.argtypes = [vp, i, vp, sz, i]
     L.ifl_flip.argtypes = [vp, i]
+    L.ifl_render.argtypes = [vp, i, vp, sz, i]
     L.ifl_get_stats.argtypes = [vp, C.POINTER(StepStats)]
     L.ifl_set_pinned_iterations.argtypes = [vp, i, i]
     L.ifl_synchronize.argtypes = [vp]
@@ -403,6 +404,17 @@ class FluidSolver:
         code = {np.dtype(np.float64): DT_F64, np.dtype(np.float32): DT_F32, np.dtype(np.uint8): DT_U8}[
             arr.dtype]
         self._check(self._L.ifl_write_field(self._h, fid, arr.ctypes.data, arr.nbytes, code), "write_field")
+
+    def to_image(self, heat: bool = False) -> np.ndarray:
+        """FluidSolver::toImage as an (h, w', 4) uint8 array (w' = 2w with heat in steps 6-7)."""
+        wide = 2 if (heat and self.variant >= HEAT) else 1
+        out = np.empty((self.h, wide * self.w, 4), dtype=np.uint8)
+        self._check(self._L.ifl_render(self._h, 1 if heat else 0, out.ctypes.data, out.nbytes, 0), "to_image")
+        return out
+
+    def render_device(self, heat: bool, dev_ptr: int, nbytes: int):
+        """toImage into device memory (asynchronous on the solver's stream)."""
+        self._check(self._L.ifl_render(self._h, 1 if heat else 0, dev_ptr, nbytes, 1), "render_device")
 
     def flip(self, quantity: int):
         self._check(self._L.ifl_flip(self._h, quantity), "flip")
@@ -657,3 +669,21 @@ class Server:
         o = ServerInfo()
         self._check(self._L.ifl_server_get_info(self._h, C.byref(o)), "info")
         return {k: getattr(o, k) for k, _ in ServerInfo._fields_ if k != "pad_"}
+
+
+def write_png(path: str, rgba: np.ndarray):
+    """Write an (h, w, 4) uint8 RGBA image as a PNG file (8-bit RGBA, no filtering),
+    rows in array order as lodepng_encode32_file writes the reference's frames."""
+    import struct
+    import zlib
+    img = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w, _ = img.shape
+    raw = b"".join(b"\x00" + img[y].tobytes() for y in range(h))
+
+    def chunk(kind: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n")
+        f.write(chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)))
+        f.write(chunk(b"IDAT", zlib.compress(raw, 6)))
+        f.write(chunk(b"IEND", b""))

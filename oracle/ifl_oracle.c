@@ -1006,6 +1006,47 @@ void ifo_flip(ifo_solver *s, int quantity_id) {
     if (quantity_id >= 0 && quantity_id < 4 && s->q[quantity_id].present) flip(&s->q[quantity_id]);
 }
 
+/* toImage of each step (references in the header). */
+void ifo_to_image(const ifo_solver *s, unsigned char *rgba, int heat) {
+    const int w = s->w, h = s->h;
+    const quantity *d = &s->q[0];
+    if (s->variant <= 5) {
+        for (int i = 0; i < w * h; i++) {
+            int shade;
+            if (s->variant == 5) shade = (int)((1.0 - d->src[i]) * d->volume[i] * 255.0);
+            else shade = (int)((1.0 - d->src[i]) * 255.0);
+            shade = shade < 255 ? shade : 255;  /* max(min(shade, 255), 0) */
+            shade = shade < 0 ? 0 : shade;
+            if (s->variant == 4 && d->cell[i] == CELL_SOLID) shade = 0;
+            rgba[i * 4 + 0] = rgba[i * 4 + 1] = rgba[i * 4 + 2] = (unsigned char)shade;
+            rgba[i * 4 + 3] = 0xFF;
+        }
+        return;
+    }
+    const quantity *t = &s->q[1];
+    for (int y = 0; y < h; y++) {
+        for (int x = 0; x < w; x++) {
+            const int idxl = 4 * (x + y * w * 2), idxr = heat ? 4 * (x + y * w * 2 + w) : 4 * (x + y * w);
+            const double volume = d->volume[x + y * w];
+            double shade = (1.0 - d->src[x + y * w]) * volume;
+            shade = smin(smax(shade, 0.0), 1.0);
+            rgba[idxr + 0] = rgba[idxr + 1] = rgba[idxr + 2] = (unsigned char)(int)(shade * 255.0);
+            rgba[idxr + 3] = 0xFF;
+            if (heat) {
+                double tt = (t->src[x + y * w] - s->t_amb) / 700.0;
+                tt = smin(smax(tt, 0.0), 1.0);
+                const double r = 1.0 + volume * (smin(tt * 4.0, 1.0) - 1.0);
+                const double g = 1.0 + volume * (smin(tt * 2.0, 1.0) - 1.0);
+                const double b = 1.0 + volume * (smax(smin(tt * 4.0 - 3.0, 1.0), 0.0) - 1.0);
+                rgba[idxl + 0] = (unsigned char)(int)(r * 255.0);
+                rgba[idxl + 1] = (unsigned char)(int)(g * 255.0);
+                rgba[idxl + 2] = (unsigned char)(int)(b * 255.0);
+                rgba[idxl + 3] = 0xFF;
+            }
+        }
+    }
+}
+
 /* Scalar kernels exported for the known-answer tests. */
 double ifo_occupancy(double d11, double d12, double d21, double d22) { return occupancy(d11, d12, d21, d22); }
 double ifo_cerp(double a, double b, double c, double d, double x) { return cerp1(a, b, c, d, x); }

@@ -103,6 +103,12 @@ uint8_t *ifo_bytes(ifo_solver *s, int quantity, int which, int *w, int *h);
 /* Swap src/dst of one quantity (FluidQuantity::flip). */
 void ifo_flip(ifo_solver *s, int quantity);
 
+/* FluidSolver::toImage: 8-bit RGBA, w x h (heat and step >= 6: 2w x h, heat
+ * colours left, shade right); 3-conjugate-gradients/Fluid.cpp:455-465,
+ * 4-solid-boundaries/Fluid.cpp:903-916, 5-curved-boundaries/Fluid.cpp:961-972,
+ * 7-variable-density/Fluid.cpp:1047-1081. */
+void ifo_to_image(const ifo_solver *s, unsigned char *rgba, int heat);
+
 /* Scalar kernels for known-answer tests: occupancy() of
  * 7-variable-density/Fluid.cpp:68-102 and the clamped Catmull-Rom of
  * 3-conjugate-gradients/Fluid.cpp:55-69. */

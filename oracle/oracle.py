@@ -85,6 +85,8 @@ def _oracle_lib():
         L.ifo_occupancy.restype = d
         L.ifo_cerp.argtypes = [d, d, d, d, d]
         L.ifo_cerp.restype = d
+        L.ifo_to_image.argtypes = [vp, C.c_void_p, i]
+        L.ifo_to_image.restype = None
         _lib = L
     return _lib
 
@@ -165,6 +167,16 @@ class OracleSolver:
         return _view(self.L.ifo_bytes(self.p, q, which, C.byref(w), C.byref(h)),
                      w.value, h.value, np.uint8)
 
+    def to_image(self, heat: bool = False) -> np.ndarray:
+        """FluidSolver::toImage as an (h, w', 4) uint8 array (w' = 2w with heat, steps 6-7)."""
+        wide = 2 if (heat and self.variant >= HEAT) else 1
+        out = np.zeros((self.h, wide * self.w, 4), dtype=np.uint8)
+        self._to_image(out.ctypes.data, 1 if heat else 0)
+        return out
+
+    def _to_image(self, ptr, heat):
+        self.L.ifo_to_image(self.p, ptr, heat)
+
 
 def occupancy(d11, d12, d21, d22) -> float:
     return _oracle_lib().ifo_occupancy(d11, d12, d21, d22)
@@ -198,6 +210,8 @@ def _ref_lib(step):
         L.ref_array.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
         L.ref_bytes.restype = C.POINTER(C.c_uint8)
         L.ref_bytes.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
+        L.ref_to_image.argtypes = [vp, C.c_void_p, i]
+        L.ref_to_image.restype = None
         _ref_libs[step] = L
     return _ref_libs[step]
 
@@ -268,3 +282,13 @@ class RefSolver:
         w, h = C.c_int(), C.c_int()
         return _view(self.L.ref_bytes(self.p, q, which, C.byref(w), C.byref(h)),
                      w.value, h.value, np.uint8)
+
+    def to_image(self, heat: bool = False) -> np.ndarray:
+        """FluidSolver::toImage as an (h, w', 4) uint8 array (w' = 2w with heat, steps 6-7)."""
+        wide = 2 if (heat and self.variant >= HEAT) else 1
+        out = np.zeros((self.h, wide * self.w, 4), dtype=np.uint8)
+        self._to_image(out.ctypes.data, 1 if heat else 0)
+        return out
+
+    def _to_image(self, ptr, heat):
+        self.L.ref_to_image(self.p, ptr, heat)

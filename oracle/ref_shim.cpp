@@ -280,4 +280,13 @@ uint8_t *ref_bytes(void *p, int qid, int which, int *w, int *h) {
 #endif
 }
 
+void ref_to_image(void *p, unsigned char *rgba, int heat) {
+#if REF_STEP >= 6
+    ((RefScene *)p)->solver->toImage(rgba, heat != 0);
+#else
+    (void)heat;
+    ((RefScene *)p)->solver->toImage(rgba);
+#endif
+}
+
 }  // extern "C"

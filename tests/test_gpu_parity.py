@@ -245,6 +245,18 @@ def test_fp32_form_error_vs_fp64_oracle(ifl, case):
     assert errs["p"] < 1e-4 and errs["velocity"] < 1e-4, errs
 
 
+@pytest.mark.parametrize("case", CASES, ids=IDS)
+def test_to_image_bit_exact_fp64(ifl, case):
+    """toImage from the oracle's state: identical RGBA bytes (with and without
+    the heat panel in steps 6-7)."""
+    variant, w, h, warm, inflow, bodies = case
+    o = warm_oracle(variant, w, h, warm + 1, inflow, bodies)
+    g = make_gpu(ifl, variant, w, h, o.bodies())
+    upload(ifl, g, o, variant)
+    for heat in ((False, True) if variant >= 6 else (False,)):
+        assert np.array_equal(g.to_image(heat), o.to_image(heat)), heat
+
+
 def test_deterministic_and_stream_ordered(ifl):
     """Two identical runs give bit-identical fields (fixed-order reductions)."""
     outs = []

@@ -96,6 +96,8 @@ def test_oracle_matches_reference_every_step(case):
         if variant == O.VARDENS:
             assert np.array_equal(a.array(0, O.A_UDENS), b.array(0, O.A_UDENS))
             assert np.array_equal(a.array(0, O.A_VDENS), b.array(0, O.A_VDENS))
+        for heat in ((False, True) if variant >= O.HEAT else (False,)):
+            assert np.array_equal(a.to_image(heat), b.to_image(heat)), (step, heat)
 
 
 def test_config0_as_stated_injects_nothing():
