@@ -52,7 +52,9 @@ enum {
     IFL_SOLID = 4,    /* 4-solid-boundaries: binary solid cells               */
     IFL_CURVED = 5,   /* 5-curved-boundaries: fractional cell volumes         */
     IFL_HEAT = 6,     /* 6-heat: + temperature, heat diffusion, buoyancy       */
-    IFL_VARDENS = 7   /* 7-variable-density: + per-face density               */
+    IFL_VARDENS = 7,  /* 7-variable-density: + per-face density               */
+    IFL_FLIP = 8      /* 8-flip: step 7's grid solve; FLIP particles carry d,
+                         T, u, v instead of semi-Lagrangian advection (FP64) */
 };
 
 /* Storage / arithmetic form. */
@@ -76,7 +78,7 @@ enum {
     IFL_A_VOLUME = 3,   /* fluid volume fraction                                 */
     IFL_A_NORMALX = 4,
     IFL_A_NORMALY = 5,
-    IFL_A_CELL = 8,     /* u8: 0 fluid, 1 solid                                  */
+    IFL_A_CELL = 8,     /* u8: 0 fluid, 1 solid, 2 empty (step 8, transient)    */
     IFL_A_BODY = 9      /* u8: index of the nearest body                         */
 };
 #define IFL_FIELD(q, a) (((q) << 8) | (a))
@@ -93,14 +95,22 @@ enum {
     IFL_PH_FILL_SOLID = 0, IFL_PH_HEAT = 1, IFL_PH_EXTRAP_T = 2, IFL_PH_BUOYANCY = 3,
     IFL_PH_BC = 4, IFL_PH_RHS = 5, IFL_PH_DENSITIES = 6, IFL_PH_MATRIX = 7,
     IFL_PH_PRECON = 8, IFL_PH_PROJECT = 9, IFL_PH_APPLY_P = 10,
-    IFL_PH_EXTRAP_DUV = 11, IFL_PH_ADVECT = 12
+    IFL_PH_EXTRAP_DUV = 11, IFL_PH_ADVECT = 12,
+    /* step 8 (FLIP) only */
+    IFL_PH_P2G = 13,        /* particlesToGrid: transfer, extrapolation, count,
+                               prune, seed (places the initial particles first
+                               when that has not happened)                      */
+    IFL_PH_FLIP_COPY = 14,  /* copy() of every quantity, then the inflows added
+                               since the last update                            */
+    IFL_PH_G2P = 15,        /* diff, gridToParticles(alpha), undiff             */
+    IFL_PH_PADVECT = 16     /* ParticleQuantities::advect                      */
 };
 
 /* PCG outcome. */
 enum { IFL_PCG_CONVERGED = 0, IFL_PCG_INITIAL = 1, IFL_PCG_CAP = 2 };
 
 typedef struct {
-    int32_t variant;           /* IFL_PLAIN .. IFL_VARDENS                       */
+    int32_t variant;           /* IFL_PLAIN .. IFL_FLIP                          */
     int32_t w, h;              /* pressure grid size (>= 2 each)                 */
     int32_t precision;         /* IFL_FP64 or IFL_FP32                           */
     double density_air;        /* `density` of steps 3-5, rhoAir of 6-7 (0.1)    */
@@ -131,7 +141,11 @@ typedef struct {
     ifl_pcg_stats pressure;
     ifl_pcg_stats heat;
     uint32_t device_flags;  /* bit 0: bounded wait timed out; bit 1: solid cell on
-                               the outer ring (outside the parity envelope) */
+                               the outer ring (outside the parity envelope);
+                               bit 2 (step 8): seeding tested a particle number
+                               beyond the live count (fewer particles than
+                               cells); bit 3: empty-cell extrapolation exceeded
+                               its work bound */
     uint32_t steps;         /* update() calls completed                         */
 } ifl_step_stats;
 
@@ -142,7 +156,7 @@ void ifl_default_params(ifl_params *p, int variant, int w, int h);
 int ifl_create(const ifl_params *p, ifl_solver **out);
 int ifl_destroy(ifl_solver *s);
 
-/* Bodies (steps 4-7).  The reference keeps references to caller-owned bodies
+/* Bodies (steps 4-8).  The reference keeps references to caller-owned bodies
  * and the caller moves them between steps (SolidBody::update); here the caller
  * passes the current body table before update() (it is copied), or lets the
  * handle advance its own copy with ifl_advance_bodies. */
@@ -150,7 +164,10 @@ int ifl_set_bodies(ifl_solver *s, const ifl_body *bodies, int n);
 int ifl_get_bodies(ifl_solver *s, ifl_body *bodies, int capacity, int *n);
 int ifl_advance_bodies(ifl_solver *s, double dt);
 
-/* FluidSolver::addInflow; `t` is ignored below step 6. */
+/* FluidSolver::addInflow; `t` is ignored below step 6.  Step 8 adds its
+ * inflow inside update(), between copy() and the heat solve
+ * (8-flip/Fluid.cpp:1365-1368): there the rectangles added before update()
+ * are applied at that point of the next update. */
 int ifl_add_inflow(ifl_solver *s, double x, double y, double w, double h,
                    double d, double t, double u, double v);
 /* FluidSolver::update; asynchronous on the handle's stream. */
@@ -167,8 +184,8 @@ int ifl_read_field(ifl_solver *s, int field, void *host, size_t bytes, int dtype
 int ifl_write_field(ifl_solver *s, int field, const void *host, size_t bytes, int dtype);
 /* FluidSolver::toImage (3-conjugate-gradients/Fluid.cpp:455-465,
  * 4-solid-boundaries/Fluid.cpp:903-916, 5-curved-boundaries/Fluid.cpp:961-972,
- * 7-variable-density/Fluid.cpp:1047-1081): 8-bit RGBA, w x h pixels, pixel
- * (x, y) at 4*(x + y*width); with heat != 0 in steps 6-7 the image is 2w wide
+ * 7-variable-density/Fluid.cpp:1047-1081, 8-flip/Fluid.cpp:1426-1470): 8-bit RGBA, w x h pixels, pixel
+ * (x, y) at 4*(x + y*width); with heat != 0 in steps 6-8 the image is 2w wide
  * (heat colours left, density shade right) as renderHeat in the reference.
  * on_device = 0: `rgba` is host memory and the call synchronises; 1: `rgba`
  * is device memory, written asynchronously on the handle's stream (a headless
@@ -177,6 +194,23 @@ int ifl_write_field(ifl_solver *s, int field, const void *host, size_t bytes, in
 int ifl_render(ifl_solver *s, int heat, void *rgba, size_t bytes, int on_device);
 /* FluidQuantity::flip for one quantity (tests). */
 int ifl_flip(ifl_solver *s, int quantity);
+
+/* Step 8 (FLIP) particles: ParticleQuantities::_posX, _posY and the carried
+ * d, T, u, v (8-flip/Fluid.cpp:692-722), FP64, capacity 12 per cell.  The
+ * initial particles (initParticles + gridToParticles(1.0) of the
+ * constructor, 8-flip/Fluid.cpp:733-750, 1307-1314) are placed by the first
+ * update, against the bodies set by then, or by ifl_flip_init.  Reads and
+ * writes synchronise.  Writing a count replaces the initial placement. */
+enum { IFL_P_X = 0, IFL_P_Y = 1, IFL_P_D = 2, IFL_P_T = 3, IFL_P_U = 4, IFL_P_V = 5 };
+int ifl_flip_init(ifl_solver *s);
+int ifl_particle_count(ifl_solver *s, int *n);
+int ifl_read_particles(ifl_solver *s, int which, double *out, int capacity, int *n);
+int ifl_write_particles(ifl_solver *s, int which, const double *in, int n);
+int ifl_set_particle_count(ifl_solver *s, int n);
+/* frand() state (8-flip/Fluid.cpp:38-46), one stream per handle starting at
+ * 0xBA5EBA11 as the reference's static seed. */
+int ifl_get_rng_state(ifl_solver *s, uint32_t *state);
+int ifl_set_rng_state(ifl_solver *s, uint32_t state);
 
 /* PCG outcome of the last update (synchronises). */
 int ifl_get_stats(ifl_solver *s, ifl_step_stats *out);
@@ -195,7 +229,8 @@ enum {
     IFL_K_SOLID = 3,       /* distance field, cells, normals, volumes         */
     IFL_K_EXTRAPOLATE = 4, /* solid-cell extrapolation                        */
     IFL_K_FACES = 5,       /* inflow, boundary conditions, buoyancy, pressure update */
-    IFL_K_GROUPS = 6
+    IFL_K_PARTICLES = 6,   /* step 8: particle transfers, seeding, advection  */
+    IFL_K_GROUPS = 7
 };
 typedef struct {
     double ms[IFL_K_GROUPS];           /* device time per group               */

@@ -413,7 +413,7 @@ class BatchImpl final : public BatchBase {
             launch_batch_extrapolate<F>(B_, 1u << 1, st_);
             launch_batch_buoyancy<F>(B_, dt, st_);
             launch_batch_bc<F>(B_, st_);
-            launch_batch_assemble<F>(B_, dt, ASM_RHS | ASM_MATRIX | (variant_ == IFL_VARDENS ? ASM_DENS : 0),
+            launch_batch_assemble<F>(B_, dt, ASM_RHS | ASM_MATRIX | (variant_ >= IFL_VARDENS ? ASM_DENS : 0),
                                      st_);
             launches_ += 1 + 3 + 1 + 1 + 1;
         }
@@ -581,6 +581,10 @@ int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, 
     for (int i = 0; i < n; i++) {
         if (!members[i]) return IFL_ERR_ARG;
         const ifl_params &p = members[i]->params();
+        if (p.variant == IFL_FLIP) {
+            if (err) *err = "step 8 (FLIP) handles are stepped one by one, not in batches";
+            return IFL_ERR_UNSUPPORTED;
+        }
         if (p.variant != p0.variant || p.precision != p0.precision || p.device != p0.device) {
             if (err) *err = "batch members differ in variant, precision or device";
             return IFL_ERR_ARG;

@@ -101,9 +101,11 @@ void ifl_default_params(ifl_params *p, int variant, int w, int h) {
 int ifl_create(const ifl_params *p, ifl_solver **out) {
     if (!p || !out) return IFL_ERR_ARG;
     *out = nullptr;
-    if (p->variant < IFL_PLAIN || p->variant > IFL_VARDENS) return IFL_ERR_ARG;
+    if (p->variant < IFL_PLAIN || p->variant > IFL_FLIP) return IFL_ERR_ARG;
     if (p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768) return IFL_ERR_ARG;
     if (p->precision != IFL_FP64 && p->precision != IFL_FP32) return IFL_ERR_ARG;
+    if (p->variant == IFL_FLIP && p->precision != IFL_FP64) return IFL_ERR_UNSUPPORTED;  // particles are FP64
+    if (p->variant == IFL_FLIP && (int64_t)p->w * p->h * 12 > 0x7fffffff) return IFL_ERR_UNSUPPORTED;
     if (p->device < 0) return IFL_ERR_ARG;
     if (p->max_iter_pressure < 0 || p->max_iter_heat < 0) return IFL_ERR_ARG;
     if (!(p->density_air > 0.0)) return IFL_ERR_ARG;
@@ -188,6 +190,35 @@ int ifl_render(ifl_solver *s, int heat, void *rgba, size_t bytes, int on_device)
 
 int ifl_flip(ifl_solver *s, int quantity) {
     return guarded(s, [&](ifl::SolverBase &v) { return v.flip(quantity); });
+}
+
+int ifl_flip_init(ifl_solver *s) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.flip_init(); });
+}
+
+int ifl_particle_count(ifl_solver *s, int *n) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.particle_count(n); });
+}
+
+int ifl_read_particles(ifl_solver *s, int which, double *out, int capacity, int *n) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.read_particles(which, out, capacity, n); });
+}
+
+int ifl_write_particles(ifl_solver *s, int which, const double *in, int n) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.write_particles(which, in, n); });
+}
+
+int ifl_set_particle_count(ifl_solver *s, int n) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.set_particle_count(n); });
+}
+
+int ifl_get_rng_state(ifl_solver *s, uint32_t *state) {
+    if (!state) return IFL_ERR_ARG;
+    return guarded(s, [&](ifl::SolverBase &v) { return v.rng_state(state, nullptr); });
+}
+
+int ifl_set_rng_state(ifl_solver *s, uint32_t state) {
+    return guarded(s, [&](ifl::SolverBase &v) { return v.rng_state(nullptr, &state); });
 }
 
 int ifl_get_stats(ifl_solver *s, ifl_step_stats *out) {
@@ -322,7 +353,7 @@ const char *ifl_server_last_error(const ifl_server *s) {
 
 int64_t ifl_device_bytes(const ifl_params *p) {
     if (!p || p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768 || p->variant < IFL_PLAIN ||
-        p->variant > IFL_VARDENS || (p->precision != IFL_FP64 && p->precision != IFL_FP32))
+        p->variant > IFL_FLIP || (p->precision != IFL_FP64 && p->precision != IFL_FP32))
         return IFL_ERR_ARG;
     int sms = 152, dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -148,6 +148,22 @@ __device__ __forceinline__ double cubic_pulse(double x) {
     return 1.0 - x * x * (3.0 - 2.0 * x);
 }
 
+template <typename F> __device__ __forceinline__ F lerp1(F a, F b, F x) { return a * (F(1.0) - x) + b * x; }
+
+// FluidQuantity::lerp (3-conjugate-gradients/Fluid.cpp:121-133) on a pitched grid.
+template <typename F>
+__device__ __forceinline__ F q_lerp(const F *__restrict__ src, int P, int w, int h, F ox, F oy, F x, F y) {
+    x = smin(smax(x - ox, F(0.0)), F(w) - F(1.001));
+    y = smin(smax(y - oy, F(0.0)), F(h) - F(1.001));
+    int ix = (int)x, iy = (int)y;
+    x -= F(ix);
+    y -= F(iy);
+    const F *r0 = src + ix + (size_t)iy * P;
+    F x00 = __ldg(r0), x10 = __ldg(r0 + 1);
+    F x01 = __ldg(r0 + P), x11 = __ldg(r0 + P + 1);
+    return lerp1(lerp1(x00, x10, x), lerp1(x01, x11, x), y);
+}
+
 // Bounded spin: the status word records a timeout and the caller proceeds
 // (the result is then garbage, but nothing hangs and the host sees the flag).
 constexpr long long kSpinLimit = 1ll << 26;

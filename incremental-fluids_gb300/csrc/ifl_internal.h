@@ -26,7 +26,7 @@
 
 namespace ifl {
 
-enum : uint8_t { CELL_FLUID = 0, CELL_SOLID = 1 };
+enum : uint8_t { CELL_FLUID = 0, CELL_SOLID = 1, CELL_EMPTY = 2 };
 
 // Neighbour bits consumed by the PCG kernel (one byte per cell).
 enum : uint8_t {
@@ -208,10 +208,58 @@ template <typename F> void launch_batch_apply_pressure(const SceneBatch<F> &B, d
 template <typename F> void launch_batch_extrapolate(const SceneBatch<F> &B, unsigned qmask, cudaStream_t st);
 template <typename F> void launch_batch_advect(const SceneBatch<F> &B, double dt, cudaStream_t st);
 
+// ------------------------------------------------------------ step 8: FLIP
+// Particle state (FP64 structure of arrays, capacity 12 particles per cell,
+// the reference's _maxParticles) and the work tables of its transfers.
+// The particle-to-grid transfer runs on three grids: kind 0 = w x h (density
+// and temperature share positions and weights), 1 = (w+1) x h (u), 2 =
+// w x (h+1) (v); their nodes are numbered densely, kind after kind.
+enum FlipCtl {
+    FC_COUNT = 0,   // live particles
+    FC_RNG = 1,     // frand() LCG state (bits of a uint32)
+    FC_EMPTY = 2,   // 2..5: CELL_EMPTY cells of quantity d, T, u, v after the transfer
+    FC_EXEC = 6,    // seeding attempts executed when the particle cap was reached
+    FC_N0 = 7,      // particles before seeding
+    FC_WORDS = 16
+};
+struct FlipState {
+    double *px, *py;
+    double *prop[4];                    // d, T, u, v carried by the particles
+    int cap;                            // 12 * w * h
+    int node_off[4];                    // first node of each kind, node_off[3] = total
+    unsigned long long *bcount;         // per node: particles whose base cell is the node
+    unsigned long long *bstart;         // exclusive scan of bcount (node_off[3] + 1)
+    int *brank;                         // 3 x cap: rank of a particle inside its bucket
+    int *blist;                         // 3 x cap: particle indices bucket by bucket
+    int *cell_count;                    // w * h particles per cell (countParticles)
+    unsigned long long *seedv, *seedx;  // w * h (+1): attempts | accepted << 32, and its scan
+    unsigned long long *scan_tmp;       // tile sums of the scans
+    int *cand;                          // prune candidates (cap)
+    int *ctl;                           // FlipCtl words
+};
+// Tile sums a scan of n values needs.
+inline size_t flip_scan_tiles(size_t n) { return (n + 1023) / 1024 + 2; }
+
+// Launchers (FP64 scenes; stream-ordered, no host synchronisation).
+void launch_flip_init(const Scene<double> &S, const FlipState &X, cudaStream_t st);
+void launch_flip_p2g(const Scene<double> &S, const FlipState &X, cudaStream_t st);
+void launch_flip_copy(const Scene<double> &S, cudaStream_t st);
+void launch_flip_g2p(const Scene<double> &S, const FlipState &X, cudaStream_t st);
+void launch_flip_advect(const Scene<double> &S, const FlipState &X, double dt, cudaStream_t st);
+// Extrapolation of the transfer (k_fields.cu): the parallel DAG relaxation
+// for quantities without CELL_EMPTY cells, the order-exact LIFO walk for the
+// others (skip[q] selects per quantity, read on the device).
+void launch_extrapolate_guarded(const Scene<double> &S, unsigned qmask, const int *empty_counts, cudaStream_t st);
+
 // what-bits for launch_assemble
 enum { ASM_RHS = 1, ASM_MATRIX = 2, ASM_DENS = 4 };
 
 // Device flag bits (Scene::flags[0]).
-enum : unsigned { FLAG_TIMEOUT = 1u, FLAG_RING_SOLID = 2u };
+enum : unsigned {
+    FLAG_TIMEOUT = 1u,
+    FLAG_RING_SOLID = 2u,
+    FLAG_FLIP_SEED = 4u,   // seeding tested a particle number beyond the live count
+    FLAG_FLIP_STACK = 8u   // the empty-cell extrapolation ran out of its work bound
+};
 
 }  // namespace ifl

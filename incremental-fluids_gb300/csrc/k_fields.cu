@@ -208,7 +208,7 @@ template <typename F>
 __device__ __forceinline__ double xface_factor(const Scene<F> &S, double scale, double alpha, int x, int y) {
     if (S.variant <= 4) return scale;
     double vol = S.q[2].vol[x + (size_t)y * S.P];
-    if (S.variant == 7) return scale * vol / udens_at(S, alpha, x, y);
+    if (S.variant >= 7) return scale * vol / udens_at(S, alpha, x, y);
     return scale * vol;
 }
 // y-face between (x, y-1) and (x, y).  Step 7 reads the face density at the
@@ -219,7 +219,7 @@ __device__ __forceinline__ double yface_factor(const Scene<F> &S, double scale, 
                                                bool *present) {
     if (S.variant <= 4) return scale;
     double vol = S.q[3].vol[x + (size_t)y * S.P];
-    if (S.variant == 7) {
+    if (S.variant >= 7) {
         long flat = (long)x + (long)y * (S.w + 1);
         if (flat >= (long)S.w * (S.h + 1)) {
             *present = false;
@@ -288,7 +288,7 @@ __device__ __forceinline__ void assemble_body(const Scene<F> &S, double dt, int 
     }
 
     if (what & ASM_MATRIX) {
-        double scale = (var == 7) ? dt / (S.hx * S.hx) : dt / (S.rho_air * S.hx * S.hx);
+        double scale = (var >= 7) ? dt / (S.hx * S.hx) : dt / (S.rho_air * S.hx * S.hx);
         bool fL = x > 0 && (plain || (fl && cell[c - 1] == CELL_FLUID));
         bool fR = x < w - 1 && (plain || (fl && cell[c + 1] == CELL_FLUID));
         bool fD = y > 0 && (plain || (fl && cell[c - P] == CELL_FLUID));
@@ -375,7 +375,7 @@ __device__ __forceinline__ void apply_pressure_body(const Scene<F> &S, double dt
     const int w = S.w, h = S.h, P = S.P, var = S.variant;
     int fx = bid.x * blockDim.x + threadIdx.x, fy = bid.y * blockDim.y + threadIdx.y;
     const uint8_t *cell = S.q[0].cell;
-    const double scale = (var == 7) ? dt / S.hx : dt / (S.rho_air * S.hx);
+    const double scale = (var >= 7) ? dt / S.hx : dt / (S.rho_air * S.hx);
     if (bid.z == 0) {  // u faces
         if (fx > w || fy >= h) return;
         size_t f = fx + (size_t)fy * P;
@@ -387,11 +387,11 @@ __device__ __forceinline__ void apply_pressure_body(const Scene<F> &S, double dt
         double val = (double)*u;
         if (fx > 0 && (var == 3 || cell[f - 1] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx - 1, fy)];
-            val += (var == 7) ? scale * pv / (double)S.udens[f] : scale * pv;
+            val += (var >= 7) ? scale * pv / (double)S.udens[f] : scale * pv;
         }
         if (fx < w && (var == 3 || cell[f] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx, fy)];
-            val -= (var == 7) ? scale * pv / (double)S.udens[f] : scale * pv;
+            val -= (var >= 7) ? scale * pv / (double)S.udens[f] : scale * pv;
         }
         *u = (F)val;
     } else {  // v faces
@@ -405,11 +405,11 @@ __device__ __forceinline__ void apply_pressure_body(const Scene<F> &S, double dt
         double val = (double)*v;
         if (fy > 0 && (var == 3 || cell[f - P] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx, fy - 1)];
-            val += (var == 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
+            val += (var >= 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
         }
         if (fy < h && (var == 3 || cell[f] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx, fy)];
-            val -= (var == 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
+            val -= (var >= 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
         }
         *v = (F)val;
     }
@@ -494,22 +494,163 @@ __global__ void __launch_bounds__(1024) extrap_solve_kernel(Scene<F> S, unsigned
     extrap_solve_body(S, qmask, counters, blockIdx.x);
 }
 
-// -------------------------------------------------------------- advection
-template <typename F> __device__ __forceinline__ F lerp1(F a, F b, F x) { return a * (F(1.0) - x) + b * x; }
-
-// FluidQuantity::lerp (3-conjugate-gradients/Fluid.cpp:121-133)
+// Step 8 (FLIP) extrapolation after the particle-to-grid transfer.  Without
+// CELL_EMPTY cells it is the DAG above (the outer ring is never extrapolated
+// in either form).  With empty cells the result depends on the reference's
+// LIFO order - an empty cell averages the neighbours that are fluid when it is
+// popped - so one thread per quantity replays the stack exactly; the other
+// threads of the CTA build the masks and the initial stack
+// (8-flip/Fluid.cpp:478-653).
 template <typename F>
-__device__ __forceinline__ F q_lerp(const F *__restrict__ src, int P, int w, int h, F ox, F oy, F x, F y) {
-    x = smin(smax(x - ox, F(0.0)), F(w) - F(1.001));
-    y = smin(smax(y - oy, F(0.0)), F(h) - F(1.001));
-    int ix = (int)x, iy = (int)y;
-    x -= F(ix);
-    y -= F(iy);
-    const F *r0 = src + ix + (size_t)iy * P;
-    F x00 = __ldg(r0), x10 = __ldg(r0 + 1);
-    F x01 = __ldg(r0 + P), x11 = __ldg(r0 + P + 1);
-    return lerp1(lerp1(x00, x10, x), lerp1(x01, x11, x), y);
+__global__ void extrap_mask_guard_kernel(Scene<F> S, unsigned qmask, int *counters, const int *skip) {
+    if (skip[blockIdx.z]) return;
+    extrap_mask_body(S, qmask, counters, blockIdx);
 }
+template <typename F>
+__global__ void __launch_bounds__(1024)
+    extrap_solve_guard_kernel(Scene<F> S, unsigned qmask, const int *counters, const int *skip) {
+    if (skip[blockIdx.x]) return;
+    extrap_solve_body(S, qmask, counters, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(1024) extrap_lifo_kernel(Scene<double> S, unsigned qmask, const int *empties) {
+    const int qi = blockIdx.x;
+    if (!((qmask >> qi) & 1u) || empties[qi] == 0) return;
+    const Quant<double> Q = S.q[qi];
+    const int w = Q.w, h = Q.h, P = S.P;
+    uint8_t *c = Q.cell, *m = Q.ready;  // `ready` holds the reference's _mask here
+    double *src = Q.src;
+    const double *nx = Q.nx, *ny = Q.ny;
+    int *stack = Q.list;
+    const long stack_cap = 2L * P * (S.h + 2);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+
+    // fillSolidMask: outer ring 0xFF; solid cells wait for non-fluid upwind
+    // neighbours; empty cells with no fluid neighbour wait for any neighbour.
+    for (int i = tid; i < w * h; i += blockDim.x) {
+        const int x = i % w, y = i / w;
+        const long idx = x + (long)y * P;
+        uint8_t mv = 0;
+        if (x == 0 || y == 0 || x == w - 1 || y == h - 1) {
+            mv = 0xFF;
+        } else if (c[idx] == CELL_SOLID) {
+            const double ax = nx[idx], ay = ny[idx];
+            if (ax != 0.0 && c[idx + sgn(ax)] != CELL_FLUID) mv |= 1;
+            if (ay != 0.0 && c[idx + (long)sgn(ay) * P] != CELL_FLUID) mv |= 2;
+        } else if (c[idx] == CELL_EMPTY) {
+            mv = c[idx - 1] != CELL_FLUID && c[idx + 1] != CELL_FLUID && c[idx - P] != CELL_FLUID &&
+                 c[idx + P] != CELL_FLUID;
+        }
+        m[idx] = mv;
+    }
+    __syncthreads();
+
+    // Initial stack: interior cells in row-major order (ordered compaction).
+    __shared__ int s_warp[32];
+    __shared__ int s_base, s_total;
+    if (tid == 0) s_base = 0;
+    __syncthreads();
+    const int iw = w - 2, ni = iw > 0 && h > 2 ? iw * (h - 2) : 0;
+    for (int base = 0; base < ni; base += blockDim.x) {
+        const int i = base + tid;
+        long idx = 0;
+        bool f = false;
+        if (i < ni) {
+            idx = 1 + i % iw + (long)(1 + i / iw) * P;
+            f = c[idx] != CELL_FLUID && m[idx] == 0;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        if (warp == 0) {
+            int v = lane < nwarps ? s_warp[lane] : 0, incl = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            s_warp[lane] = incl - v;
+            if (lane == 31) s_total = incl;
+        }
+        __syncthreads();
+        const int total = s_total;
+        if (f) stack[s_base + s_warp[warp] + __popc(bal & ((1u << lane) - 1u))] = (int)idx;
+        __syncthreads();
+        if (tid == 0) s_base += total;
+        __syncthreads();
+    }
+
+    if (tid == 0) {
+        long top = s_base, guard = 0;
+        const long limit = 8L * w * h + 64;
+        bool bad = false;
+        auto push = [&](long v) {
+            if (top >= stack_cap) bad = true;
+            else stack[top++] = (int)v;
+        };
+        while (top > 0 && !bad) {
+            if (++guard > limit) {
+                bad = true;
+                break;
+            }
+            const long idx = stack[--top];
+            if (c[idx] == CELL_EMPTY) {  // extrapolateAverage
+                double sum = 0.0;
+                int k = 0;
+                const long nb[4] = {idx - 1, idx + 1, idx - P, idx + P};
+                for (int j = 0; j < 4; j++)
+                    if (c[nb[j]] == CELL_FLUID) {
+                        sum += src[nb[j]];
+                        k++;
+                    }
+                src[idx] = sum / k;
+                c[idx] = CELL_FLUID;
+            } else {  // extrapolateNormal
+                const double ax = nx[idx], ay = ny[idx];
+                src[idx] = (fabs(ax) * src[idx + sgn(ax)] + fabs(ay) * src[idx + (long)sgn(ay) * P]) /
+                           (fabs(ax) + fabs(ay));
+            }
+            // freeSolidNeighbour: a solid neighbour whose normal points here
+            const long sn[4] = {idx - 1, idx + 1, idx - P, idx + P};
+            const bool toward[4] = {nx[idx - 1] > 0.0, nx[idx + 1] < 0.0, ny[idx - P] > 0.0, ny[idx + P] < 0.0};
+            for (int j = 0; j < 4; j++) {
+                if (!toward[j] || c[sn[j]] != CELL_SOLID) continue;
+                m[sn[j]] &= (uint8_t)~(j < 2 ? 1 : 2);
+                if (m[sn[j]] == 0) push(sn[j]);
+            }
+            // freeEmptyNeighbour
+            for (int j = 0; j < 4; j++)
+                if (c[sn[j]] == CELL_EMPTY && m[sn[j]] == 1) {
+                    m[sn[j]] = 0;
+                    push(sn[j]);
+                }
+        }
+        if (bad) atomicOr(S.flags, FLAG_FLIP_STACK);
+        // extrapolateEmptyBorders: ring cells copy the inward neighbour,
+        // corners average two ring cells.
+        for (int x = 1; x < w - 1; x++) {
+            const long t = x, b = x + (long)(h - 1) * P;
+            if (c[t] == CELL_EMPTY) src[t] = src[t + P];
+            if (c[b] == CELL_EMPTY) src[b] = src[b - P];
+        }
+        for (int y = 1; y < h - 1; y++) {
+            const long l = (long)y * P, r = (long)y * P + w - 1;
+            if (c[l] == CELL_EMPTY) src[l] = src[l + 1];
+            if (c[r] == CELL_EMPTY) src[r] = src[r - 1];
+        }
+        const long tl = 0, tr = w - 1, bl = (long)(h - 1) * P, br = (long)(h - 1) * P + w - 1;
+        if (c[tl] == CELL_EMPTY) src[tl] = 0.5 * (src[tl + 1] + src[tl + P]);
+        if (c[tr] == CELL_EMPTY) src[tr] = 0.5 * (src[tr - 1] + src[tr + P]);
+        if (c[bl] == CELL_EMPTY) src[bl] = 0.5 * (src[bl + 1] + src[bl - P]);
+        if (c[br] == CELL_EMPTY) src[br] = 0.5 * (src[br - 1] + src[br - P]);
+    }
+    __syncthreads();
+    for (int i = tid; i < w * h; i += blockDim.x) {
+        const long idx = i % w + (long)(i / w) * P;
+        if (c[idx] == CELL_EMPTY) c[idx] = CELL_FLUID;
+    }
+}
+
+// -------------------------------------------------------------- advection
 
 // Catmull-Rom weights of 3-conjugate-gradients/Fluid.cpp:55-69 (computed once
 // per fractional offset; the same expressions as the reference).
@@ -625,8 +766,9 @@ __global__ void sd_to_rows_kernel(SDIdx sd, int P, F *rows, const double *sd_arr
 // ------------------------------------------------------------------ image
 // FluidSolver::toImage (3-conjugate-gradients/Fluid.cpp:455-465,
 // 4-solid-boundaries/Fluid.cpp:903-916, 5-curved-boundaries/Fluid.cpp:961-972,
-// 7-variable-density/Fluid.cpp:1047-1081): 8-bit RGBA, row y at y*width; with
-// heat (steps 6-7) the image is 2w wide, heat colours left, shade right.
+// 7-variable-density/Fluid.cpp:1047-1081, 8-flip/Fluid.cpp:1426-1470): 8-bit
+// RGBA, row y at y*width; with heat (steps 6-8) the image is 2w wide, heat
+// colours left, shade right.
 template <typename F>
 __global__ void render_kernel(Scene<F> S, unsigned char *rgba, int heat) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -650,8 +792,13 @@ __global__ void render_kernel(Scene<F> S, unsigned char *rgba, int heat) {
     const size_t oright = heat ? 4 * (x + (size_t)y * w * 2 + w) : 4 * (x + (size_t)y * w);
     rgba[oright] = rgba[oright + 1] = rgba[oright + 2] = (unsigned char)(int)(shade * 255.0);
     rgba[oright + 3] = 0xFF;
+    if (S.variant == 8 && S.q[0].cell[c] == CELL_EMPTY) {  // 8-flip/Fluid.cpp:1446-1449
+        rgba[oright] = 0xFF;
+        rgba[oright + 1] = rgba[oright + 2] = 0;
+    }
     if (heat) {
-        double t = ((double)S.q[1].src[c] - S.t_amb) / 700.0;
+        double t = S.variant == 8 ? fabs((double)S.q[1].src[c] - S.t_amb) / 70.0
+                                  : ((double)S.q[1].src[c] - S.t_amb) / 700.0;
         t = smin(smax(t, 0.0), 1.0);
         const double r = 1.0 + volume * (smin(t * 4.0, 1.0) - 1.0);
         const double g = 1.0 + volume * (smin(t * 2.0, 1.0) - 1.0);
@@ -722,6 +869,15 @@ void launch_extrapolate(const Scene<F> &S, unsigned qmask, cudaStream_t st) {
     dim3 b(32, 8);
     extrap_mask_kernel<F><<<grid2(S.w + 1, S.h + 1, 4, b), b, 0, st>>>(S, qmask, counters);
     extrap_solve_kernel<F><<<4, 1024, 0, st>>>(S, qmask, counters);
+}
+
+void launch_extrapolate_guarded(const Scene<double> &S, unsigned qmask, const int *empty_counts, cudaStream_t st) {
+    int *counters = (int *)(S.flags + 4);
+    cudaMemsetAsync(counters, 0, 4 * sizeof(int), st);
+    dim3 b(32, 8);
+    extrap_mask_guard_kernel<double><<<grid2(S.w + 1, S.h + 1, 4, b), b, 0, st>>>(S, qmask, counters, empty_counts);
+    extrap_solve_guard_kernel<double><<<4, 1024, 0, st>>>(S, qmask, counters, empty_counts);
+    extrap_lifo_kernel<<<4, 1024, 0, st>>>(S, qmask, empty_counts);
 }
 
 template <typename F>

@@ -4,13 +4,15 @@
 // update() follows FluidSolver::update of the reference step selected by the
 // variant (3-conjugate-gradients/Fluid.cpp:433-447, 4-solid-boundaries/Fluid.cpp:869-895,
 // 5-curved-boundaries/Fluid.cpp:927-953, 6-heat/Fluid.cpp:966-1006,
-// 7-variable-density/Fluid.cpp:995-1034); buildRhs/computeDensities/
+// 7-variable-density/Fluid.cpp:995-1034, 8-flip/Fluid.cpp:1350-1413); buildRhs/computeDensities/
 // buildPressureMatrix run as one assembly launch and buildPreconditioner +
 // project as one persistent PCG launch.
 #include "solver.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <type_traits>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -94,12 +96,21 @@ class SolverImpl final : public SolverBase {
                       "init T"))
                 return IFL_ERR_CUDA;
         }
+        if (prm_.variant == IFL_FLIP) {
+            int ctl[FC_WORDS] = {};
+            ctl[FC_RNG] = (int)0xBA5EBA11u;  // frand's seed, 8-flip/Fluid.cpp:39
+            if (check(cudaMemcpy(X_.ctl, ctl, sizeof ctl, cudaMemcpyHostToDevice), "flip state")) return IFL_ERR_CUDA;
+        }
         if (check(cudaStreamSynchronize(stream_), "init sync")) return IFL_ERR_CUDA;
         return IFL_OK;
     }
 
     // ----------------------------------------------------------- phases
     int add_inflow(double x, double y, double w, double h, double d, double t, double u, double v) override {
+        if (prm_.variant == IFL_FLIP) {  // applied inside the next update, after copy()
+            pending_.push_back({x, y, w, h, d, t, u, v});
+            return IFL_OK;
+        }
         const double val[4] = {d, t, u, v};
         for (int q = 0; q < 4; q++) {
             if (!present(q)) continue;
@@ -147,7 +158,7 @@ class SolverImpl final : public SolverBase {
             break;
         case IFL_PH_RHS: assemble(dt, ASM_RHS); break;
         case IFL_PH_DENSITIES:
-            if (var == IFL_VARDENS) assemble(dt, ASM_DENS);
+            if (var >= IFL_VARDENS) assemble(dt, ASM_DENS);
             break;
         case IFL_PH_MATRIX: assemble(dt, ASM_MATRIX); break;
         case IFL_PH_PRECON: return pcg(PCG_FACTOR, false);
@@ -162,7 +173,14 @@ class SolverImpl final : public SolverBase {
         case IFL_PH_EXTRAP_DUV:
             if (var >= IFL_SOLID) extrapolate((1u << 0) | (1u << 2) | (1u << 3));
             break;
+        case IFL_PH_P2G:
+        case IFL_PH_FLIP_COPY:
+        case IFL_PH_G2P:
+        case IFL_PH_PADVECT:
+            if (var == IFL_FLIP) return flip_phase(ph, dt);
+            break;
         case IFL_PH_ADVECT: {
+            if (var == IFL_FLIP) break;  // particles carry the quantities instead
             int t = tbegin(IFL_K_ADVECT);
             launch_advect<F>(S_, dt, stream_);
             tend(t);
@@ -179,7 +197,17 @@ class SolverImpl final : public SolverBase {
     int update(double dt) override {
         const int var = prm_.variant;
         int e;
-        if (var == IFL_PLAIN) {
+        if (var == IFL_FLIP) {  // 8-flip/Fluid.cpp:1350-1413
+            static const int order[] = {IFL_PH_FILL_SOLID, IFL_PH_P2G, IFL_PH_FLIP_COPY, IFL_PH_HEAT,
+                                        IFL_PH_EXTRAP_T, IFL_PH_BUOYANCY, IFL_PH_BC};
+            for (int ph : order)
+                if ((e = run_phase(ph, dt))) return e;
+            assemble(dt, ASM_RHS | ASM_MATRIX | ASM_DENS);
+            if ((e = pcg(PCG_FACTOR | PCG_SOLVE, false))) return e;
+            static const int tail[] = {IFL_PH_APPLY_P, IFL_PH_EXTRAP_DUV, IFL_PH_BC, IFL_PH_G2P, IFL_PH_PADVECT};
+            for (int ph : tail)
+                if ((e = run_phase(ph, dt))) return e;
+        } else if (var == IFL_PLAIN) {
             assemble(dt, ASM_RHS | ASM_MATRIX);
             if ((e = pcg(PCG_FACTOR | PCG_SOLVE, false))) return e;
             if ((e = run_phase(IFL_PH_APPLY_P, dt))) return e;
@@ -192,7 +220,7 @@ class SolverImpl final : public SolverBase {
                 if ((e = run_phase(IFL_PH_BUOYANCY, dt))) return e;
             }
             if ((e = run_phase(IFL_PH_BC, dt))) return e;
-            assemble(dt, ASM_RHS | ASM_MATRIX | (var == IFL_VARDENS ? ASM_DENS : 0));
+            assemble(dt, ASM_RHS | ASM_MATRIX | (var >= IFL_VARDENS ? ASM_DENS : 0));
             if ((e = pcg(PCG_FACTOR | PCG_SOLVE, false))) return e;
             if ((e = run_phase(IFL_PH_APPLY_P, dt))) return e;
             extrapolate((1u << 0) | (1u << 2) | (1u << 3));
@@ -304,12 +332,117 @@ class SolverImpl final : public SolverBase {
         return IFL_OK;
     }
 
+    // ------------------------------------------------------ FLIP particles
+    int particle_count(int *n) override {
+        if (prm_.variant != IFL_FLIP || !n) return IFL_ERR_ARG;
+        if (check(cudaMemcpyAsync(n, X_.ctl + FC_COUNT, sizeof(int), cudaMemcpyDeviceToHost, stream_), "count") ||
+            check(cudaStreamSynchronize(stream_), "count sync"))
+            return IFL_ERR_CUDA;
+        return IFL_OK;
+    }
+    int read_particles(int which, double *out, int capacity, int *n) override {
+        if (prm_.variant != IFL_FLIP || which < 0 || which > 5 || !out || !n) return IFL_ERR_ARG;
+        if (int e = particle_count(n)) return e;
+        if (*n > capacity) return IFL_ERR_ARG;
+        if (check(cudaMemcpyAsync(out, particle_array(which), sizeof(double) * *n, cudaMemcpyDeviceToHost, stream_),
+                  "particles") ||
+            check(cudaStreamSynchronize(stream_), "particles sync"))
+            return IFL_ERR_CUDA;
+        return IFL_OK;
+    }
+    int write_particles(int which, const double *in, int n) override {
+        if (prm_.variant != IFL_FLIP || which < 0 || which > 5 || !in || n < 0 || n > X_.cap) return IFL_ERR_ARG;
+        if (check(cudaMemcpyAsync(particle_array(which), in, sizeof(double) * n, cudaMemcpyHostToDevice, stream_),
+                  "particles") ||
+            check(cudaStreamSynchronize(stream_), "particles sync"))
+            return IFL_ERR_CUDA;
+        return IFL_OK;
+    }
+    int set_particle_count(int n) override {
+        if (prm_.variant != IFL_FLIP || n < 0 || n > X_.cap) return IFL_ERR_ARG;
+        if (check(cudaMemcpyAsync(X_.ctl + FC_COUNT, &n, sizeof(int), cudaMemcpyHostToDevice, stream_), "count") ||
+            check(cudaStreamSynchronize(stream_), "count sync"))
+            return IFL_ERR_CUDA;
+        flip_ready_ = true;  // the caller's particles replace the initial ones
+        return IFL_OK;
+    }
+    int flip_init() override {
+        if (prm_.variant != IFL_FLIP) return IFL_ERR_ARG;
+        return flip_ensure_init();
+    }
+    int rng_state(uint32_t *get, const uint32_t *set) override {
+        if (prm_.variant != IFL_FLIP) return IFL_ERR_ARG;
+        if (set && check(cudaMemcpyAsync(X_.ctl + FC_RNG, set, 4, cudaMemcpyHostToDevice, stream_), "rng"))
+            return IFL_ERR_CUDA;
+        if (get && check(cudaMemcpyAsync(get, X_.ctl + FC_RNG, 4, cudaMemcpyDeviceToHost, stream_), "rng"))
+            return IFL_ERR_CUDA;
+        return check(cudaStreamSynchronize(stream_), "rng sync") ? IFL_ERR_CUDA : IFL_OK;
+    }
+
     void *scene_ptr() override { return &S_; }
     void *scratch_ptr() override { return &scratch_; }
     bool has_quantity(int q) const override { return q >= 0 && q < 4 && present(q); }
 
   private:
     bool present(int q) const { return q != 1 || nq_ == 4; }
+
+    double *particle_array(int which) const {
+        return which == 0 ? X_.px : which == 1 ? X_.py : X_.prop[which - 2];
+    }
+
+    int flip_ensure_init() {
+        if (flip_ready_) return IFL_OK;
+        if constexpr (std::is_same<F, double>::value) {
+            if (int e = upload_bodies()) return e;
+            int t = tbegin(IFL_K_PARTICLES);
+            launch_flip_init(S_, X_, stream_);
+            tend(t);
+            launches_ += 7;
+            flip_ready_ = true;
+            return launch_check("particle init");
+        }
+        return IFL_ERR_UNSUPPORTED;
+    }
+
+    // The FLIP phases (8-flip/Fluid.cpp:1356-1412); FP64 handles only.
+    int flip_phase(int ph, double dt) {
+        if constexpr (std::is_same<F, double>::value) {
+            int t = -1;
+            switch (ph) {
+            case IFL_PH_P2G:
+                if (int e = flip_ensure_init()) return e;
+                t = tbegin(IFL_K_PARTICLES);
+                launch_flip_p2g(S_, X_, stream_);
+                launches_ += 25;
+                break;
+            case IFL_PH_FLIP_COPY:
+                t = tbegin(IFL_K_FACES);
+                launch_flip_copy(S_, stream_);
+                launches_++;
+                for (const auto &f : pending_) {
+                    for (int q = 0; q < 4; q++) launch_inflow<F>(S_, q, f[0], f[1], f[0] + f[2], f[1] + f[3], f[4 + q], stream_);
+                    launches_ += 4;
+                }
+                pending_.clear();
+                break;
+            case IFL_PH_G2P:
+                t = tbegin(IFL_K_PARTICLES);
+                launch_flip_g2p(S_, X_, stream_);
+                launches_ += 2;
+                break;
+            case IFL_PH_PADVECT:
+                t = tbegin(IFL_K_PARTICLES);
+                launch_flip_advect(S_, X_, dt, stream_);
+                launches_++;
+                break;
+            default: return IFL_ERR_ARG;
+            }
+            tend(t);
+            return launch_check("flip phase");
+        }
+        (void)ph; (void)dt;
+        return IFL_ERR_UNSUPPORTED;
+    }
 
     void carve(char *base, Carver &c) {
         const size_t N = (size_t)P_ * rows_;
@@ -365,7 +498,7 @@ class SolverImpl final : public SolverBase {
         S_.mic = c.take<F>(base, 4 * NS);
         S_.pc = c.take<double>(base, NS);
         S_.nb = c.take<uint8_t>(base, NS);
-        if (prm_.variant == IFL_VARDENS) {
+        if (prm_.variant >= IFL_VARDENS) {
             S_.udens = c.take<F>(base, N);
             S_.vdens = c.take<F>(base, N);
         } else {
@@ -375,6 +508,29 @@ class SolverImpl final : public SolverBase {
         S_.bodies = d_bodies_;
         S_.nbodies = 0;
         S_.flags = c.take<unsigned>(base, 8);
+        X_ = FlipState{};
+        if (prm_.variant == IFL_FLIP) {
+            const int w = prm_.w, h = prm_.h, cells = w * h;
+            X_.cap = 12 * cells;  // _maxParticles = w*h*_MaxPerCell
+            X_.px = c.take<double>(base, X_.cap);
+            X_.py = c.take<double>(base, X_.cap);
+            for (int k = 0; k < 4; k++) X_.prop[k] = c.take<double>(base, X_.cap);
+            X_.node_off[0] = 0;
+            X_.node_off[1] = cells;
+            X_.node_off[2] = cells + (w + 1) * h;
+            X_.node_off[3] = X_.node_off[2] + w * (h + 1);
+            const int nodes = X_.node_off[3];
+            X_.bcount = c.take<unsigned long long>(base, nodes);
+            X_.bstart = c.take<unsigned long long>(base, nodes + 1);
+            X_.brank = c.take<int>(base, 3 * (size_t)X_.cap);
+            X_.blist = c.take<int>(base, 3 * (size_t)X_.cap);
+            X_.cell_count = c.take<int>(base, cells);
+            X_.seedv = c.take<unsigned long long>(base, cells);
+            X_.seedx = c.take<unsigned long long>(base, cells + 1);
+            X_.scan_tmp = c.take<unsigned long long>(base, flip_scan_tiles(std::max(nodes, cells)));
+            X_.cand = c.take<int>(base, X_.cap);
+            X_.ctl = c.take<int>(base, FC_WORDS);
+        }
         scratch_.max_blocks = max_blocks_;
         scratch_.partials = c.take<double>(base, 4 * pcg_chunks(S_.sd));
         scratch_.barrier = c.take<unsigned>(base, 2);
@@ -468,6 +624,9 @@ class SolverImpl final : public SolverBase {
     }
 
     Scene<F> S_{};
+    FlipState X_{};
+    bool flip_ready_ = false;
+    std::vector<std::array<double, 8>> pending_;  // FLIP inflows of the next update
     PcgScratch scratch_{};
     DevBody *d_bodies_ = nullptr;
     DevBody *staging_ = nullptr;  // pinned host copy of the body table

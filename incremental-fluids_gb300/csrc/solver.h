@@ -28,6 +28,20 @@ class SolverBase {
     // toImage into a host buffer (synchronising) or a device buffer (async).
     virtual int render(int heat, void *rgba, size_t bytes, bool on_device) = 0;
 
+    // Step 8 (FLIP) particle state; IFL_ERR_ARG for the other variants.
+    virtual int particle_count(int *n) { (void)n; return IFL_ERR_ARG; }
+    virtual int read_particles(int which, double *out, int capacity, int *n) {
+        (void)which; (void)out; (void)capacity; (void)n;
+        return IFL_ERR_ARG;
+    }
+    virtual int write_particles(int which, const double *in, int n) {
+        (void)which; (void)in; (void)n;
+        return IFL_ERR_ARG;
+    }
+    virtual int set_particle_count(int n) { (void)n; return IFL_ERR_ARG; }
+    virtual int flip_init() { return IFL_ERR_ARG; }
+    virtual int rng_state(uint32_t *get, const uint32_t *set) { (void)get; (void)set; return IFL_ERR_ARG; }
+
     // Access for the batch (batch.cu): Scene<F>* and PcgScratch* of this
     // handle, F as its precision.
     virtual void *scene_ptr() = 0;

@@ -23,19 +23,24 @@ LIB_PATH = os.path.join(_HERE, "libifluids.so")
 
 # include/ifluids.h constants
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5
-PLAIN, SOLID, CURVED, HEAT, VARDENS = 3, 4, 5, 6, 7
+PLAIN, SOLID, CURVED, HEAT, VARDENS, FLIP = 3, 4, 5, 6, 7, 8
 FP64, FP32 = 0, 1
 DT_F64, DT_F32, DT_U8 = 0, 1, 2
 Q_D, Q_T, Q_U, Q_V = 0, 1, 2, 3
 A_SRC, A_DST, A_PHI, A_VOLUME, A_NORMALX, A_NORMALY, A_CELL, A_BODY = 0, 1, 2, 3, 4, 5, 8, 9
 F_R, F_P, F_Z, F_S, F_PRECON, F_ADIAG, F_APLUSX, F_APLUSY, F_UDENS, F_VDENS = range(16, 26)
 (PH_FILL_SOLID, PH_HEAT, PH_EXTRAP_T, PH_BUOYANCY, PH_BC, PH_RHS, PH_DENSITIES, PH_MATRIX,
- PH_PRECON, PH_PROJECT, PH_APPLY_P, PH_EXTRAP_DUV, PH_ADVECT) = range(13)
+ PH_PRECON, PH_PROJECT, PH_APPLY_P, PH_EXTRAP_DUV, PH_ADVECT,
+ PH_P2G, PH_FLIP_COPY, PH_G2P, PH_PADVECT) = range(17)
+P_X, P_Y, P_D, P_T, P_U, P_V = range(6)
+CELL_FLUID, CELL_SOLID, CELL_EMPTY = 0, 1, 2
 PCG_CONVERGED, PCG_INITIAL, PCG_CAP = 0, 1, 2
 
 EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", "ifl_get_bodies",
            "ifl_advance_bodies", "ifl_add_inflow", "ifl_update", "ifl_run_phase", "ifl_ambient_t",
            "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_render", "ifl_flip", "ifl_get_stats",
+           "ifl_flip_init", "ifl_particle_count", "ifl_read_particles", "ifl_write_particles",
+           "ifl_set_particle_count", "ifl_get_rng_state", "ifl_set_rng_state",
            "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
            "ifl_set_timing", "ifl_get_timing", "ifl_pcg_solve_noalloc",
            "ifl_batch_default_options", "ifl_batch_create", "ifl_batch_destroy", "ifl_batch_set_inflows",
@@ -63,11 +68,11 @@ class Params(C.Structure):
 
 
 K_PCG, K_ASSEMBLE, K_ADVECT, K_SOLID, K_EXTRAPOLATE, K_FACES = range(6)
-K_NAMES = ("pcg", "assemble", "advect", "solid", "extrapolate", "faces")
+K_NAMES = ("pcg", "assemble", "advect", "solid", "extrapolate", "faces", "particles")
 
 
 class Timing(C.Structure):
-    _fields_ = [("ms", C.c_double * 6), ("launches", C.c_int64 * 6), ("pcg_iterations", C.c_int64)]
+    _fields_ = [("ms", C.c_double * 7), ("launches", C.c_int64 * 7), ("pcg_iterations", C.c_int64)]
 
 
 class _CBody(C.Structure):
@@ -160,6 +165,13 @@ def load_library(path: str = LIB_PATH):
     L.ifl_read_field.argtypes = [vp, i, vp, sz, i]
     L.ifl_write_field.argtypes = [vp, i, vp, sz, i]
     L.ifl_flip.argtypes = [vp, i]
+    L.ifl_flip_init.argtypes = [vp]
+    L.ifl_particle_count.argtypes = [vp, C.POINTER(i)]
+    L.ifl_read_particles.argtypes = [vp, i, vp, i, C.POINTER(i)]
+    L.ifl_write_particles.argtypes = [vp, i, vp, i]
+    L.ifl_set_particle_count.argtypes = [vp, i]
+    L.ifl_get_rng_state.argtypes = [vp, C.POINTER(C.c_uint32)]
+    L.ifl_set_rng_state.argtypes = [vp, C.c_uint32]
     L.ifl_render.argtypes = [vp, i, vp, sz, i]
     L.ifl_get_stats.argtypes = [vp, C.POINTER(StepStats)]
     L.ifl_set_pinned_iterations.argtypes = [vp, i, i]
@@ -262,7 +274,8 @@ class FluidSolver:
 
         FluidSolver(w, h, density)                          # 3-conjugate-gradients
         FluidSolver(w, h, density, bodies)                  # 4-solid-boundaries (variant=5: curved)
-        FluidSolver(w, h, rhoAir, rhoSoot, diffusion, bodies)  # 7-variable-density (variant=6: heat)
+        FluidSolver(w, h, rhoAir, rhoSoot, diffusion, bodies)  # 7-variable-density (variant=6: heat,
+                                                               #   variant=8: 8-flip, FP64 only)
 
     Bodies are held by reference as in the reference: before every update()
     their current state is sent to the device, so callers move them with
@@ -354,7 +367,8 @@ class FluidSolver:
 
     # -- reference surface
     def addInflow(self, x, y, w, h, d, *rest):
-        """addInflow(x, y, w, h, d, u, v) (steps 3-5) or (x, y, w, h, d, t, u, v) (steps 6-7)."""
+        """addInflow(x, y, w, h, d, u, v) (steps 3-5) or (x, y, w, h, d, t, u, v) (steps 6-8;
+        step 8 applies it inside the next update, after copy())."""
         if len(rest) == 2:
             t, (u, v) = 0.0, rest
         elif len(rest) == 3:
@@ -406,7 +420,7 @@ class FluidSolver:
         self._check(self._L.ifl_write_field(self._h, fid, arr.ctypes.data, arr.nbytes, code), "write_field")
 
     def to_image(self, heat: bool = False) -> np.ndarray:
-        """FluidSolver::toImage as an (h, w', 4) uint8 array (w' = 2w with heat in steps 6-7)."""
+        """FluidSolver::toImage as an (h, w', 4) uint8 array (w' = 2w with heat in steps 6-8)."""
         wide = 2 if (heat and self.variant >= HEAT) else 1
         out = np.empty((self.h, wide * self.w, 4), dtype=np.uint8)
         self._check(self._L.ifl_render(self._h, 1 if heat else 0, out.ctypes.data, out.nbytes, 0), "to_image")
@@ -418,6 +432,45 @@ class FluidSolver:
 
     def flip(self, quantity: int):
         self._check(self._L.ifl_flip(self._h, quantity), "flip")
+
+    # ---- step 8 (FLIP) particles
+    def flip_init(self):
+        """Place the initial particles now (the first update does it otherwise)."""
+        self._sync_bodies()
+        self._check(self._L.ifl_flip_init(self._h), "flip_init")
+
+    def particle_count(self) -> int:
+        n = C.c_int()
+        self._check(self._L.ifl_particle_count(self._h, C.byref(n)), "particle_count")
+        return n.value
+
+    def particles(self, which: int) -> np.ndarray:
+        """One particle array (P_X, P_Y, P_D, P_T, P_U, P_V) of the live particles."""
+        cap = self.w * self.h * 12
+        out = np.empty(cap, dtype=np.float64)
+        n = C.c_int()
+        self._check(self._L.ifl_read_particles(self._h, which, out.ctypes.data, cap, C.byref(n)), "particles")
+        return out[:n.value].copy()
+
+    def set_particles(self, arrays):
+        """Replace the particle state: arrays = (x, y, d, t, u, v) of equal length."""
+        n = len(arrays[0])
+        for k, a in enumerate(arrays):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if len(a) != n:
+                raise ValueError("particle arrays differ in length")
+            self._check(self._L.ifl_write_particles(self._h, k, a.ctypes.data, n), "set_particles")
+        self._check(self._L.ifl_set_particle_count(self._h, n), "set_particles")
+
+    @property
+    def rng_state(self) -> int:
+        v = C.c_uint32()
+        self._check(self._L.ifl_get_rng_state(self._h, C.byref(v)), "rng_state")
+        return int(v.value)
+
+    @rng_state.setter
+    def rng_state(self, value: int):
+        self._check(self._L.ifl_set_rng_state(self._h, int(value) & 0xFFFFFFFF), "rng_state")
 
     def set_pinned_iterations(self, pressure: int, heat: int = -1):
         """-1: stop on the residual test; k >= 0: run exactly k PCG iterations."""

@@ -5,7 +5,7 @@
  * CPU baseline in bench.py.  Never part of the product path.
  *
  * A restatement, in this project's own C, of FluidSolver::update from the
- * reference tutorial steps 3-7 (tunabrain/incremental-fluids).  Each function
+ * reference tutorial steps 3-8 (tunabrain/incremental-fluids).  Each function
  * cites the reference lines whose arithmetic it follows.  The floating-point
  * operation order of every cell update is kept identical to the reference so
  * that results are bit-identical when both sides are compiled with
@@ -31,6 +31,7 @@
 
 #define CELL_FLUID 0
 #define CELL_SOLID 1
+#define CELL_EMPTY 2
 #define PCG_TOL 1e-5
 #define MIC_TAU 0.97
 #define MIC_SIGMA 0.25
@@ -210,6 +211,13 @@ struct ifo_solver {
     int pinned, pinned_heat;
     ifo_pcg_stats st_pressure, st_heat;
     int *stack;
+    /* step 8: particles (ParticleQuantities, 8-flip/Fluid.cpp:692-731) */
+    double *px, *py, *prop[4], *weight;
+    int *counts;
+    int np, np_cap, particles_ready;
+    uint32_t rng;
+    double inflow[16][8];
+    int ninflow;
 };
 
 #define AT(qq, x, y) ((qq)->src[(x) + (y) * (qq)->w])
@@ -443,7 +451,7 @@ static void q_extrapolate(ifo_solver *s, quantity *q) {
 
 ifo_solver *ifo_create(int variant, int w, int h, double density_air,
                        double density_soot, double diffusion) {
-    if (variant < IFO_PLAIN || variant > IFO_VARDENS || w < 2 || h < 2) return NULL;
+    if (variant < IFO_PLAIN || variant > IFO_FLIP || w < 2 || h < 2) return NULL;
     ifo_solver *s = calloc(1, sizeof(ifo_solver));
     s->variant = variant;
     s->w = w;
@@ -471,6 +479,15 @@ ifo_solver *ifo_create(int variant, int w, int h, double density_air,
     s->udens = calloc((size_t)(w + 1) * h, 8);
     s->vdens = calloc((size_t)w * (h + 1), 8);
     s->stack = malloc(sizeof(int) * (16 * (size_t)(w + 2) * (h + 2) + 64));
+    s->rng = 0xBA5EBA11u;  /* frand's seed, 8-flip/Fluid.cpp:39 */
+    if (variant == IFO_FLIP) {
+        s->np_cap = w * h * 12;  /* _maxParticles = w*h*_MaxPerCell */
+        s->px = calloc((size_t)s->np_cap, 8);
+        s->py = calloc((size_t)s->np_cap, 8);
+        for (int k = 0; k < 4; k++) s->prop[k] = calloc((size_t)s->np_cap, 8);
+        s->weight = calloc((size_t)(w + 1) * (h + 1), 8);
+        s->counts = calloc(n, sizeof(int));
+    }
     return s;
 }
 
@@ -480,6 +497,8 @@ void ifo_destroy(ifo_solver *s) {
     free(s->r); free(s->p); free(s->z); free(s->s); free(s->precon);
     free(s->adiag); free(s->aplusx); free(s->aplusy); free(s->udens); free(s->vdens);
     free(s->stack);
+    free(s->px); free(s->py); free(s->weight); free(s->counts);
+    for (int k = 0; k < 4; k++) free(s->prop[k]);
     free(s);
 }
 
@@ -507,6 +526,13 @@ void ifo_advance_bodies(ifo_solver *s, double dt) {
  * 7-variable-density/Fluid.cpp:1036-1041 */
 void ifo_add_inflow(ifo_solver *s, double x, double y, double w, double h,
                     double d, double t, double u, double v) {
+    if (s->variant == IFO_FLIP) {  /* applied inside the next update, after copy() */
+        if (s->ninflow < 16) {
+            double *f = s->inflow[s->ninflow++];
+            f[0] = x; f[1] = y; f[2] = w; f[3] = h; f[4] = d; f[5] = t; f[6] = u; f[7] = v;
+        }
+        return;
+    }
     q_add_inflow(&s->q[IFO_QD], x, y, x + w, y + h, d);
     if (s->variant >= IFO_HEAT) q_add_inflow(&s->q[IFO_QT], x, y, x + w, y + h, t);
     q_add_inflow(&s->q[IFO_QU], x, y, x + w, y + h, u);
@@ -602,7 +628,7 @@ static void build_matrix(ifo_solver *s, double dt) {
             }
         return;
     }
-    double scale = (s->variant == IFO_VARDENS) ? dt / (s->hx * s->hx)
+    double scale = (s->variant >= IFO_VARDENS) ? dt / (s->hx * s->hx)
                                                : dt / (s->rho_air * s->hx * s->hx);
     memset(s->adiag, 0, n * 8);
     memset(s->aplusx, 0, n * 8);
@@ -615,7 +641,7 @@ static void build_matrix(ifo_solver *s, double dt) {
             if (x < w - 1 && cell[idx + 1] == CELL_FLUID) {
                 double f;
                 if (s->variant == IFO_SOLID) f = scale;
-                else if (s->variant == IFO_VARDENS)
+                else if (s->variant >= IFO_VARDENS)
                     f = scale * U->volume[x + 1 + y * U->w] / s->udens[x + 1 + y * (w + 1)];
                 else f = scale * U->volume[x + 1 + y * U->w];
                 s->adiag[idx] += f;
@@ -625,7 +651,7 @@ static void build_matrix(ifo_solver *s, double dt) {
             if (y < h - 1 && cell[idx + w] == CELL_FLUID) {
                 double f;
                 if (s->variant == IFO_SOLID) f = scale;
-                else if (s->variant == IFO_VARDENS) {
+                else if (s->variant >= IFO_VARDENS) {
                     long vi = (long)x + (long)(y + 1) * (w + 1);
                     if (vi >= vdn) continue;
                     f = scale * V->volume[x + (y + 1) * V->w] / s->vdens[vi];
@@ -800,7 +826,7 @@ static void apply_pressure(ifo_solver *s, double dt) {
     const uint8_t *cell = s->q[IFO_QD].cell;
     int w = s->w, h = s->h;
     int masked = s->variant >= IFO_SOLID;
-    if (s->variant == IFO_VARDENS) {
+    if (s->variant >= IFO_VARDENS) {
         double scale = dt / s->hx;
         for (int y = 0, idx = 0; y < h; y++)
             for (int x = 0; x < w; x++, idx++) {
@@ -877,6 +903,323 @@ static void flip(quantity *q) {
     q->dst = t;
 }
 
+/* ------------------------------------------------------------ step 8: FLIP
+ * ParticleQuantities and the FLIP additions to FluidQuantity
+ * (8-flip/Fluid.cpp:37-47, 296-303, 374-389, 472-690, 692-940, 1350-1413). */
+
+#define FLIP_MAX_PER_CELL 12
+#define FLIP_MIN_PER_CELL 3
+#define FLIP_AVG_PER_CELL 4
+#define FLIP_ALPHA 0.001
+
+/* frand: a 31-bit LCG whose new state's top 23 bits are the fraction of a
+ * float in [0, 1) (8-flip/Fluid.cpp:38-46; the reference forms the float by
+ * bit pattern, which is the same number). */
+float ifo_frand(uint32_t *state) {
+    *state = (*state * 1103515245u + 12345u) & 0x7FFFFFFFu;
+    return (float)(*state >> 8) * 0x1p-23f;
+}
+
+/* pointInBody: 8-flip/Fluid.cpp:724-731 (x, y in grid units) */
+static int point_in_body(const ifo_solver *s, double x, double y) {
+    for (int i = 0; i < s->nbodies; i++)
+        if (body_distance(&s->bodies[i], x * s->hx, y * s->hx) < 0.0) return 1;
+    return 0;
+}
+
+/* gridToParticles: 8-flip/Fluid.cpp:886-897 */
+static void grid_to_particles(ifo_solver *s, double alpha) {
+    for (int t = 0; t < 4; t++) {
+        const quantity *q = &s->q[t];
+        double *pr = s->prop[t];
+        for (int i = 0; i < s->np; i++) {
+            pr[i] *= 1.0 - alpha;
+            pr[i] += q_lerp(q, s->px[i], s->py[i]);
+        }
+    }
+}
+
+/* initParticles (8-flip/Fluid.cpp:733-750) followed by the solver ctor's
+ * gridToParticles(1.0) (8-flip/Fluid.cpp:1307-1314).  A position is int +
+ * float in float arithmetic, as `x + frand()` is in the reference. */
+static void flip_init(ifo_solver *s) {
+    if (s->particles_ready) return;
+    int n = 0;
+    for (int y = 0; y < s->h; y++)
+        for (int x = 0; x < s->w; x++)
+            for (int i = 0; i < FLIP_AVG_PER_CELL; i++) {
+                s->px[n] = (double)((float)x + ifo_frand(&s->rng));
+                s->py[n] = (double)((float)y + ifo_frand(&s->rng));
+                if (!point_in_body(s, s->px[n], s->py[n])) n++;
+            }
+    s->np = n;
+    s->particles_ready = 1;
+    grid_to_particles(s, 1.0);
+}
+
+/* fromParticles + addSample: hat-filter transfer onto the quantity's grid;
+ * nodes without weight turn fluid cells into CELL_EMPTY
+ * (8-flip/Fluid.cpp:296-303, 663-690). */
+static void sample_add(quantity *q, double *wgt, double value, double x, double y, int ix, int iy) {
+    if (ix < 0 || iy < 0 || ix >= q->w || iy >= q->h) return;
+    double k = (1.0 - fabs(ix - x)) * (1.0 - fabs(iy - y));
+    wgt[ix + iy * q->w] += k;
+    q->src[ix + iy * q->w] += k * value;
+}
+static void from_particles(ifo_solver *s, quantity *q, const double *value) {
+    size_t n = (size_t)q->w * q->h;
+    double *wgt = s->weight;
+    memset(q->src, 0, n * 8);
+    memset(wgt, 0, n * 8);
+    for (int i = 0; i < s->np; i++) {
+        double x = smax(0.5, smin(q->w - 1.5, s->px[i] - q->ox));
+        double y = smax(0.5, smin(q->h - 1.5, s->py[i] - q->oy));
+        int ix = (int)x, iy = (int)y;
+        sample_add(q, wgt, value[i], x, y, ix, iy);
+        sample_add(q, wgt, value[i], x, y, ix + 1, iy);
+        sample_add(q, wgt, value[i], x, y, ix, iy + 1);
+        sample_add(q, wgt, value[i], x, y, ix + 1, iy + 1);
+    }
+    for (size_t i = 0; i < n; i++) {
+        if (wgt[i] != 0.0) q->src[i] /= wgt[i];
+        else if (q->cell[i] == CELL_FLUID) q->cell[i] = CELL_EMPTY;
+    }
+}
+
+/* extrapolate with empty cells: fillSolidMask, extrapolateNormal,
+ * extrapolateAverage, freeSolidNeighbour, freeEmptyNeighbour,
+ * extrapolateEmptyBorders (8-flip/Fluid.cpp:478-653).  The outer ring is
+ * never pushed (mask 0xFF); empty cells take the mean of the neighbours that
+ * are fluid when they are popped, so the LIFO order matters here. */
+static void flip_free_solid(quantity *q, int idx, int *stack, int *top, int m) {
+    if (q->cell[idx] != CELL_SOLID) return;
+    q->mask[idx] &= (uint8_t)~m;
+    if (q->mask[idx] == 0) stack[(*top)++] = idx;
+}
+static void flip_free_empty(quantity *q, int idx, int *stack, int *top) {
+    if (q->cell[idx] == CELL_EMPTY && q->mask[idx] == 1) {
+        q->mask[idx] = 0;
+        stack[(*top)++] = idx;
+    }
+}
+static void flip_extrapolate(ifo_solver *s, quantity *q) {
+    const int w = q->w, h = q->h;
+    uint8_t *c = q->cell, *m = q->mask;
+    double *src = q->src;
+    for (int x = 0; x < w; x++) m[x] = m[x + (h - 1) * w] = 0xFF;
+    for (int y = 0; y < h; y++) m[y * w] = m[y * w + w - 1] = 0xFF;
+    for (int y = 1; y < h - 1; y++)
+        for (int x = 1; x < w - 1; x++) {
+            int idx = x + y * w;
+            m[idx] = 0;
+            if (c[idx] == CELL_SOLID) {
+                double nx = q->nx[idx], ny = q->ny[idx];
+                if (nx != 0.0 && c[idx + sgn(nx)] != CELL_FLUID) m[idx] |= 1;
+                if (ny != 0.0 && c[idx + sgn(ny) * w] != CELL_FLUID) m[idx] |= 2;
+            } else if (c[idx] == CELL_EMPTY) {
+                m[idx] = c[idx - 1] != CELL_FLUID && c[idx + 1] != CELL_FLUID &&
+                         c[idx - w] != CELL_FLUID && c[idx + w] != CELL_FLUID;
+            }
+        }
+    int *stack = s->stack, top = 0;
+    for (int y = 1; y < h - 1; y++)
+        for (int x = 1; x < w - 1; x++) {
+            int idx = x + y * w;
+            if (c[idx] != CELL_FLUID && m[idx] == 0) stack[top++] = idx;
+        }
+    while (top > 0) {
+        int idx = stack[--top];
+        if (c[idx] == CELL_EMPTY) {
+            double sum = 0.0;
+            int k = 0;
+            const int nb[4] = {idx - 1, idx + 1, idx - w, idx + w};
+            for (int j = 0; j < 4; j++)
+                if (c[nb[j]] == CELL_FLUID) {
+                    sum += src[nb[j]];
+                    k++;
+                }
+            src[idx] = sum / k;
+            c[idx] = CELL_FLUID;
+        } else {
+            double nx = q->nx[idx], ny = q->ny[idx];
+            src[idx] = (fabs(nx) * src[idx + sgn(nx)] + fabs(ny) * src[idx + sgn(ny) * w]) /
+                       (fabs(nx) + fabs(ny));
+        }
+        if (q->nx[idx - 1] > 0.0) flip_free_solid(q, idx - 1, stack, &top, 1);
+        if (q->nx[idx + 1] < 0.0) flip_free_solid(q, idx + 1, stack, &top, 1);
+        if (q->ny[idx - w] > 0.0) flip_free_solid(q, idx - w, stack, &top, 2);
+        if (q->ny[idx + w] < 0.0) flip_free_solid(q, idx + w, stack, &top, 2);
+        flip_free_empty(q, idx - 1, stack, &top);
+        flip_free_empty(q, idx + 1, stack, &top);
+        flip_free_empty(q, idx - w, stack, &top);
+        flip_free_empty(q, idx + w, stack, &top);
+    }
+    /* outer ring: copy the inward neighbour, corners average two ring cells */
+    for (int x = 1; x < w - 1; x++) {
+        int t = x, b = x + (h - 1) * w;
+        if (c[t] == CELL_EMPTY) src[t] = src[t + w];
+        if (c[b] == CELL_EMPTY) src[b] = src[b - w];
+    }
+    for (int y = 1; y < h - 1; y++) {
+        int l = y * w, r = y * w + w - 1;
+        if (c[l] == CELL_EMPTY) src[l] = src[l + 1];
+        if (c[r] == CELL_EMPTY) src[r] = src[r - 1];
+    }
+    const int tl = 0, tr = w - 1, bl = (h - 1) * w, br = h * w - 1;
+    if (c[tl] == CELL_EMPTY) src[tl] = 0.5 * (src[tl + 1] + src[tl + w]);
+    if (c[tr] == CELL_EMPTY) src[tr] = 0.5 * (src[tr - 1] + src[tr + w]);
+    if (c[bl] == CELL_EMPTY) src[bl] = 0.5 * (src[bl + 1] + src[bl - w]);
+    if (c[br] == CELL_EMPTY) src[br] = 0.5 * (src[br - 1] + src[br - w]);
+    for (int i = 0; i < w * h; i++)
+        if (c[i] == CELL_EMPTY) c[i] = CELL_FLUID;
+}
+
+/* countParticles / pruneParticles / seedParticles (8-flip/Fluid.cpp:752-818).
+ * Seeding rejects an attempt when particle number `cell index` (not the new
+ * particle) lies inside a body, as the reference does. */
+static void copy_particle(ifo_solver *s, int dst, int src) {
+    s->px[dst] = s->px[src];
+    s->py[dst] = s->py[src];
+    for (int t = 0; t < 4; t++) s->prop[t][dst] = s->prop[t][src];
+}
+static void count_prune_seed(ifo_solver *s) {
+    const int w = s->w, h = s->h;
+    int *cnt = s->counts;
+    memset(cnt, 0, sizeof(int) * (size_t)w * h);
+    for (int i = 0; i < s->np; i++) {
+        int ix = (int)s->px[i], iy = (int)s->py[i];
+        if (ix >= 0 && iy >= 0 && ix < w && iy < h) cnt[ix + iy * w]++;
+    }
+    for (int i = 0; i < s->np; i++) {
+        int ix = (int)s->px[i], iy = (int)s->py[i];
+        if (ix < 0 || iy < 0 || ix >= w || iy >= h) continue;
+        int idx = ix + iy * w;
+        if (cnt[idx] > FLIP_MAX_PER_CELL) {
+            copy_particle(s, i, --s->np);
+            cnt[idx]--;
+            i--;
+        }
+    }
+    for (int y = 0, idx = 0; y < h; y++)
+        for (int x = 0; x < w; x++, idx++)
+            for (int i = 0; i < FLIP_MIN_PER_CELL - cnt[idx]; i++) {
+                if (s->np == s->np_cap) return;
+                int j = s->np;
+                s->px[j] = (double)((float)x + ifo_frand(&s->rng));
+                s->py[j] = (double)((float)y + ifo_frand(&s->rng));
+                if (point_in_body(s, s->px[idx], s->py[idx])) continue;
+                for (int t = 0; t < 4; t++) s->prop[t][j] = q_lerp(&s->q[t], s->px[j], s->py[j]);
+                s->np++;
+            }
+}
+
+/* particlesToGrid: 8-flip/Fluid.cpp:899-912 */
+static void particles_to_grid(ifo_solver *s) {
+    flip_init(s);
+    for (int t = 0; t < 4; t++) {
+        from_particles(s, &s->q[t], s->prop[t]);
+        flip_extrapolate(s, &s->q[t]);
+    }
+    count_prune_seed(s);
+}
+
+/* copy() of every quantity, then the inflows of this update
+ * (8-flip/Fluid.cpp:374-376, 1359-1368) */
+static void flip_copy(ifo_solver *s) {
+    for (int t = 0; t < 4; t++) {
+        quantity *q = &s->q[t];
+        memcpy(q->dst, q->src, (size_t)q->w * q->h * 8);
+    }
+    for (int k = 0; k < s->ninflow; k++) {
+        const double *f = s->inflow[k];
+        for (int t = 0; t < 4; t++)
+            q_add_inflow(&s->q[t], f[0], f[1], f[0] + f[2], f[1] + f[3], f[4 + t]);
+    }
+    s->ninflow = 0;
+}
+
+/* diff(alpha), gridToParticles(alpha), undiff(alpha)
+ * (8-flip/Fluid.cpp:378-389, 1394-1409); `dst` holds _old in step 8. */
+static void flip_g2p(ifo_solver *s) {
+    const double keep = 1.0 - FLIP_ALPHA;
+    for (int t = 0; t < 4; t++) {
+        quantity *q = &s->q[t];
+        for (int i = 0; i < q->w * q->h; i++) q->src[i] -= keep * q->dst[i];
+    }
+    grid_to_particles(s, FLIP_ALPHA);
+    for (int t = 0; t < 4; t++) {
+        quantity *q = &s->q[t];
+        for (int i = 0; i < q->w * q->h; i++) q->src[i] += keep * q->dst[i];
+    }
+}
+
+/* ParticleQuantities::advect with the forward rungeKutta3 and backProject
+ * (8-flip/Fluid.cpp:820-870, 916-924); the last RK stage is not divided by
+ * hx, as in the reference. */
+static void particle_advect(ifo_solver *s, double dt) {
+    const quantity *u = &s->q[IFO_QU], *v = &s->q[IFO_QV];
+    const double hx = s->hx;
+    for (int i = 0; i < s->np; i++) {
+        double x = s->px[i], y = s->py[i];
+        double firstU = q_lerp(u, x, y) / hx;
+        double firstV = q_lerp(v, x, y) / hx;
+        double midX = x + 0.5 * dt * firstU;
+        double midY = y + 0.5 * dt * firstV;
+        double midU = q_lerp(u, midX, midY) / hx;
+        double midV = q_lerp(v, midX, midY) / hx;
+        double lastX = x + 0.75 * dt * midU;
+        double lastY = y + 0.75 * dt * midV;
+        double lastU = q_lerp(u, lastX, lastY);
+        double lastV = q_lerp(v, lastX, lastY);
+        x += dt * ((2.0 / 9.0) * firstU + (3.0 / 9.0) * midU + (4.0 / 9.0) * lastU);
+        y += dt * ((2.0 / 9.0) * firstV + (3.0 / 9.0) * midV + (4.0 / 9.0) * lastV);
+        double d = 1e30;
+        int nearest = -1;
+        for (int b = 0; b < s->nbodies; b++) {
+            double db = body_distance(&s->bodies[b], x * hx, y * hx);
+            if (db < d) {
+                d = db;
+                nearest = b;
+            }
+        }
+        if (d < -1.0) {
+            x *= hx;
+            y *= hx;
+            body_closest(&s->bodies[nearest], &x, &y);
+            double nx, ny;
+            body_normal(&s->bodies[nearest], &nx, &ny, x, y);
+            x -= nx * hx;
+            y -= ny * hx;
+            x /= hx;
+            y /= hx;
+        }
+        s->px[i] = smax(smin(x, s->w - 0.001), 0.0);
+        s->py[i] = smax(smin(y, s->h - 0.001), 0.0);
+    }
+}
+
+double *ifo_particles(ifo_solver *s, int which, int *count) {
+    *count = s->np;
+    if (s->variant != IFO_FLIP) return NULL;
+    switch (which) {
+    case IFO_P_X: return s->px;
+    case IFO_P_Y: return s->py;
+    case IFO_P_D: case IFO_P_T: case IFO_P_U: case IFO_P_V: return s->prop[which - IFO_P_D];
+    default: return NULL;
+    }
+}
+void ifo_set_particle_count(ifo_solver *s, int n) {
+    if (s->variant == IFO_FLIP && n >= 0 && n <= s->np_cap) {
+        s->np = n;
+        s->particles_ready = 1;
+    }
+}
+void ifo_flip_init(ifo_solver *s) {
+    if (s->variant == IFO_FLIP) flip_init(s);
+}
+uint32_t ifo_rng_state(const ifo_solver *s) { return s->rng; }
+void ifo_set_rng_state(ifo_solver *s, uint32_t state) { s->rng = state; }
+
 void ifo_phase(ifo_solver *s, int phase, double dt) {
     int v = s->variant;
     switch (phase) {
@@ -888,22 +1231,36 @@ void ifo_phase(ifo_solver *s, int phase, double dt) {
         q_fill_solid(s, &s->q[IFO_QV]);
         break;
     case IFO_PH_HEAT: if (v >= IFO_HEAT) heat_solve(s, dt); break;
-    case IFO_PH_EXTRAP_T: if (v >= IFO_HEAT) q_extrapolate(s, &s->q[IFO_QT]); break;
+    case IFO_PH_EXTRAP_T:
+        if (v == IFO_FLIP) flip_extrapolate(s, &s->q[IFO_QT]);
+        else if (v >= IFO_HEAT) q_extrapolate(s, &s->q[IFO_QT]);
+        break;
     case IFO_PH_BUOYANCY: if (v >= IFO_HEAT) add_buoyancy(s, dt); break;
     case IFO_PH_BC: if (v >= IFO_SOLID) set_bc(s); break;
     case IFO_PH_RHS: build_rhs(s); break;
-    case IFO_PH_DENSITIES: if (v == IFO_VARDENS) compute_densities(s); break;
+    case IFO_PH_DENSITIES: if (v >= IFO_VARDENS) compute_densities(s); break;
     case IFO_PH_MATRIX: build_matrix(s, dt); break;
     case IFO_PH_PRECON: build_precon(s); break;
     case IFO_PH_PROJECT: project(s, v == IFO_PLAIN ? 600 : 2000, s->pinned, &s->st_pressure); break;
     case IFO_PH_APPLY_P: apply_pressure(s, dt); break;
     case IFO_PH_EXTRAP_DUV:
         if (v < IFO_SOLID) break;
+        if (v == IFO_FLIP) {
+            flip_extrapolate(s, &s->q[IFO_QD]);
+            flip_extrapolate(s, &s->q[IFO_QU]);
+            flip_extrapolate(s, &s->q[IFO_QV]);
+            break;
+        }
         q_extrapolate(s, &s->q[IFO_QD]);
         q_extrapolate(s, &s->q[IFO_QU]);
         q_extrapolate(s, &s->q[IFO_QV]);
         break;
+    case IFO_PH_P2G: if (v == IFO_FLIP) particles_to_grid(s); break;
+    case IFO_PH_FLIP_COPY: if (v == IFO_FLIP) flip_copy(s); break;
+    case IFO_PH_G2P: if (v == IFO_FLIP) flip_g2p(s); break;
+    case IFO_PH_PADVECT: if (v == IFO_FLIP) particle_advect(s, dt); break;
     case IFO_PH_ADVECT:
+        if (v == IFO_FLIP) break;
         q_advect(s, &s->q[IFO_QD], dt);
         if (v >= IFO_HEAT) q_advect(s, &s->q[IFO_QT], dt);
         q_advect(s, &s->q[IFO_QU], dt);
@@ -926,6 +1283,15 @@ void ifo_update(ifo_solver *s, double dt) {
         ifo_phase(s, IFO_PH_PROJECT, dt);
         ifo_phase(s, IFO_PH_APPLY_P, dt);
         ifo_phase(s, IFO_PH_ADVECT, dt);
+        return;
+    }
+    if (s->variant == IFO_FLIP) {  /* 8-flip/Fluid.cpp:1350-1413 */
+        static const int order[] = {
+            IFO_PH_FILL_SOLID, IFO_PH_P2G, IFO_PH_FLIP_COPY, IFO_PH_HEAT, IFO_PH_EXTRAP_T,
+            IFO_PH_BUOYANCY, IFO_PH_BC, IFO_PH_RHS, IFO_PH_DENSITIES, IFO_PH_MATRIX,
+            IFO_PH_PRECON, IFO_PH_PROJECT, IFO_PH_APPLY_P, IFO_PH_EXTRAP_DUV, IFO_PH_BC,
+            IFO_PH_G2P, IFO_PH_PADVECT};
+        for (size_t k = 0; k < sizeof order / sizeof order[0]; k++) ifo_phase(s, order[k], dt);
         return;
     }
     ifo_phase(s, IFO_PH_FILL_SOLID, dt);
@@ -1032,8 +1398,13 @@ void ifo_to_image(const ifo_solver *s, unsigned char *rgba, int heat) {
             shade = smin(smax(shade, 0.0), 1.0);
             rgba[idxr + 0] = rgba[idxr + 1] = rgba[idxr + 2] = (unsigned char)(int)(shade * 255.0);
             rgba[idxr + 3] = 0xFF;
+            if (s->variant == IFO_FLIP && d->cell[x + y * w] == CELL_EMPTY) {
+                rgba[idxr + 0] = 0xFF;
+                rgba[idxr + 1] = rgba[idxr + 2] = 0;
+            }
             if (heat) {
-                double tt = (t->src[x + y * w] - s->t_amb) / 700.0;
+                double tt = s->variant == IFO_FLIP ? fabs(t->src[x + y * w] - s->t_amb) / 70.0
+                                                   : (t->src[x + y * w] - s->t_amb) / 700.0;
                 tt = smin(smax(tt, 0.0), 1.0);
                 const double r = 1.0 + volume * (smin(tt * 4.0, 1.0) - 1.0);
                 const double g = 1.0 + volume * (smin(tt * 2.0, 1.0) - 1.0);

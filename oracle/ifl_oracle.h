@@ -2,7 +2,7 @@
  * ifl_oracle.h - CPU oracle for the incremental-fluids per-step hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
- * solver's arithmetic (tunabrain/incremental-fluids, tutorial steps 3-7), used
+ * solver's arithmetic (tunabrain/incremental-fluids, tutorial steps 3-8), used
  * by the tests as the parity checker and by bench.py as the timed CPU
  * baseline.  The CUDA product path never links, loads or calls it.
  *
@@ -29,7 +29,9 @@ enum {
     IFO_SOLID = 4,    /* 4-solid-boundaries    */
     IFO_CURVED = 5,   /* 5-curved-boundaries   */
     IFO_HEAT = 6,     /* 6-heat                */
-    IFO_VARDENS = 7   /* 7-variable-density    */
+    IFO_VARDENS = 7,  /* 7-variable-density    */
+    IFO_FLIP = 8      /* 8-flip: step 7's grid solve, FLIP particles carry
+                         d, T, u, v instead of semi-Lagrangian advection */
 };
 
 /* Quantities (FluidQuantity instances). */
@@ -60,8 +62,19 @@ enum {
     IFO_PH_PROJECT = 9,      /* project(limit)                              */
     IFO_PH_APPLY_P = 10,     /* applyPressure                               */
     IFO_PH_EXTRAP_DUV = 11,  /* _d/_u/_v->extrapolate()                     */
-    IFO_PH_ADVECT = 12       /* advect every quantity, then flip           */
+    IFO_PH_ADVECT = 12,      /* advect every quantity, then flip           */
+    /* step 8 (FLIP) only */
+    IFO_PH_P2G = 13,         /* particlesToGrid: transfer, extrapolate,
+                                count, prune, seed (initialises the
+                                particles first when needed)               */
+    IFO_PH_FLIP_COPY = 14,   /* copy() of every quantity, then the inflows
+                                registered since the last update            */
+    IFO_PH_G2P = 15,         /* diff, gridToParticles(alpha), undiff        */
+    IFO_PH_PADVECT = 16      /* ParticleQuantities::advect                  */
 };
+
+/* Particle arrays of step 8 (ifo_particles). */
+enum { IFO_P_X = 0, IFO_P_Y = 1, IFO_P_D = 2, IFO_P_T = 3, IFO_P_U = 4, IFO_P_V = 5 };
 
 /* PCG outcome. */
 enum { IFO_PCG_CONVERGED = 0, IFO_PCG_INITIAL = 1, IFO_PCG_CAP = 2 };
@@ -106,8 +119,23 @@ void ifo_flip(ifo_solver *s, int quantity);
 /* FluidSolver::toImage: 8-bit RGBA, w x h (heat and step >= 6: 2w x h, heat
  * colours left, shade right); 3-conjugate-gradients/Fluid.cpp:455-465,
  * 4-solid-boundaries/Fluid.cpp:903-916, 5-curved-boundaries/Fluid.cpp:961-972,
- * 7-variable-density/Fluid.cpp:1047-1081. */
+ * 7-variable-density/Fluid.cpp:1047-1081, 8-flip/Fluid.cpp:1426-1470; step 8
+ * paints CELL_EMPTY density cells red and scales heat by |T - Tamb|/70. */
 void ifo_to_image(const ifo_solver *s, unsigned char *rgba, int heat);
+
+/* Step 8 (FLIP) particle state.  ifo_particles returns the array (capacity
+ * 12*w*h) and the live count; ifo_flip_init places the initial particles
+ * (initParticles + gridToParticles(1.0), 8-flip/Fluid.cpp:733-750,
+ * 1307-1314) if that has not happened yet - the first update does it
+ * otherwise.  The random stream is the reference's frand() LCG, one stream
+ * per solver, starting at 0xBA5EBA11. */
+double *ifo_particles(ifo_solver *s, int which, int *count);
+void ifo_set_particle_count(ifo_solver *s, int n);
+void ifo_flip_init(ifo_solver *s);
+uint32_t ifo_rng_state(const ifo_solver *s);
+void ifo_set_rng_state(ifo_solver *s, uint32_t state);
+/* frand() of 8-flip/Fluid.cpp:38-46 on an explicit state (known-answer tests). */
+float ifo_frand(uint32_t *state);
 
 /* Scalar kernels for known-answer tests: occupancy() of
  * 7-variable-density/Fluid.cpp:68-102 and the clamped Catmull-Rom of

@@ -3,7 +3,7 @@
 Two back-ends with one interface:
 
 * ``OracleSolver`` drives ``oracle/liboracle.so``, the plain-C restatement of
-  the reference solver (tutorial steps 3-7).  It builds on any host and is the
+  the reference solver (tutorial steps 3-8).  It builds on any host and is the
   parity checker the GPU tests use, and the CPU baseline bench.py times.
 * ``RefSolver`` drives ``oracle/_ref/libref<step>.so``: the reference's own
   ``Fluid.cpp`` compiled unmodified (see ``oracle/ref_shim.cpp``).  It exists
@@ -27,13 +27,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
-PLAIN, SOLID, CURVED, HEAT, VARDENS = 3, 4, 5, 6, 7
+PLAIN, SOLID, CURVED, HEAT, VARDENS, FLIP = 3, 4, 5, 6, 7, 8
 QD, QT, QU, QV = 0, 1, 2, 3
 A_SRC, A_DST, A_PHI, A_VOLUME, A_NORMALX, A_NORMALY = 0, 1, 2, 3, 4, 5
 A_R, A_P, A_Z, A_S, A_PRECON, A_ADIAG, A_APLUSX, A_APLUSY, A_UDENS, A_VDENS = range(16, 26)
 B_CELL, B_BODY, B_MASK = 0, 1, 2
 (PH_FILL_SOLID, PH_HEAT, PH_EXTRAP_T, PH_BUOYANCY, PH_BC, PH_RHS, PH_DENSITIES,
- PH_MATRIX, PH_PRECON, PH_PROJECT, PH_APPLY_P, PH_EXTRAP_DUV, PH_ADVECT) = range(13)
+ PH_MATRIX, PH_PRECON, PH_PROJECT, PH_APPLY_P, PH_EXTRAP_DUV, PH_ADVECT,
+ PH_P2G, PH_FLIP_COPY, PH_G2P, PH_PADVECT) = range(17)
+P_X, P_Y, P_D, P_T, P_U, P_V = range(6)
 PCG_CONVERGED, PCG_INITIAL, PCG_CAP = 0, 1, 2
 
 
@@ -87,6 +89,15 @@ def _oracle_lib():
         L.ifo_cerp.restype = d
         L.ifo_to_image.argtypes = [vp, C.c_void_p, i]
         L.ifo_to_image.restype = None
+        L.ifo_particles.restype = C.POINTER(C.c_double)
+        L.ifo_particles.argtypes = [vp, i, C.POINTER(i)]
+        L.ifo_set_particle_count.argtypes = [vp, i]
+        L.ifo_flip_init.argtypes = [vp]
+        L.ifo_rng_state.restype = C.c_uint32
+        L.ifo_rng_state.argtypes = [vp]
+        L.ifo_set_rng_state.argtypes = [vp, C.c_uint32]
+        L.ifo_frand.restype = C.c_float
+        L.ifo_frand.argtypes = [C.POINTER(C.c_uint32)]
         _lib = L
     return _lib
 
@@ -100,8 +111,14 @@ def _view(ptr, w, h, dtype):
     return arr.reshape(h, w)
 
 
+def _particle_view(ptr, n):
+    if not ptr:
+        return None
+    return np.ctypeslib.as_array(ptr, shape=(max(n, 0),))[:n]
+
+
 class OracleSolver:
-    """The C restatement of FluidSolver (steps 3-7), FP64, zero-initialised."""
+    """The C restatement of FluidSolver (steps 3-8), FP64, zero-initialised."""
 
     def __init__(self, variant: int, w: int, h: int, density: float = 0.1,
                  density_soot: float = 1.0, diffusion: float = 0.01):
@@ -177,6 +194,49 @@ class OracleSolver:
     def _to_image(self, ptr, heat):
         self.L.ifo_to_image(self.p, ptr, heat)
 
+    # ---- step 8 particles
+    def particle_count(self) -> int:
+        n = C.c_int()
+        self.L.ifo_particles(self.p, P_X, C.byref(n))
+        return n.value
+
+    def particles(self, which: int) -> np.ndarray:
+        """Live view of one particle array (P_X .. P_V), length = particle count."""
+        n = C.c_int()
+        ptr = self.L.ifo_particles(self.p, which, C.byref(n))
+        return _particle_view(ptr, n.value)
+
+    def set_particles(self, arrays):
+        """Replace the particle state: arrays = (x, y, d, t, u, v), equal lengths."""
+        n = len(arrays[0])
+        cap = self.w * self.h * 12
+        if n > cap:
+            raise ValueError("more particles than 12 per cell")
+        self.L.ifo_set_particle_count(self.p, n)
+        for k, a in enumerate(arrays):
+            m = C.c_int()
+            ptr = self.L.ifo_particles(self.p, k, C.byref(m))
+            np.ctypeslib.as_array(ptr, shape=(cap,))[:n] = np.asarray(a, dtype=np.float64)
+
+    def flip_init(self):
+        self.L.ifo_flip_init(self.p)
+
+    @property
+    def rng_state(self) -> int:
+        return int(self.L.ifo_rng_state(self.p))
+
+    @rng_state.setter
+    def rng_state(self, v: int):
+        self.L.ifo_set_rng_state(self.p, int(v) & 0xFFFFFFFF)
+
+
+def frand_stream(state: int, n: int):
+    """n values of the reference's frand() from `state`; returns (values, new state)."""
+    st = C.c_uint32(state)
+    L = _oracle_lib()
+    out = np.array([L.ifo_frand(C.byref(st)) for _ in range(n)], dtype=np.float32)
+    return out, int(st.value)
+
 
 def occupancy(d11, d12, d21, d22) -> float:
     return _oracle_lib().ifo_occupancy(d11, d12, d21, d22)
@@ -212,6 +272,10 @@ def _ref_lib(step):
         L.ref_bytes.argtypes = [vp, i, i, C.POINTER(i), C.POINTER(i)]
         L.ref_to_image.argtypes = [vp, C.c_void_p, i]
         L.ref_to_image.restype = None
+        L.ref_particles.restype = C.POINTER(C.c_double)
+        L.ref_particles.argtypes = [vp, i, C.POINTER(i)]
+        L.ref_particle_report.restype = i
+        L.ref_set_particle_count.argtypes = [vp, i]
         _ref_libs[step] = L
     return _ref_libs[step]
 
@@ -292,3 +356,27 @@ class RefSolver:
 
     def _to_image(self, ptr, heat):
         self.L.ref_to_image(self.p, ptr, heat)
+
+    # ---- step 8 particles (the reference's frand() stream is one static per
+    # process: pin step 8 in a fresh process per reference solver)
+    def particle_count(self) -> int:
+        n = C.c_int()
+        self.L.ref_particles(self.p, P_X, C.byref(n))
+        return n.value
+
+    def particles(self, which: int) -> np.ndarray:
+        n = C.c_int()
+        ptr = self.L.ref_particles(self.p, which, C.byref(n))
+        return _particle_view(ptr, n.value)
+
+    def set_particles(self, arrays):
+        """Replace the particle state: arrays = (x, y, d, t, u, v), equal lengths."""
+        n = len(arrays[0])
+        cap = self.w * self.h * 12
+        if n > cap:
+            raise ValueError("more particles than 12 per cell")
+        self.L.ref_set_particle_count(self.p, n)
+        for k, a in enumerate(arrays):
+            m = C.c_int()
+            ptr = self.L.ref_particles(self.p, k, C.byref(m))
+            np.ctypeslib.as_array(ptr, shape=(cap,))[:n] = np.asarray(a, dtype=np.float64)

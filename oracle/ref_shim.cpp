@@ -47,6 +47,7 @@ namespace {
 struct pcg_record { int iterations; int status; double max_error; };
 pcg_record g_log[8];
 int g_nlog = 0;
+int g_particle_count = -1;
 }
 
 /* Records "Exiting solver after %d iterations, maximum error is %f",
@@ -55,6 +56,11 @@ int g_nlog = 0;
 extern "C" int ref_printf_hook(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
+    if (strncmp(fmt, "Particle", 8) == 0) {  /* step 8's particlesToGrid report */
+        g_particle_count = va_arg(ap, int);
+        va_end(ap);
+        return 0;
+    }
     pcg_record rec = {0, 1, 0.0};
     if (strncmp(fmt, "Exiting", 7) == 0) {
         int it = va_arg(ap, int);
@@ -78,13 +84,18 @@ struct RefScene {
 #endif
     FluidSolver *solver = nullptr;
     int w = 0, h = 0;
+    double rho_air = 0, rho_soot = 0, diffusion = 0;
 };
 
 void zero(double *p, size_t n) { memset(p, 0, n * sizeof(double)); }
 
 void zero_quantity(FluidQuantity *q) {
     size_t n = (size_t)q->_w * q->_h;
+#if REF_STEP == 8
+    zero(q->_old, n);
+#else
     zero(q->_dst, n);
+#endif
 #if REF_STEP >= 4
     zero(q->_normalX, n);
     zero(q->_normalY, n);
@@ -95,14 +106,12 @@ void zero_quantity(FluidQuantity *q) {
     zero(q->_phi, (size_t)(q->_w + 1) * (q->_h + 1));
 #endif
 }
-}  // namespace
-
-extern "C" {
-
-void *ref_create(int w, int h, double rho_air, double rho_soot, double diffusion) {
-    RefScene *s = new RefScene();
-    s->w = w;
-    s->h = h;
+/* Constructs the reference solver.  Step 8's constructor seeds particles
+ * against the body list, so there it runs on first use, after the bodies have
+ * been added (the reference's main also creates the bodies first). */
+void build(RefScene *s) {
+    const int w = s->w, h = s->h;
+    const double rho_air = s->rho_air, rho_soot = s->rho_soot, diffusion = s->diffusion;
 #if REF_STEP == 3
     (void)rho_soot; (void)diffusion;
     s->solver = new FluidSolver(w, h, rho_air);
@@ -126,11 +135,37 @@ void *ref_create(int w, int h, double rho_air, double rho_soot, double diffusion
     zero(f->_uDensity, (size_t)(w + 1) * h);
     zero(f->_vDensity, (size_t)w * (h + 1));
 #endif
+}
+
+FluidSolver *solver_of(void *p) {
+    RefScene *s = (RefScene *)p;
+    if (!s->solver) build(s);
+    return s->solver;
+}
+}  // namespace
+
+extern "C" {
+
+void *ref_create(int w, int h, double rho_air, double rho_soot, double diffusion) {
+    RefScene *s = new RefScene();
+    s->w = w;
+    s->h = h;
+    s->rho_air = rho_air;
+    s->rho_soot = rho_soot;
+    s->diffusion = diffusion;
+#if REF_STEP != 8
+    build(s);
+#endif
     return s;
 }
 
 void ref_destroy(void *p) {
     RefScene *s = (RefScene *)p;
+#if REF_STEP == 8
+    /* ~FluidSolver of step 8 deletes the quantities twice (once itself, once
+     * through ~ParticleQuantities); the solver is left allocated. */
+    s->solver = nullptr;
+#endif
     delete s->solver;
 #if REF_STEP >= 4
     for (SolidBody *b : s->bodies) delete b;
@@ -176,7 +211,10 @@ void ref_advance_bodies(void *p, double dt) {
 
 void ref_add_inflow(void *p, double x, double y, double w, double h, double d, double t, double u, double v) {
     RefScene *s = (RefScene *)p;
-#if REF_STEP >= 6
+#if REF_STEP == 8
+    /* step 8's update() applies its own fixed inflow (8-flip/Fluid.cpp:1368) */
+    (void)s; (void)x; (void)y; (void)w; (void)h; (void)d; (void)t; (void)u; (void)v;
+#elif REF_STEP >= 6
     s->solver->addInflow(x, y, w, h, d, t, u, v);
 #else
     (void)t;
@@ -188,7 +226,7 @@ void ref_add_inflow(void *p, double x, double y, double w, double h, double d, d
 int ref_update(void *p, double dt) {
     RefScene *s = (RefScene *)p;
     g_nlog = 0;
-    s->solver->update(dt);
+    solver_of(s)->update(dt);
     return g_nlog;
 }
 
@@ -205,7 +243,7 @@ int ref_pcg_record(int k, int *iterations, int *status, double *max_error) {
 /* Same array identifiers as the oracle (ifl_oracle.h). */
 double *ref_array(void *p, int qid, int which, int *w, int *h) {
     RefScene *s = (RefScene *)p;
-    FluidSolver *f = s->solver;
+    FluidSolver *f = solver_of(s);
     if (which >= 16) {
         *w = s->w;
         *h = s->h;
@@ -239,7 +277,11 @@ double *ref_array(void *p, int qid, int which, int *w, int *h) {
     *h = q->_h;
     switch (which) {
     case 0: return q->_src;
+#if REF_STEP == 8
+    case 1: return q->_old;
+#else
     case 1: return q->_dst;
+#endif
 #if REF_STEP >= 5
     case 2: *w = q->_w + 1; *h = q->_h + 1; return q->_phi;
     case 3: return q->_volume;
@@ -255,7 +297,7 @@ double *ref_array(void *p, int qid, int which, int *w, int *h) {
 uint8_t *ref_bytes(void *p, int qid, int which, int *w, int *h) {
 #if REF_STEP >= 4
     RefScene *s = (RefScene *)p;
-    FluidSolver *f = s->solver;
+    FluidSolver *f = solver_of(s);
     FluidQuantity *q = nullptr;
     switch (qid) {
     case 0: q = f->_d; break;
@@ -282,11 +324,40 @@ uint8_t *ref_bytes(void *p, int qid, int which, int *w, int *h) {
 
 void ref_to_image(void *p, unsigned char *rgba, int heat) {
 #if REF_STEP >= 6
-    ((RefScene *)p)->solver->toImage(rgba, heat != 0);
+    solver_of(p)->toImage(rgba, heat != 0);
 #else
     (void)heat;
     ((RefScene *)p)->solver->toImage(rgba);
 #endif
 }
+
+/* Step 8 particle arrays (ParticleQuantities::_posX, _posY, _properties[k])
+ * and the live count; the same identifiers as ifo_particles. */
+double *ref_particles(void *p, int which, int *count) {
+#if REF_STEP == 8
+    ParticleQuantities *q = solver_of(p)->_qs;
+    *count = q->_particleCount;
+    if (which == 0) return q->_posX;
+    if (which == 1) return q->_posY;
+    if (which >= 2 && which < 6) return q->_properties[which - 2];
+    return nullptr;
+#else
+    (void)p; (void)which;
+    *count = 0;
+    return nullptr;
+#endif
+}
+
+/* Sets the live particle count (tests write the arrays through ref_particles). */
+void ref_set_particle_count(void *p, int n) {
+#if REF_STEP == 8
+    solver_of(p)->_qs->_particleCount = n;
+#else
+    (void)p; (void)n;
+#endif
+}
+
+/* Particle count the last particlesToGrid printed (-1 before any). */
+int ref_particle_report(void) { return g_particle_count; }
 
 }  // extern "C"

@@ -7,7 +7,12 @@ The fixtures travel with the repository, so the oracle restatement and the GPU
 path can be checked against reference outputs where the reference source is
 not available.
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [scene ...]
+
+Step 8 (FLIP) also stores the particles and their count after every step;
+its reference keeps the frand() seed in a static, so at most one step-8 scene
+runs per process (here: one).  Its update() adds a fixed inflow, which the
+scene's inflow tuple repeats for the other side.
 """
 import math
 import os
@@ -36,21 +41,29 @@ SCENES = [
     ("curved_32", 5, 32, 32, 0.005, 6, (0.45, 0.2, 0.15, 0.06, 1.0, 0.0, 0.0, 3.0), [BOX]),
     ("heat_32", 6, 32, 32, 0.005, 6, (0.35, 0.2, 0.2, 0.1, 1.0, 594.0, 0.0, 0.0), [BOX]),
     ("vardens_32", 7, 32, 32, 0.005, 6, (0.45, 0.2, 0.1, 0.1, 1.0, 700.0, 0.0, 0.0), [BOX]),
+    ("flip_32", 8, 32, 32, 0.0025, 4, (0.45, 0.2, 0.2, 0.05, 1.0, 294.0, 0.0, 0.0), [BOX]),
 ]
+PARTICLE_KEYS = ("px", "py", "pd", "pt", "pu", "pv")
 
 
 def run_reference(variant, w, h, dt, steps, inflow, bodies):
     s = O.RefSolver(variant, w, h)
     if bodies:
         s.set_bodies(bodies)
-    iters = []
+    iters, counts = [], []
     for _ in range(steps):
         s.add_inflow(*inflow)
         s.update(dt)
         s.advance_bodies(dt)
         pr, ht = s.stats()
         iters.append((pr[0], pr[1], ht[0], ht[1]))
+        if variant == O.FLIP:
+            counts.append(s.particle_count())
     out = {"iters": np.array(iters, dtype=np.int64), "p": s.array(0, O.A_P).copy()}
+    if variant == O.FLIP:
+        out["np"] = np.array(counts, dtype=np.int64)
+        for k, key in enumerate(PARTICLE_KEYS):
+            out[key] = s.particles(k).copy()
     for name, q in (("d", O.QD), ("t", O.QT), ("u", O.QU), ("v", O.QV)):
         a = s.array(q, O.A_SRC)
         if a is not None:
@@ -59,7 +72,10 @@ def run_reference(variant, w, h, dt, steps, inflow, bodies):
 
 
 def main():
+    only = set(sys.argv[1:])
     for name, variant, w, h, dt, steps, inflow, bodies in SCENES:
+        if only and name not in only:
+            continue
         if not O.ref_available(variant):
             raise SystemExit(f"reference step {variant} not built: make -C oracle ref")
         out = run_reference(variant, w, h, dt, steps, inflow, bodies)

@@ -1,0 +1,172 @@
+"""Step 8 (FLIP) CUDA path against the oracle, through the C ABI (needs a GB300).
+
+Bars:
+* bit-exact (equal IEEE values) from the same state for the particle phases:
+  the initial placement, particle -> grid transfer with its extrapolation
+  (empty cells included), count / prune / seed, the frand() stream, the
+  grid -> particle update (diff, gridToParticles, undiff) and the particle
+  advection, and for toImage;
+* whole updates, where the PCG solves differ in rounding (parallel dot
+  products), with the PCG pinned to the same iteration counts on both sides:
+  fields 1e-9 relative (to max(|field|, 1)), particle positions 1e-9 cells,
+  carried values 1e-8 relative (to max(|value|, 1)), identical particle counts.
+The oracle is pinned to the reference's own step-8 code in test_flip_pin.py.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+import flip_cases as FC
+
+pytestmark = pytest.mark.gpu
+
+QUANTS = (O.QD, O.QT, O.QU, O.QV)
+
+
+def _pair(ifl, w, h, bodies):
+    o = O.OracleSolver(O.FLIP, w, h, FC.RHO_AIR, FC.RHO_SOOT, FC.DIFFUSION)
+    objs = [ifl.SolidBox(*b[1:]) if b[0] == 0 else ifl.SolidSphere(b[1], b[2], b[3], *b[5:]) for b in bodies]
+    g = ifl.FluidSolver(w, h, FC.RHO_AIR, FC.RHO_SOOT, FC.DIFFUSION, objs, variant=ifl.FLIP)
+    if bodies:
+        o.set_bodies(bodies)
+    return o, g, objs
+
+
+def _particles_equal(ifl, g, o, tag):
+    assert g.particle_count() == o.particle_count(), tag
+    for k in range(6):
+        a, b = g.particles(k), o.particles(k)
+        assert np.array_equal(a, b), (tag, k, int(np.argmax(a != b)))
+    assert g.rng_state == o.rng_state, tag
+
+
+def _fields_equal(ifl, g, o, tag):
+    for q in QUANTS:
+        assert np.array_equal(g.read_field(ifl.field_id(q, ifl.A_SRC)), o.array(q, O.A_SRC)), (tag, q)
+        assert np.array_equal(g.read_field(ifl.field_id(q, ifl.A_CELL), np.uint8), o.bytes(q, O.B_CELL)), (tag, q)
+
+
+def _random_fields(ifl, g, o, seed):
+    rng = np.random.default_rng(seed)
+    for q in QUANTS:
+        a = o.array(q, O.A_SRC)
+        vals = rng.normal(294.0 if q == O.QT else 0.0, 0.5, a.shape)
+        a[...] = vals
+        g.write_field(ifl.field_id(q, ifl.A_SRC), vals.copy())
+
+
+@pytest.mark.parametrize("scene", FC.SCENES, ids=[s[0] for s in FC.SCENES])
+def test_initial_particles_bit_exact(ifl, scene):
+    _, w, h, bodies, _ = scene
+    o, g, _ = _pair(ifl, w, h, bodies)
+    o.flip_init()
+    g.flip_init()
+    _particles_equal(ifl, g, o, "init")
+
+
+@pytest.mark.parametrize("scene", FC.SCENES, ids=[s[0] for s in FC.SCENES])
+def test_particles_to_grid_bit_exact(ifl, scene):
+    """Transfer, order-exact extrapolation with empty cells, prune and seeding
+    from the crafted particle state (every branch taken)."""
+    _, w, h, bodies, _ = scene
+    o, g, _ = _pair(ifl, w, h, bodies)
+    o.flip_init()
+    g.flip_init()
+    arrays = FC.crafted(w, h, o.particles(O.P_X).copy(), o.particles(O.P_Y).copy())
+    o.set_particles(arrays)
+    g.set_particles(arrays)
+    _random_fields(ifl, g, o, 1)
+    for ph in (O.PH_FILL_SOLID, O.PH_P2G):
+        o.phase(ph, FC.DT)
+        g.run_phase(ph, FC.DT)
+    _fields_equal(ifl, g, o, "p2g")
+    _particles_equal(ifl, g, o, "p2g")
+    assert g.stats()[2] & 0xC == 0
+
+
+@pytest.mark.parametrize("scene", FC.SCENES, ids=[s[0] for s in FC.SCENES])
+def test_grid_to_particles_and_advection_bit_exact(ifl, scene):
+    _, w, h, bodies, _ = scene
+    o, g, _ = _pair(ifl, w, h, bodies)
+    o.flip_init()
+    g.flip_init()
+    _random_fields(ifl, g, o, 2)
+    for ph in (O.PH_FILL_SOLID, O.PH_FLIP_COPY):  # old = src
+        o.phase(ph, FC.DT)
+        g.run_phase(ph, FC.DT)
+    _random_fields(ifl, g, o, 3)                   # the update's change
+    for ph in (O.PH_G2P, O.PH_PADVECT):
+        o.phase(ph, FC.DT)
+        g.run_phase(ph, FC.DT)
+    _fields_equal(ifl, g, o, "g2p")               # src after diff + undiff
+    _particles_equal(ifl, g, o, "g2p")
+
+
+def test_seeding_stops_at_the_particle_cap(ifl):
+    """Seeding stops once the count reaches 12 per cell, and the frand()
+    stream advances by the attempts actually made.  Particles outside the
+    grid count towards the cap but not towards any cell (countParticles skips
+    them), which is how the cap can be reached."""
+    w, h = 24, 20
+    o, g, _ = _pair(ifl, w, h, [FC.BOX])
+    rng = np.random.default_rng(5)
+    cap = 12 * w * h
+    cells = np.repeat(np.arange(w * h), 2)            # 2 per cell: one seeding attempt each
+    n_out = cap - 5 - len(cells)                       # 5 free slots
+    x = np.concatenate([(cells % w) + rng.random(len(cells)), np.full(n_out, -3.0)])
+    y = np.concatenate([(cells // w) + rng.random(len(cells)), h * rng.random(n_out)])
+    n = len(x)
+    arrays = (x, y, rng.random(n), 294.0 + rng.random(n), rng.random(n), rng.random(n))
+    o.set_particles(arrays)
+    g.set_particles(arrays)
+    g.rng_state = o.rng_state
+    for ph in (O.PH_FILL_SOLID, O.PH_P2G):
+        o.phase(ph, FC.DT)
+        g.run_phase(ph, FC.DT)
+    assert o.particle_count() == cap
+    _particles_equal(ifl, g, o, "cap")
+
+
+@pytest.mark.parametrize("scene", FC.SCENES, ids=[s[0] for s in FC.SCENES])
+def test_whole_updates_with_pinned_pcg(ifl, scene):
+    _, w, h, bodies, steps = scene
+    o, g, objs = _pair(ifl, w, h, bodies)
+    o.set_pinned_iterations(30, 3)
+    g.set_pinned_iterations(30, 3)
+    for step in range(steps + 2):
+        o.add_inflow(*FC.INFLOW)
+        g.addInflow(*FC.INFLOW)
+        o.update(FC.DT)
+        g.update(FC.DT)
+        o.advance_bodies(FC.DT)
+        for b in objs:
+            b.update(FC.DT)
+        assert g.particle_count() == o.particle_count(), step
+        for q in QUANTS:
+            a, b = g.read_field(ifl.field_id(q, ifl.A_SRC)), o.array(q, O.A_SRC)
+            # relative to the field's scale, floored at 1 (a velocity field of
+            # rounding-level values in a body-free start has no scale of its own)
+            assert np.abs(a - b).max() <= 1e-9 * max(np.abs(b).max(), 1.0), (step, q)
+        assert np.abs(g.particles(O.P_X) - o.particles(O.P_X)).max() <= 1e-9
+        assert np.abs(g.particles(O.P_Y) - o.particles(O.P_Y)).max() <= 1e-9
+        for k in (O.P_D, O.P_T, O.P_U, O.P_V):
+            a, b = g.particles(k), o.particles(k)
+            assert np.abs(a - b).max() <= 1e-8 * max(np.abs(b).max(), 1.0), (step, k)
+    assert g.stats()[2] == 0
+
+
+def test_to_image_marks_empty_cells(ifl):
+    w, h = 40, 32
+    o, g, _ = _pair(ifl, w, h, [FC.BOX])
+    o.flip_init()
+    g.flip_init()
+    _random_fields(ifl, g, o, 4)
+    cells = np.zeros((h, w), dtype=np.uint8)
+    cells[5:9, 10:20] = 2  # CELL_EMPTY
+    cells[20, :] = 1
+    o.bytes(O.QD, O.B_CELL)[...] = cells
+    g.write_field(ifl.field_id(ifl.Q_D, ifl.A_CELL), cells.copy())
+    for heat in (False, True):
+        a, b = g.to_image(heat), o.to_image(heat)
+        assert np.array_equal(a, b), heat
+    assert (g.to_image(False)[6, 12] == [255, 0, 0, 255]).all()

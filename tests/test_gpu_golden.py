@@ -69,3 +69,9 @@ def test_gpu_fp64_matches_golden(ifl, path):
             if key == "p":
                 a, b = a[fluid], b[fluid]
             assert np.abs(a - b).max() <= 1e-9 * max(np.abs(b).max(), 1e-300), key
+    if variant == 8:  # FLIP particles: same count, positions to 1e-9 cells, carried values 1e-8
+        assert s.particle_count() == int(g["np"][-1])
+        for k, key in enumerate(("px", "py", "pd", "pt", "pu", "pv")):
+            a, b = s.particles(k), g[key]
+            tol = 1e-9 if k < 2 else 1e-8 * max(np.abs(b).max(), 1e-300)
+            assert np.abs(a - b).max() <= tol, key

@@ -36,18 +36,24 @@ def test_oracle_reproduces_golden(path):
     s = O.OracleSolver(variant, w, h)
     if bodies:
         s.set_bodies(bodies)
-    iters = []
+    iters, counts = [], []
     for _ in range(steps):
         s.add_inflow(*inflow)
         s.update(dt)
         s.advance_bodies(dt)
         pr, ht = s.stats()
         iters.append((pr[0], pr[1], ht[0], ht[1]))
+        if variant == O.FLIP:
+            counts.append(s.particle_count())
     assert np.array_equal(np.array(iters), g["iters"])
     for key, q in (("d", O.QD), ("t", O.QT), ("u", O.QU), ("v", O.QV)):
         if key in g:
             assert np.array_equal(s.array(q, O.A_SRC), g[key]), key
     assert np.array_equal(s.array(0, O.A_P), g["p"])
+    if variant == O.FLIP:
+        assert counts == list(g["np"])
+        for k, key in enumerate(("px", "py", "pd", "pt", "pu", "pv")):
+            assert np.array_equal(s.particles(k), g[key]), key
 
 
 BOX = (0, 0.5, 0.6, 0.7, 0.1, math.pi * 0.25, 0.0, 0.0, 0.0)
