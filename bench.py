@@ -23,7 +23,10 @@ cell-steps/s = sum of w*h over the scenes x steps per second.
             cores over a size-stratified sample of the scenes.
 
 --workload single: the single solid-boundary scene at 1024 x 1024 (3 seeded
-bodies) instead.  --impl reference times the reference's CPU algorithm (the
+bodies) instead.  --workload flip: step 8 (FLIP particles) on the reference
+main()'s own scene (rotated box, its fixed inflow, rhoAir 0.1, rhoSoot 0.25,
+diffusion 0.01, dt 0.0025) at --size (128, the reference's grid), FP64,
+one handle; its CPU baseline is the oracle's step-8 restatement.  --impl reference times the reference's CPU algorithm (the
 oracle port; the reference's own sources are not present on the GPU host) on
 the same workload.  Multi-GPU (torchrun): each rank runs an independent
 replica ("replicas only": scenes do not exchange data), barrier + max over
@@ -336,6 +339,114 @@ def run_gpu(args, rank, world, local_rank):
             "pcg_status_last": pst, "fp64_dropin": fp64, "cells": cells, "scene": sc}
 
 
+# ----------------------------------------------------------- FLIP workload
+FLIP_BOX = (0.5, 0.6, 0.7, 0.1, math.pi * 0.25, 0.0, 0.0, 0.0)   # 8-flip/Fluid.cpp:1489
+FLIP_INFLOW = (0.45, 0.2, 0.2, 0.05, 1.0, 294.0, 0.0, 0.0)       # 8-flip/Fluid.cpp:1368
+FLIP_RHO = (0.1, 0.25, 0.01)                                     # 8-flip/Fluid.cpp:1479-1481
+FLIP_DT = 0.0025
+
+
+def cpu_baseline_flip(n: int, steps: int):
+    """The oracle's step-8 restatement (single thread, as the reference) on the same scene."""
+    from oracle import oracle as O
+    s = O.OracleSolver(O.FLIP, n, n, *FLIP_RHO)
+    s.set_bodies([(0,) + FLIP_BOX])
+    s.add_inflow(*FLIP_INFLOW)
+    s.update(FLIP_DT)  # first update places the particles (not timed)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.add_inflow(*FLIP_INFLOW)
+        s.update(FLIP_DT)
+    t = time.perf_counter() - t0
+    return {"value": n * n * steps / t, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{steps} update() of the {n}x{n} FLIP scene after its first step, FP64 oracle "
+                      f"(bit-identical to the reference's step-8 code), {s.particle_count()} particles",
+            "seconds": round(t, 3), "particles": s.particle_count()}
+
+
+def run_flip(args, local_rank):
+    import torch
+    import ifluids as ifl
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n = args.size
+
+    def make():
+        box = ifl.SolidBox(*FLIP_BOX)
+        return ifl.FluidSolver(n, n, *FLIP_RHO, [box], variant=ifl.FLIP, device=local_rank)
+
+    def step(s):
+        s.addInflow(*FLIP_INFLOW)
+        s.update(FLIP_DT)
+
+    g, ge = make(), make()
+    stream = torch.cuda.ExternalStream(g.stream, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(1, args.warmup)):
+        step(g)
+        step(ge)
+    g.synchronize()
+    ge.synchronize()
+    g.set_timing(True)
+    g.timing()
+    launches0 = g.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+                ev[k][0].record(stream)
+            step(g)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+        g.synchronize()
+        torch.cuda.synchronize(dev)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_ms = sum(step_ms)
+    launches = g.launch_count() - launches0
+    kms, klaunch, iters = g.timing()
+    g.set_timing(False)
+    (pit, pst, _), (hit, _, _), flags = g.stats()
+    if flags & 1:
+        raise RuntimeError("device-side wait timed out during the benchmark")
+    particles = g.particle_count()
+
+    host_d = torch.empty((n, n), dtype=torch.float64, pin_memory=True).numpy()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(ge)
+        ge.read_field("d", dtype=host_d.dtype, out=host_d)
+    e2e_s = time.perf_counter() - t0
+    ge.close()
+    cells = n * n
+    # particle kernels: algorithmic bytes per particle and step (FP64 state of
+    # x, y and four carried values = 48 B): transfer reads x, y, the carried
+    # value of the grid's quantities once per grid kind and writes a bucket
+    # rank and index (3 x (16 + 8)), the per-node gather reads x, y and the
+    # carried values once more (3 x 16 + 32), count reads x, y (16), the
+    # grid -> particle update reads x, y and reads/writes the four values
+    # (16 + 64), advection reads/writes x, y (32): 312 B
+    part_bytes = 312.0 * particles
+    pk_ms = kms.get("particles", 0.0) / args.steps
+    peak, peak_kind = load_peaks()
+    achieved = part_bytes / (pk_ms / 1e3) / 1e9 if pk_ms > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": "particle kernels (transfer, seeding, update, advection)",
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "peak_kind": f"of {peak_kind}", "traffic": None,
+            "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
+            "pcg_iterations_last_step": [pit, hit]}
+    g.close()
+    return {"value": cells * args.steps / (dev_ms / 1e3), "ms_per_step": dev_ms / args.steps,
+            "e2e": {"value": cells * args.steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 96,
+                    "d2h_bytes_per_step": cells * 8},
+            "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(), "fp64_dropin": None,
+            "particles": particles,
+            "particle_steps_per_s": particles * args.steps / (dev_ms / 1e3),
+            "latency_ms": {"p50": round(statistics.median(step_ms), 3), "max": round(max(step_ms), 3)}}
+
+
 # ----------------------------------------------------- batched workload
 BATCH_COUNT, BATCH_SEED = 512, 2
 
@@ -618,7 +729,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=("batch", "single", "c3"), default="batch")
+    ap.add_argument("--workload", choices=("batch", "single", "c3", "flip"), default="batch")
     ap.add_argument("--count", type=int, default=BATCH_COUNT, help="scenes of the batched workload")
     ap.add_argument("--size", type=int, default=0, help="side of the single-scene workload (1024; c3: 2048)")
     ap.add_argument("--precision", choices=("fp32", "fp64"), default="fp32")
@@ -633,7 +744,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
     if not args.size:
-        args.size = 2048 if args.workload == "c3" else 1024
+        args.size = {"c3": 2048, "flip": 128}.get(args.workload, 1024)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -647,6 +758,13 @@ def main():
                   "variant": "4-solid-boundaries", "scenes": args.count, "seed": BATCH_SEED,
                   "precision_form": args.precision,
                   "l2": "inputs larger than L2 (about 6 GB of scene state)", "scene_data": "seeded synthetic scenes"}
+    elif args.workload == "flip":
+        config = {"workload": f"FLIP particles (8-flip) on the reference main's scene {args.size}x{args.size}: "
+                              f"rotated box, fixed inflow d=1 T=294 K, rhoAir 0.1, rhoSoot 0.25, diffusion 0.01, "
+                              f"dt=0.0025",
+                  "variant": "8-flip", "grid": [args.size, args.size], "precision_form": "fp64",
+                  "l2": "flushed between timed steps (512 MiB write)", "scene_data": "the reference's own scene"}
+        args.precision = "fp64"
     elif args.workload == "c3":
         config = {"workload": f"heat + variable density scene {args.size}x{args.size} (7-variable-density), "
                               f"ambient 294 K, inflow d=1 T=700 K, the reference main's box, dt=0.001 (configs[3])",
@@ -664,7 +782,10 @@ def main():
         if rank != 0:
             return
         steps = max(1, min(args.steps, 2))
-        if batch:
+        if args.workload == "flip":
+            cb = cpu_baseline_flip(args.size, max(2, min(args.steps, 20)))
+            note = "the reference's step-8 algorithm on one host core (oracle port, bit-identical to it)"
+        elif batch:
             cb = cpu_baseline_batch(procs, steps=1)
             note = ("reference algorithm on the host cores (oracle port of the reference sources, "
                     "bit-identical to them where they compile) over a size-stratified sample of the batch")
@@ -685,12 +806,18 @@ def main():
 
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu:  # before any GPU work (spawned pool)
-        cb = cpu_baseline_batch(procs) if batch else cpu_baseline(args.size, 1, procs, args.seed)
+        if args.workload == "flip":
+            cb = cpu_baseline_flip(args.size, 10)
+        else:
+            cb = cpu_baseline_batch(procs) if batch else cpu_baseline(args.size, 1, procs, args.seed)
     if world > 1:
         import torch.distributed as dist
         import torch
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    r = run_batch(args, rank, world, local_rank) if batch else run_gpu(args, rank, world, local_rank)
+    if args.workload == "flip":
+        r = run_flip(args, local_rank)
+    else:
+        r = run_batch(args, rank, world, local_rank) if batch else run_gpu(args, rank, world, local_rank)
     if rank != 0:
         return
     line = {"metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -704,6 +831,10 @@ def main():
         line["batch"] = r["batch"]
         if args.serve_requests > 0 and world == 1:
             line["serving"] = run_serve(args, local_rank)
+    elif args.workload == "flip":
+        line["particles"] = r["particles"]
+        line["particle_steps_per_s"] = r["particle_steps_per_s"]
+        line["latency_ms"] = r["latency_ms"]
     else:
         line["pcg"] = {"iterations_last_step": r["pcg_iterations_last"], "status_last_step": r["pcg_status_last"]}
     print(json.dumps(line), flush=True)

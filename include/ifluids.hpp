@@ -68,7 +68,7 @@ class FluidSolver {
         : bodies_(&bodies) {
         init(variant, w, h, density, 1.0, 0.01, precision);
     }
-    // 7-variable-density (variant = IFL_HEAT for 6-heat)
+    // 7-variable-density (variant = IFL_HEAT for 6-heat, IFL_FLIP for 8-flip)
     FluidSolver(int w, int h, double rhoAir, double rhoSoot, double diffusion,
                 const std::vector<const SolidBody *> &bodies, int variant = IFL_VARDENS,
                 int precision = IFL_FP64)
@@ -88,8 +88,12 @@ class FluidSolver {
         check(ifl_add_inflow(h_, x, y, w, h, d, t, u, v), "addInflow");
     }
     // The bodies are held by reference, as in the reference: their current
-    // state is sent to the device at every update.
+    // state is sent to the device at every update.  Step 8's update() adds
+    // its own inflow after copy() (8-flip/Fluid.cpp:1368); so does this one
+    // unless builtinInflow(false) was called.
     void update(double timestep) {
+        if (variant_ == IFL_FLIP && builtin_inflow_)
+            check(ifl_add_inflow(h_, 0.45, 0.2, 0.2, 0.05, 1.0, ambientT(), 0.0, 0.0), "addInflow");
         if (bodies_) {
             std::vector<ifl_body> tab;
             tab.reserve(bodies_->size());
@@ -111,7 +115,16 @@ class FluidSolver {
         if (h) *h = fh;
         return out;
     }
-    // FluidSolver::toImage: rgba holds w*h*4 bytes (2*w*h*4 with renderHeat in steps 6-7).
+    // Step 8: particle positions or carried values (IFL_P_X .. IFL_P_V).
+    std::vector<double> particles(int which) {
+        int n = 0;
+        check(ifl_particle_count(h_, &n), "particle count");
+        std::vector<double> out((size_t)n);
+        check(ifl_read_particles(h_, which, out.data(), n, &n), "particles");
+        return out;
+    }
+    void builtinInflow(bool on) { builtin_inflow_ = on; }
+    // FluidSolver::toImage: rgba holds w*h*4 bytes (2*w*h*4 with renderHeat in steps 6-8).
     void toImage(unsigned char *rgba, bool renderHeat = false) {
         int w = 0, h = 0;
         check(ifl_field_shape(h_, IFL_FIELD(IFL_Q_D, IFL_A_SRC), &w, &h), "field shape");
@@ -143,6 +156,7 @@ class FluidSolver {
     }
     ifl_solver *h_ = nullptr;
     int variant_ = IFL_PLAIN;
+    bool builtin_inflow_ = true;
     const std::vector<const SolidBody *> *bodies_ = nullptr;
 };
 
