@@ -48,6 +48,10 @@ enum {
 
 /* Variant = tutorial step of the reference whose update() is reproduced. */
 enum {
+    IFL_GS_EULER = 1, /* 1-matrixless: Gauss-Seidel solve, forward Euler +
+                         bilinear advection, flat inflow (h <= 1024)          */
+    IFL_GS = 2,       /* 2-better-advection: Gauss-Seidel solve, step 3's
+                         advection and inflow (h <= 1024)                     */
     IFL_PLAIN = 3,    /* 3-conjugate-gradients: MIC(0)-PCG, no solids          */
     IFL_SOLID = 4,    /* 4-solid-boundaries: binary solid cells               */
     IFL_CURVED = 5,   /* 5-curved-boundaries: fractional cell volumes         */
@@ -110,13 +114,14 @@ enum {
 enum { IFL_PCG_CONVERGED = 0, IFL_PCG_INITIAL = 1, IFL_PCG_CAP = 2 };
 
 typedef struct {
-    int32_t variant;           /* IFL_PLAIN .. IFL_FLIP                          */
+    int32_t variant;           /* IFL_GS_EULER .. IFL_FLIP                       */
     int32_t w, h;              /* pressure grid size (>= 2 each)                 */
     int32_t precision;         /* IFL_FP64 or IFL_FP32                           */
     double density_air;        /* `density` of steps 3-5, rhoAir of 6-7 (0.1)    */
     double density_soot;       /* rhoSoot (1.0)                                  */
     double diffusion;          /* heat diffusion (0.01)                          */
-    int32_t max_iter_pressure; /* 600 in step 3, 2000 in steps 4-7               */
+    int32_t max_iter_pressure; /* 600 in steps 1-3 (Gauss-Seidel sweeps in 1-2),
+                                  2000 in steps 4-8                             */
     int32_t max_iter_heat;     /* 2000                                           */
     void *stream;              /* cudaStream_t to use; NULL = handle-owned stream */
     int32_t device;            /* CUDA device ordinal the handle lives on (0)    */

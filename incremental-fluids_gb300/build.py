@@ -22,7 +22,7 @@ OUT_DIR = os.path.join(PKG, "ifluids")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT_DIR, "libifluids.so")
 
-SOURCES = ["k_fields.cu", "k_pcg.cu", "k_flip.cu", "solver.cu", "batch.cu", "noalloc.cu", "server.cpp", "capi.cpp"]
+SOURCES = ["k_fields.cu", "k_pcg.cu", "k_flip.cu", "k_gs.cu", "solver.cu", "batch.cu", "noalloc.cu", "server.cpp", "capi.cpp"]
 HEADERS = ["ifl_internal.h", "ifl_device.cuh", "solver.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",

@@ -581,8 +581,8 @@ int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, 
     for (int i = 0; i < n; i++) {
         if (!members[i]) return IFL_ERR_ARG;
         const ifl_params &p = members[i]->params();
-        if (p.variant == IFL_FLIP) {
-            if (err) *err = "step 8 (FLIP) handles are stepped one by one, not in batches";
+        if (p.variant == IFL_FLIP || p.variant <= IFL_GS) {
+            if (err) *err = "step 1, 2 and 8 handles are stepped one by one, not in batches";
             return IFL_ERR_UNSUPPORTED;
         }
         if (p.variant != p0.variant || p.precision != p0.precision || p.device != p0.device) {

@@ -93,7 +93,7 @@ void ifl_default_params(ifl_params *p, int variant, int w, int h) {
     p->density_air = 0.1;   // every reference main(): density / densityAir = 0.1
     p->density_soot = 1.0;  // 7-variable-density/Fluid.cpp:1090
     p->diffusion = 0.01;    // 7-variable-density/Fluid.cpp:1091
-    p->max_iter_pressure = variant == IFL_PLAIN ? 600 : 2000;  // 3-conjugate-gradients/Fluid.cpp:437
+    p->max_iter_pressure = variant <= IFL_PLAIN ? 600 : 2000;  // 1-matrixless/Fluid.cpp:286, 3-conjugate-gradients/Fluid.cpp:437
     p->max_iter_heat = 2000;                                    // 7-variable-density/Fluid.cpp:1004
     p->stream = nullptr;
 }
@@ -101,8 +101,9 @@ void ifl_default_params(ifl_params *p, int variant, int w, int h) {
 int ifl_create(const ifl_params *p, ifl_solver **out) {
     if (!p || !out) return IFL_ERR_ARG;
     *out = nullptr;
-    if (p->variant < IFL_PLAIN || p->variant > IFL_FLIP) return IFL_ERR_ARG;
+    if (p->variant < IFL_GS_EULER || p->variant > IFL_FLIP) return IFL_ERR_ARG;
     if (p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768) return IFL_ERR_ARG;
+    if (p->variant <= IFL_GS && p->h > ifl::gs_max_rows()) return IFL_ERR_UNSUPPORTED;  // one CTA of strips
     if (p->precision != IFL_FP64 && p->precision != IFL_FP32) return IFL_ERR_ARG;
     if (p->variant == IFL_FLIP && p->precision != IFL_FP64) return IFL_ERR_UNSUPPORTED;  // particles are FP64
     if (p->variant == IFL_FLIP && (int64_t)p->w * p->h * 12 > 0x7fffffff) return IFL_ERR_UNSUPPORTED;
@@ -352,7 +353,7 @@ const char *ifl_server_last_error(const ifl_server *s) {
 }
 
 int64_t ifl_device_bytes(const ifl_params *p) {
-    if (!p || p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768 || p->variant < IFL_PLAIN ||
+    if (!p || p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768 || p->variant < IFL_GS_EULER ||
         p->variant > IFL_FLIP || (p->precision != IFL_FP64 && p->precision != IFL_FP32))
         return IFL_ERR_ARG;
     int sms = 152, dev = 0;

@@ -154,6 +154,10 @@ template <typename F> void launch_render(const Scene<F> &S, unsigned char *rgba,
 template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
                                              cudaStream_t st, int *blocks_used);
 template <typename F> int pcg_max_blocks();
+// Gauss-Seidel solve of steps 1-2 (k_gs.cu): one CTA, h <= gs_max_rows().
+template <typename F>
+cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st);
+int gs_max_rows();
 
 // Batched PCG: many scenes in one cooperative launch (k_pcg.cu).  The plan
 // holds the per-scene job tables and the team/queue tables on the device.

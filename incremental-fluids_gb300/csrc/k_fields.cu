@@ -19,14 +19,15 @@ template <typename F> __device__ __forceinline__ F ldv(const F *p) { return *(co
 template <typename F> __device__ __forceinline__ void stv(F *p, F v) { *(volatile F *)p = v; }
 
 // ----------------------------------------------------------------- inflow
-// FluidQuantity::addInflow (3-conjugate-gradients/Fluid.cpp:167-184).  The x
+// FluidQuantity::addInflow (3-conjugate-gradients/Fluid.cpp:167-184; step 1
+// sets the value itself without the pulse, 1-matrixless/Fluid.cpp:141-151).  The x
 // bound is the quantity's height (as in the reference) and cells are
 // addressed by the flat index x + y*w.  When that index can wrap into the next
 // row two rectangle cells may hit one location, so the rectangle is then
 // walked by one thread in the reference's order.
 template <typename F>
 __device__ __forceinline__ void inflow_body(const Quant<F> &Q, int P, double hx, double x0, double y0, double x1,
-                                            double y1, double val) {
+                                            double y1, double val, bool flat = false) {
     int ix0 = (int)(x0 / hx - Q.ox);
     int iy0 = (int)(y0 / hx - Q.oy);
     int ix1 = (int)(x1 / hx - Q.ox);
@@ -44,7 +45,7 @@ __device__ __forceinline__ void inflow_body(const Quant<F> &Q, int P, double hx,
         int x = xlo + i % nx, y = ylo + i / nx;
         double l = length2((2.0 * (x + 0.5) * hx - (x0 + x1)) / (x1 - x0),
                            (2.0 * (y + 0.5) * hx - (y0 + y1)) / (y1 - y0));
-        double vi = cubic_pulse(l) * val;
+        double vi = flat ? val : cubic_pulse(l) * val;
         long flat = (long)x + (long)y * Q.w;
         if (flat >= n) continue;
         int fx = (int)(flat % Q.w), fy = (int)(flat / Q.w);
@@ -54,8 +55,8 @@ __device__ __forceinline__ void inflow_body(const Quant<F> &Q, int P, double hx,
 }
 template <typename F>
 __global__ void inflow_kernel(Quant<F> Q, int P, double hx, double x0, double y0, double x1, double y1,
-                              double val) {
-    inflow_body(Q, P, hx, x0, y0, x1, y1, val);
+                              double val, bool flat) {
+    inflow_body(Q, P, hx, x0, y0, x1, y1, val, flat);
 }
 
 // ------------------------------------------------------------ solid fields
@@ -248,7 +249,7 @@ __device__ __forceinline__ void assemble_body(const Scene<F> &S, double dt, int 
     const size_t k = S.sd.slot(x, y);  // pressure-system arrays are strip-diagonal
     const int var = S.variant;
     const uint8_t *cell = S.q[0].cell;
-    const bool plain = var == 3;
+    const bool plain = var <= 3;
     const bool fl = plain || cell[c] == CELL_FLUID;
     const double alpha = (S.rho_soot - S.rho_air) / S.rho_air;
     const F *U = S.q[2].src, *V = S.q[3].src;
@@ -380,16 +381,16 @@ __device__ __forceinline__ void apply_pressure_body(const Scene<F> &S, double dt
         if (fx > w || fy >= h) return;
         size_t f = fx + (size_t)fy * P;
         F *u = S.q[2].src + f;
-        if (var == 3 && (fx == 0 || fx == w)) {
+        if (var <= 3 && (fx == 0 || fx == w)) {
             *u = (F)0.0;
             return;
         }
         double val = (double)*u;
-        if (fx > 0 && (var == 3 || cell[f - 1] == CELL_FLUID)) {
+        if (fx > 0 && (var <= 3 || cell[f - 1] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx - 1, fy)];
             val += (var >= 7) ? scale * pv / (double)S.udens[f] : scale * pv;
         }
-        if (fx < w && (var == 3 || cell[f] == CELL_FLUID)) {
+        if (fx < w && (var <= 3 || cell[f] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx, fy)];
             val -= (var >= 7) ? scale * pv / (double)S.udens[f] : scale * pv;
         }
@@ -398,16 +399,16 @@ __device__ __forceinline__ void apply_pressure_body(const Scene<F> &S, double dt
         if (fx >= w || fy > h) return;
         size_t f = fx + (size_t)fy * P;
         F *v = S.q[3].src + f;
-        if (var == 3 && (fy == 0 || fy == h)) {
+        if (var <= 3 && (fy == 0 || fy == h)) {
             *v = (F)0.0;
             return;
         }
         double val = (double)*v;
-        if (fy > 0 && (var == 3 || cell[f - P] == CELL_FLUID)) {
+        if (fy > 0 && (var <= 3 || cell[f - P] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx, fy - 1)];
             val += (var >= 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
         }
-        if (fy < h && (var == 3 || cell[f] == CELL_FLUID)) {
+        if (fy < h && (var <= 3 || cell[f] == CELL_FLUID)) {
             double pv = (double)S.p[S.sd.slot(fx, fy)];
             val -= (var >= 7) ? scale * pv / (double)S.vdens[f] : scale * pv;
         }
@@ -720,6 +721,14 @@ __device__ __forceinline__ void advect_body(const Scene<F> &S, double dt, const 
     const double fdt = dt;
     double x = ix + Q.ox;
     double y = iy + Q.oy;
+    if (S.variant == 1) {  // euler + lerp (1-matrixless/Fluid.cpp:65-73, 124-138)
+        F uVel = q_lerp(U.src, P, U.w, U.h, uox, uoy, F(x), F(y)) / hx;
+        F vVel = q_lerp(V.src, P, V.w, V.h, vox, voy, F(x), F(y)) / hx;
+        x -= (double)uVel * fdt;
+        y -= (double)vVel * fdt;
+        Q.dst[idx] = q_lerp(Q.src, P, Q.w, Q.h, F(Q.ox), F(Q.oy), F(x), F(y));
+        return;
+    }
     {
         F firstU = q_lerp(U.src, P, U.w, U.h, uox, uoy, F(x), F(y)) / hx;
         F firstV = q_lerp(V.src, P, V.w, V.h, vox, voy, F(x), F(y)) / hx;
@@ -821,7 +830,7 @@ inline dim3 grid2(int nx, int ny, int nz, dim3 b) {
 template <typename F>
 void launch_inflow(const Scene<F> &S, int qi, double x0, double y0, double x1, double y1, double val,
                    cudaStream_t st) {
-    inflow_kernel<F><<<1, 256, 0, st>>>(S.q[qi], S.P, S.hx, x0, y0, x1, y1, val);
+    inflow_kernel<F><<<1, 256, 0, st>>>(S.q[qi], S.P, S.hx, x0, y0, x1, y1, val, S.variant == 1);
 }
 
 template <typename F>

@@ -2,7 +2,7 @@
 // field transfer behind the C ABI (include/ifluids.h).  No kernels live here.
 //
 // update() follows FluidSolver::update of the reference step selected by the
-// variant (3-conjugate-gradients/Fluid.cpp:433-447, 4-solid-boundaries/Fluid.cpp:869-895,
+// variant (1-matrixless/Fluid.cpp:284-297, 3-conjugate-gradients/Fluid.cpp:433-447, 4-solid-boundaries/Fluid.cpp:869-895,
 // 5-curved-boundaries/Fluid.cpp:927-953, 6-heat/Fluid.cpp:966-1006,
 // 7-variable-density/Fluid.cpp:995-1034, 8-flip/Fluid.cpp:1350-1413); buildRhs/computeDensities/
 // buildPressureMatrix run as one assembly launch and buildPreconditioner +
@@ -160,9 +160,15 @@ class SolverImpl final : public SolverBase {
         case IFL_PH_DENSITIES:
             if (var >= IFL_VARDENS) assemble(dt, ASM_DENS);
             break;
-        case IFL_PH_MATRIX: assemble(dt, ASM_MATRIX); break;
-        case IFL_PH_PRECON: return pcg(PCG_FACTOR, false);
-        case IFL_PH_PROJECT: return pcg(PCG_SOLVE, false);
+        case IFL_PH_MATRIX:
+            if (var > IFL_GS) assemble(dt, ASM_MATRIX);
+            break;
+        case IFL_PH_PRECON:
+            if (var > IFL_GS) return pcg(PCG_FACTOR, false);
+            break;
+        case IFL_PH_PROJECT:
+            if (var <= IFL_GS) return gauss_seidel(dt);
+            return pcg(PCG_SOLVE, false);
         case IFL_PH_APPLY_P: {
             int t = tbegin(IFL_K_FACES);
             launch_apply_pressure<F>(S_, dt, stream_);
@@ -207,6 +213,11 @@ class SolverImpl final : public SolverBase {
             static const int tail[] = {IFL_PH_APPLY_P, IFL_PH_EXTRAP_DUV, IFL_PH_BC, IFL_PH_G2P, IFL_PH_PADVECT};
             for (int ph : tail)
                 if ((e = run_phase(ph, dt))) return e;
+        } else if (var <= IFL_GS) {  // 1-matrixless/Fluid.cpp:284-297
+            assemble(dt, ASM_RHS);
+            if ((e = gauss_seidel(dt))) return e;
+            if ((e = run_phase(IFL_PH_APPLY_P, dt))) return e;
+            if ((e = run_phase(IFL_PH_ADVECT, dt))) return e;
         } else if (var == IFL_PLAIN) {
             assemble(dt, ASM_RHS | ASM_MATRIX);
             if ((e = pcg(PCG_FACTOR | PCG_SOLVE, false))) return e;
@@ -586,6 +597,16 @@ class SolverImpl final : public SolverBase {
         cudaError_t e = launch_pcg<F>(S_, scratch_, cfg, stream_, &G);
         tend(t);
         if (check(e, "pcg launch")) return IFL_ERR_CUDA;
+        launches_++;
+        return IFL_OK;
+    }
+
+    // project() of steps 1-2: Gauss-Seidel sweeps on p, which persists between steps.
+    int gauss_seidel(double dt) {
+        int t = tbegin(IFL_K_PCG);
+        cudaError_t e = launch_gs<F>(S_, scratch_, dt, prm_.max_iter_pressure, pinned_, stream_);
+        tend(t);
+        if (check(e, "gauss-seidel launch")) return IFL_ERR_CUDA;
         launches_++;
         return IFL_OK;
     }

@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(_HERE, "libifluids.so")
 
 # include/ifluids.h constants
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5
+GS_EULER, GS = 1, 2
 PLAIN, SOLID, CURVED, HEAT, VARDENS, FLIP = 3, 4, 5, 6, 7, 8
 FP64, FP32 = 0, 1
 DT_F64, DT_F32, DT_U8 = 0, 1, 2
@@ -272,7 +273,8 @@ class FluidSolver:
 
     Positional forms follow the reference constructors::
 
-        FluidSolver(w, h, density)                          # 3-conjugate-gradients
+        FluidSolver(w, h, density)                          # 3-conjugate-gradients (variant=1:
+                                                            #   1-matrixless, 2: 2-better-advection)
         FluidSolver(w, h, density, bodies)                  # 4-solid-boundaries (variant=5: curved)
         FluidSolver(w, h, rhoAir, rhoSoot, diffusion, bodies)  # 7-variable-density (variant=6: heat,
                                                                #   variant=8: 8-flip, FP64 only)

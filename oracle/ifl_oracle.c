@@ -5,7 +5,7 @@
  * CPU baseline in bench.py.  Never part of the product path.
  *
  * A restatement, in this project's own C, of FluidSolver::update from the
- * reference tutorial steps 3-8 (tunabrain/incremental-fluids).  Each function
+ * reference tutorial steps 1-8 (tunabrain/incremental-fluids).  Each function
  * cites the reference lines whose arithmetic it follows.  The floating-point
  * operation order of every cell update is kept identical to the reference so
  * that results are bit-identical when both sides are compiled with
@@ -328,6 +328,18 @@ static void back_project(const ifo_solver *s, const quantity *q, double *px, dou
 static void q_advect(const ifo_solver *s, quantity *q, double dt) {
     const quantity *u = &s->q[IFO_QU], *v = &s->q[IFO_QV];
     int solid = s->variant >= IFO_SOLID;
+    if (s->variant == IFO_GS_EULER) {  /* euler + lerp: 1-matrixless/Fluid.cpp:65-73, 124-138 */
+        for (int iy = 0, idx = 0; iy < q->h; iy++)
+            for (int ix = 0; ix < q->w; ix++, idx++) {
+                double x = ix + q->ox, y = iy + q->oy;
+                double uVel = q_lerp(u, x, y) / q->hx;
+                double vVel = q_lerp(v, x, y) / q->hx;
+                x -= uVel * dt;
+                y -= vVel * dt;
+                q->dst[idx] = q_lerp(q, x, y);
+            }
+        return;
+    }
     for (int iy = 0, idx = 0; iy < q->h; iy++) {
         for (int ix = 0; ix < q->w; ix++, idx++) {
             if (solid && q->cell[idx] != CELL_FLUID) continue;
@@ -343,6 +355,7 @@ static void q_advect(const ifo_solver *s, quantity *q, double dt) {
 /* addInflow: 3-conjugate-gradients/Fluid.cpp:167-184.  The x loop bound is
  * the grid height as in the reference; cells are addressed by the flat index
  * x + y*w, and a flat index beyond the array is skipped. */
+static void q_add_inflow_flat(quantity *q, double x0, double y0, double x1, double y1, double val);
 static void q_add_inflow(quantity *q, double x0, double y0, double x1, double y1, double val) {
     int ix0 = (int)(x0 / q->hx - q->ox);
     int iy0 = (int)(y0 / q->hx - q->oy);
@@ -359,6 +372,22 @@ static void q_add_inflow(quantity *q, double x0, double y0, double x1, double y1
             if (fabs(q->src[flat]) < fabs(vi)) q->src[flat] = vi;
         }
     }
+}
+
+/* Step 1's addInflow sets the value itself, without the pulse
+ * (1-matrixless/Fluid.cpp:141-151); same bounds and flat-index rule. */
+static void q_add_inflow_flat(quantity *q, double x0, double y0, double x1, double y1, double val) {
+    int ix0 = (int)(x0 / q->hx - q->ox);
+    int iy0 = (int)(y0 / q->hx - q->oy);
+    int ix1 = (int)(x1 / q->hx - q->ox);
+    int iy1 = (int)(y1 / q->hx - q->oy);
+    long n = (long)q->w * q->h;
+    for (int y = imax(iy0, 0); y < imin(iy1, q->h); y++)
+        for (int x = imax(ix0, 0); x < imin(ix1, q->h); x++) {
+            long flat = (long)x + (long)y * q->w;
+            if (flat >= n) continue;
+            if (fabs(q->src[flat]) < fabs(val)) q->src[flat] = val;
+        }
 }
 
 /* fillSolidFields: 4-solid-boundaries/Fluid.cpp:449-480 (binary cells),
@@ -451,7 +480,7 @@ static void q_extrapolate(ifo_solver *s, quantity *q) {
 
 ifo_solver *ifo_create(int variant, int w, int h, double density_air,
                        double density_soot, double diffusion) {
-    if (variant < IFO_PLAIN || variant > IFO_FLIP || w < 2 || h < 2) return NULL;
+    if (variant < IFO_GS_EULER || variant > IFO_FLIP || w < 2 || h < 2) return NULL;
     ifo_solver *s = calloc(1, sizeof(ifo_solver));
     s->variant = variant;
     s->w = w;
@@ -533,6 +562,12 @@ void ifo_add_inflow(ifo_solver *s, double x, double y, double w, double h,
         }
         return;
     }
+    if (s->variant == IFO_GS_EULER) {
+        q_add_inflow_flat(&s->q[IFO_QD], x, y, x + w, y + h, d);
+        q_add_inflow_flat(&s->q[IFO_QU], x, y, x + w, y + h, u);
+        q_add_inflow_flat(&s->q[IFO_QV], x, y, x + w, y + h, v);
+        return;
+    }
     q_add_inflow(&s->q[IFO_QD], x, y, x + w, y + h, d);
     if (s->variant >= IFO_HEAT) q_add_inflow(&s->q[IFO_QT], x, y, x + w, y + h, t);
     q_add_inflow(&s->q[IFO_QU], x, y, x + w, y + h, u);
@@ -550,7 +585,7 @@ static void build_rhs(ifo_solver *s) {
     int w = s->w, h = s->h;
     for (int y = 0, idx = 0; y < h; y++) {
         for (int x = 0; x < w; x++, idx++) {
-            if (s->variant == IFO_PLAIN) {
+            if (s->variant <= IFO_PLAIN) {  /* 1-matrixless/Fluid.cpp:176-186 as well */
                 s->r[idx] = -scale * (SU(x + 1, y) - SU(x, y) + SV(x, y + 1) - SV(x, y));
             } else if (s->variant == IFO_SOLID) {
                 if (D->cell[idx] == CELL_FLUID)
@@ -1220,6 +1255,45 @@ void ifo_flip_init(ifo_solver *s) {
 uint32_t ifo_rng_state(const ifo_solver *s) { return s->rng; }
 void ifo_set_rng_state(ifo_solver *s, uint32_t state) { s->rng = state; }
 
+/* project() of steps 1-2: lexicographic Gauss-Seidel on the implicit
+ * five-point stencil, walls solid, p kept from the previous step (zeroed only
+ * by the constructor), stop when the largest change of a sweep is below 1e-5
+ * (1-matrixless/Fluid.cpp:192-240). */
+static void gs_project(ifo_solver *s, int limit, double dt) {
+    const int w = s->w, h = s->h;
+    const double scale = dt / (s->rho_air * s->hx * s->hx);
+    double *p = s->p;
+    const double *r = s->r;
+    double maxDelta = 0.0;
+    int sweeps = 0;
+    for (int it = 0; it < limit; it++) {
+        maxDelta = 0.0;
+        for (int y = 0; y < h; y++)
+            for (int x = 0; x < w; x++) {
+                int idx = x + y * w;
+                double diag = 0.0, off = 0.0;
+                if (x > 0) { diag += scale; off -= scale * p[idx - 1]; }
+                if (y > 0) { diag += scale; off -= scale * p[idx - w]; }
+                if (x < w - 1) { diag += scale; off -= scale * p[idx + 1]; }
+                if (y < h - 1) { diag += scale; off -= scale * p[idx + w]; }
+                double np_ = (r[idx] - off) / diag;
+                maxDelta = smax(maxDelta, fabs(p[idx] - np_));
+                p[idx] = np_;
+            }
+        sweeps = it + 1;
+        if (maxDelta < 1e-5) {
+            s->st_pressure.iterations = sweeps;
+            s->st_pressure.status = IFO_PCG_CONVERGED;
+            s->st_pressure.max_error = maxDelta;
+            return;
+        }
+    }
+    s->st_pressure.iterations = limit;
+    s->st_pressure.status = IFO_PCG_CAP;
+    s->st_pressure.max_error = maxDelta;
+    (void)sweeps;
+}
+
 void ifo_phase(ifo_solver *s, int phase, double dt) {
     int v = s->variant;
     switch (phase) {
@@ -1239,9 +1313,12 @@ void ifo_phase(ifo_solver *s, int phase, double dt) {
     case IFO_PH_BC: if (v >= IFO_SOLID) set_bc(s); break;
     case IFO_PH_RHS: build_rhs(s); break;
     case IFO_PH_DENSITIES: if (v >= IFO_VARDENS) compute_densities(s); break;
-    case IFO_PH_MATRIX: build_matrix(s, dt); break;
-    case IFO_PH_PRECON: build_precon(s); break;
-    case IFO_PH_PROJECT: project(s, v == IFO_PLAIN ? 600 : 2000, s->pinned, &s->st_pressure); break;
+    case IFO_PH_MATRIX: if (v > IFO_GS) build_matrix(s, dt); break;
+    case IFO_PH_PRECON: if (v > IFO_GS) build_precon(s); break;
+    case IFO_PH_PROJECT:
+        if (v <= IFO_GS) gs_project(s, 600, dt);
+        else project(s, v == IFO_PLAIN ? 600 : 2000, s->pinned, &s->st_pressure);
+        break;
     case IFO_PH_APPLY_P: apply_pressure(s, dt); break;
     case IFO_PH_EXTRAP_DUV:
         if (v < IFO_SOLID) break;
@@ -1272,10 +1349,17 @@ void ifo_phase(ifo_solver *s, int phase, double dt) {
     }
 }
 
-/* FluidSolver::update: 3-conjugate-gradients/Fluid.cpp:433-447,
+/* FluidSolver::update: 1-matrixless/Fluid.cpp:284-297, 3-conjugate-gradients/Fluid.cpp:433-447,
  * 4-solid-boundaries/Fluid.cpp:869-895, 5-curved-boundaries/Fluid.cpp:927-953,
  * 6-heat/Fluid.cpp:966-1006, 7-variable-density/Fluid.cpp:995-1034 */
 void ifo_update(ifo_solver *s, double dt) {
+    if (s->variant <= IFO_GS) {  /* 1-matrixless/Fluid.cpp:284-297 */
+        ifo_phase(s, IFO_PH_RHS, dt);
+        ifo_phase(s, IFO_PH_PROJECT, dt);
+        ifo_phase(s, IFO_PH_APPLY_P, dt);
+        ifo_phase(s, IFO_PH_ADVECT, dt);
+        return;
+    }
     if (s->variant == IFO_PLAIN) {
         ifo_phase(s, IFO_PH_RHS, dt);
         ifo_phase(s, IFO_PH_MATRIX, dt);

@@ -2,7 +2,7 @@
  * ifl_oracle.h - CPU oracle for the incremental-fluids per-step hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
- * solver's arithmetic (tunabrain/incremental-fluids, tutorial steps 3-8), used
+ * solver's arithmetic (tunabrain/incremental-fluids, tutorial steps 1-8), used
  * by the tests as the parity checker and by bench.py as the timed CPU
  * baseline.  The CUDA product path never links, loads or calls it.
  *
@@ -25,6 +25,10 @@ extern "C" {
 
 /* Variant = reference tutorial step whose FluidSolver::update is restated. */
 enum {
+    IFO_GS_EULER = 1, /* 1-matrixless: Gauss-Seidel solve, forward Euler + bilinear
+                         advection, flat inflow                              */
+    IFO_GS = 2,       /* 2-better-advection: Gauss-Seidel solve, step 3's
+                         advection and inflow                                */
     IFO_PLAIN = 3,    /* 3-conjugate-gradients */
     IFO_SOLID = 4,    /* 4-solid-boundaries    */
     IFO_CURVED = 5,   /* 5-curved-boundaries   */
@@ -76,7 +80,8 @@ enum {
 /* Particle arrays of step 8 (ifo_particles). */
 enum { IFO_P_X = 0, IFO_P_Y = 1, IFO_P_D = 2, IFO_P_T = 3, IFO_P_U = 4, IFO_P_V = 5 };
 
-/* PCG outcome. */
+/* Solve outcome (the PCG of steps 3-8; the Gauss-Seidel solve of steps 1-2
+ * reports sweeps made, CONVERGED or CAP, and the last maximum change). */
 enum { IFO_PCG_CONVERGED = 0, IFO_PCG_INITIAL = 1, IFO_PCG_CAP = 2 };
 
 typedef struct ifo_solver ifo_solver;

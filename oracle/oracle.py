@@ -3,7 +3,7 @@
 Two back-ends with one interface:
 
 * ``OracleSolver`` drives ``oracle/liboracle.so``, the plain-C restatement of
-  the reference solver (tutorial steps 3-8).  It builds on any host and is the
+  the reference solver (tutorial steps 1-8).  It builds on any host and is the
   parity checker the GPU tests use, and the CPU baseline bench.py times.
 * ``RefSolver`` drives ``oracle/_ref/libref<step>.so``: the reference's own
   ``Fluid.cpp`` compiled unmodified (see ``oracle/ref_shim.cpp``).  It exists
@@ -27,6 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
+GS_EULER, GS = 1, 2
 PLAIN, SOLID, CURVED, HEAT, VARDENS, FLIP = 3, 4, 5, 6, 7, 8
 QD, QT, QU, QV = 0, 1, 2, 3
 A_SRC, A_DST, A_PHI, A_VOLUME, A_NORMALX, A_NORMALY = 0, 1, 2, 3, 4, 5
@@ -118,7 +119,7 @@ def _particle_view(ptr, n):
 
 
 class OracleSolver:
-    """The C restatement of FluidSolver (steps 3-8), FP64, zero-initialised."""
+    """The C restatement of FluidSolver (steps 1-8), FP64, zero-initialised."""
 
     def __init__(self, variant: int, w: int, h: int, density: float = 0.1,
                  density_soot: float = 1.0, diffusion: float = 0.01):

@@ -112,7 +112,7 @@ void zero_quantity(FluidQuantity *q) {
 void build(RefScene *s) {
     const int w = s->w, h = s->h;
     const double rho_air = s->rho_air, rho_soot = s->rho_soot, diffusion = s->diffusion;
-#if REF_STEP == 3
+#if REF_STEP <= 3
     (void)rho_soot; (void)diffusion;
     s->solver = new FluidSolver(w, h, rho_air);
 #elif REF_STEP <= 5
@@ -129,8 +129,11 @@ void build(RefScene *s) {
 #if REF_STEP >= 6
     zero_quantity(f->_t);
 #endif
-    zero(f->_r, n); zero(f->_p, n); zero(f->_z, n); zero(f->_s, n);
+    zero(f->_r, n);
+#if REF_STEP >= 3
+    zero(f->_p, n); zero(f->_z, n); zero(f->_s, n);
     zero(f->_precon, n); zero(f->_aDiag, n); zero(f->_aPlusX, n); zero(f->_aPlusY, n);
+#endif
 #if REF_STEP >= 7
     zero(f->_uDensity, (size_t)(w + 1) * h);
     zero(f->_vDensity, (size_t)w * (h + 1));
@@ -250,12 +253,14 @@ double *ref_array(void *p, int qid, int which, int *w, int *h) {
         switch (which) {
         case 16: return f->_r;
         case 17: return f->_p;
+#if REF_STEP >= 3
         case 18: return f->_z;
         case 19: return f->_s;
         case 20: return f->_precon;
         case 21: return f->_aDiag;
         case 22: return f->_aPlusX;
         case 23: return f->_aPlusY;
+#endif
 #if REF_STEP >= 7
         case 24: *w = s->w + 1; return f->_uDensity;
         case 25: *h = s->h + 1; return f->_vDensity;

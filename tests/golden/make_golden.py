@@ -32,6 +32,8 @@ BALL = (1, 0.3, 0.45, 0.2, 0.2, 0.0, 0.05, 0.0, 0.8)
 
 # name, variant, w, h, dt, steps, inflow (x, y, w, h, d, t, u, v), bodies
 SCENES = [
+    ("gs1_32", 1, 32, 32, 0.005, 6, (0.45, 0.2, 0.1, 0.05, 1.0, 0.0, 0.0, 3.0), []),
+    ("gs2_32", 2, 32, 32, 0.005, 6, (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.0, 3.0), []),
     ("plain_32", 3, 32, 32, 0.005, 6, (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.0, 3.0), []),
     ("plain_40x24", 3, 40, 24, 0.005, 6, (0.3, 0.2, 0.3, 0.1, 1.0, 0.0, 0.5, 3.0), []),
     ("solid_32", 4, 32, 32, 0.005, 6, (0.45, 0.2, 0.15, 0.06, 1.0, 0.0, 0.0, 3.0), [SPIN, BALL]),

@@ -48,7 +48,7 @@ def test_default_params_follow_reference(ifl, lib):
     assert p.density_soot == 1.0 and p.diffusion == 0.01
 
 
-@pytest.mark.parametrize("field,value", [("variant", 2), ("variant", 9), ("w", 1), ("h", 0),
+@pytest.mark.parametrize("field,value", [("variant", 0), ("variant", 9), ("w", 1), ("h", 0),
                                          ("precision", 5), ("density_air", 0.0), ("max_iter_heat", -1)])
 def test_create_rejects_bad_parameters_without_touching_the_gpu(ifl, lib, field, value):
     p = ifl.Params()

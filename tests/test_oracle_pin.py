@@ -61,6 +61,9 @@ SPIN = (0, 0.55, 0.55, 0.3, 0.12, 0.7, 0.0, 0.0, 1.0)
 BALL = (1, 0.3, 0.45, 0.2, 0.2, 0.0, 0.1, 0.0, 1.0)
 
 STEPWISE = [
+    (1, 48, 40, 5, (0.45, 0.2, 0.1, 0.05, 1.0, 0.0, 0.0, 3.0), []),    # Gauss-Seidel, Euler + lerp
+    (1, 128, 128, 3, (0.45, 0.2, 0.1, 0.01, 1.0, 0.0, 0.0, 3.0), []),  # 1-matrixless main() scene
+    (2, 40, 56, 5, (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.0, 3.0), []),   # Gauss-Seidel, RK3 + cerp
     (3, 48, 48, 6, (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.0, 3.0), []),
     (3, 40, 56, 6, (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 0.5, 3.0), []),
     (3, 56, 36, 6, (0.2, 0.2, 0.6, 0.1, 1.0, 0.0, -1.0, 2.0), []),  # wide rectangle on a wide grid
@@ -73,7 +76,7 @@ STEPWISE = [
 ]
 
 
-@pytest.mark.skipif(not all(O.ref_available(v) for v in (3, 4, 5, 6, 7)),
+@pytest.mark.skipif(not all(O.ref_available(v) for v in (1, 2, 3, 4, 5, 6, 7)),
                     reason="reference not compiled here (make -C oracle ref)")
 @pytest.mark.parametrize("case", STEPWISE, ids=[f"v{c[0]}-{c[1]}x{c[2]}" for c in STEPWISE])
 def test_oracle_matches_reference_every_step(case):
@@ -97,7 +100,9 @@ def test_oracle_matches_reference_every_step(case):
                 assert np.array_equal(a.array(q, O.A_NORMALX), b.array(q, O.A_NORMALX))
             if variant >= O.CURVED:
                 assert np.array_equal(a.array(q, O.A_VOLUME), b.array(q, O.A_VOLUME))
-        for which in (O.A_R, O.A_P, O.A_PRECON, O.A_ADIAG, O.A_APLUSX, O.A_APLUSY):
+        solver_arrays = (O.A_R, O.A_P) + ((O.A_PRECON, O.A_ADIAG, O.A_APLUSX, O.A_APLUSY)
+                                          if variant >= O.PLAIN else ())
+        for which in solver_arrays:
             assert np.array_equal(a.array(0, which), b.array(0, which)), (step, which)
         if variant == O.VARDENS:
             assert np.array_equal(a.array(0, O.A_UDENS), b.array(0, O.A_UDENS))
