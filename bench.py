@@ -26,7 +26,9 @@ cell-steps/s = sum of w*h over the scenes x steps per second.
 bodies) instead.  --workload flip: step 8 (FLIP particles) on the reference
 main()'s own scene (rotated box, its fixed inflow, rhoAir 0.1, rhoSoot 0.25,
 diffusion 0.01, dt 0.0025) at --size (128, the reference's grid), FP64,
-one handle; its CPU baseline is the oracle's step-8 restatement.  --impl reference times the reference's CPU algorithm (the
+one handle; its CPU baseline is the oracle's step-8 restatement.
+--workload gs [--gs-variant 1|2]: the Gauss-Seidel steps on their reference
+main() scene (128^2 by default), FP64, one handle.  --impl reference times the reference's CPU algorithm (the
 oracle port; the reference's own sources are not present on the GPU host) on
 the same workload.  Multi-GPU (torchrun): each rank runs an independent
 replica ("replicas only": scenes do not exchange data), barrier + max over
@@ -364,22 +366,13 @@ def cpu_baseline_flip(n: int, steps: int):
             "seconds": round(t, 3), "particles": s.particle_count()}
 
 
-def run_flip(args, local_rank):
+def time_handle(args, local_rank, make, step, cells):
+    """Device time of K steps of one handle (CUDA events on its stream, L2
+    flushed between steps), then an identical twin through the public API
+    with the density read back into pinned host memory every step."""
     import torch
-    import ifluids as ifl
-
-    torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    n = args.size
-
-    def make():
-        box = ifl.SolidBox(*FLIP_BOX)
-        return ifl.FluidSolver(n, n, *FLIP_RHO, [box], variant=ifl.FLIP, device=local_rank)
-
-    def step(s):
-        s.addInflow(*FLIP_INFLOW)
-        s.update(FLIP_DT)
-
+    torch.cuda.set_device(local_rank)
     g, ge = make(), make()
     stream = torch.cuda.ExternalStream(g.stream, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -408,19 +401,40 @@ def run_flip(args, local_rank):
     launches = g.launch_count() - launches0
     kms, klaunch, iters = g.timing()
     g.set_timing(False)
-    (pit, pst, _), (hit, _, _), flags = g.stats()
-    if flags & 1:
+    stats = g.stats()
+    if stats[2] & 1:
         raise RuntimeError("device-side wait timed out during the benchmark")
-    particles = g.particle_count()
-
-    host_d = torch.empty((n, n), dtype=torch.float64, pin_memory=True).numpy()
+    n, m = g.shape(0)
+    host_d = torch.empty((n, m), dtype=torch.float64, pin_memory=True).numpy()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step(ge)
         ge.read_field("d", dtype=host_d.dtype, out=host_d)
     e2e_s = time.perf_counter() - t0
     ge.close()
+    return {"g": g, "dev_ms": dev_ms, "step_ms": step_ms, "launches": launches, "kms": kms, "klaunch": klaunch,
+            "iters": iters, "stats": stats, "clocks": clk.summary(),
+            "e2e": {"value": cells * args.steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 96,
+                    "d2h_bytes_per_step": cells * 8}}
+
+
+def run_flip(args, local_rank):
+    import ifluids as ifl
+    n = args.size
+
+    def make():
+        box = ifl.SolidBox(*FLIP_BOX)
+        return ifl.FluidSolver(n, n, *FLIP_RHO, [box], variant=ifl.FLIP, device=local_rank)
+
+    def step(s):
+        s.addInflow(*FLIP_INFLOW)
+        s.update(FLIP_DT)
+
     cells = n * n
+    T = time_handle(args, local_rank, make, step, cells)
+    g, kms = T["g"], T["kms"]
+    (pit, _, _), (hit, _, _), _ = T["stats"]
+    particles = g.particle_count()
     # particle kernels: algorithmic bytes per particle and step (FP64 state of
     # x, y and four carried values = 48 B): transfer reads x, y, the carried
     # value of the grid's quantities once per grid kind and writes a bucket
@@ -438,13 +452,70 @@ def run_flip(args, local_rank):
             "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()},
             "pcg_iterations_last_step": [pit, hit]}
     g.close()
-    return {"value": cells * args.steps / (dev_ms / 1e3), "ms_per_step": dev_ms / args.steps,
-            "e2e": {"value": cells * args.steps / e2e_s, "unit": METRIC, "h2d_bytes_per_step": 96,
-                    "d2h_bytes_per_step": cells * 8},
-            "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(), "fp64_dropin": None,
-            "particles": particles,
-            "particle_steps_per_s": particles * args.steps / (dev_ms / 1e3),
-            "latency_ms": {"p50": round(statistics.median(step_ms), 3), "max": round(max(step_ms), 3)}}
+    dev_ms = T["dev_ms"]
+    return {"value": cells * args.steps / (dev_ms / 1e3), "ms_per_step": dev_ms / args.steps, "e2e": T["e2e"],
+            "roofline": roof, "gpu_launches": T["launches"], "clocks": T["clocks"], "fp64_dropin": None,
+            "particles": particles, "particle_steps_per_s": particles * args.steps / (dev_ms / 1e3),
+            "latency_ms": {"p50": round(statistics.median(T["step_ms"]), 3), "max": round(max(T["step_ms"]), 3)}}
+
+
+# ---------------------------------------------------- Gauss-Seidel steps 1-2
+GS_INFLOW = {1: (0.45, 0.2, 0.1, 0.01, 1.0, 0.0, 3.0),      # 1-matrixless/Fluid.cpp:353
+             2: (0.45, 0.2, 0.15, 0.03, 1.0, 0.0, 3.0)}     # 2-better-advection/Fluid.cpp:370
+GS_DT = 0.005
+
+
+def cpu_baseline_gs(variant: int, n: int, steps: int):
+    """The oracle's step-1/2 restatement (single thread, as the reference) on the same scene."""
+    from oracle import oracle as O
+    s = O.OracleSolver(variant, n, n)
+    d, u, v = GS_INFLOW[variant][4:]
+    x, y, w, h = GS_INFLOW[variant][:4]
+    s.add_inflow(x, y, w, h, d, 0.0, u, v)
+    s.update(GS_DT)
+    t0 = time.perf_counter()
+    sweeps = 0
+    for _ in range(steps):
+        s.add_inflow(x, y, w, h, d, 0.0, u, v)
+        s.update(GS_DT)
+        sweeps += s.stats()[0][0]
+    t = time.perf_counter() - t0
+    return {"value": n * n * steps / t, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{steps} update() of the {n}x{n} step-{variant} scene after its first step "
+                      f"({sweeps} Gauss-Seidel sweeps), FP64 oracle (bit-identical to the reference)",
+            "seconds": round(t, 3)}
+
+
+def run_gs(args, local_rank):
+    import ifluids as ifl
+    n, variant = args.size, args.gs_variant
+
+    def make():
+        return ifl.FluidSolver(n, n, 0.1, variant=variant, device=local_rank)
+
+    def step(s):
+        s.addInflow(*GS_INFLOW[variant])
+        s.update(GS_DT)
+
+    cells = n * n
+    T = time_handle(args, local_rank, make, step, cells)
+    kms, klaunch, iters = T["kms"], T["klaunch"], T["iters"]
+    # Gauss-Seidel sweep: reads r, p (own, right, upper) and writes p: 24 B per
+    # cell per sweep at the lower bound (p and r once each, p written once)
+    gs_ms = kms.get("pcg", 0.0)
+    peak, peak_kind = load_peaks()
+    gs_bytes = 24.0 * cells * iters
+    achieved = gs_bytes / (gs_ms / 1e3) / 1e9 if gs_ms > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": "gs_kernel", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": f"of {peak_kind}", "traffic": None,
+            "sweeps_per_step": round(iters / args.steps, 1),
+            "us_per_sweep": round(1e3 * gs_ms / max(1, iters), 2),
+            "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kms.items()}}
+    T["g"].close()
+    dev_ms = T["dev_ms"]
+    return {"value": cells * args.steps / (dev_ms / 1e3), "ms_per_step": dev_ms / args.steps, "e2e": T["e2e"],
+            "roofline": roof, "gpu_launches": T["launches"], "clocks": T["clocks"], "fp64_dropin": None,
+            "latency_ms": {"p50": round(statistics.median(T["step_ms"]), 3), "max": round(max(T["step_ms"]), 3)}}
 
 
 # ----------------------------------------------------- batched workload
@@ -729,7 +800,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=("batch", "single", "c3", "flip"), default="batch")
+    ap.add_argument("--workload", choices=("batch", "single", "c3", "flip", "gs"), default="batch")
+    ap.add_argument("--gs-variant", type=int, choices=(1, 2), default=1, help="gs workload: tutorial step 1 or 2")
     ap.add_argument("--count", type=int, default=BATCH_COUNT, help="scenes of the batched workload")
     ap.add_argument("--size", type=int, default=0, help="side of the single-scene workload (1024; c3: 2048)")
     ap.add_argument("--precision", choices=("fp32", "fp64"), default="fp32")
@@ -744,7 +816,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
     if not args.size:
-        args.size = {"c3": 2048, "flip": 128}.get(args.workload, 1024)
+        args.size = {"c3": 2048, "flip": 128, "gs": 128}.get(args.workload, 1024)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -763,6 +835,13 @@ def main():
                               f"rotated box, fixed inflow d=1 T=294 K, rhoAir 0.1, rhoSoot 0.25, diffusion 0.01, "
                               f"dt=0.0025",
                   "variant": "8-flip", "grid": [args.size, args.size], "precision_form": "fp64",
+                  "l2": "flushed between timed steps (512 MiB write)", "scene_data": "the reference's own scene"}
+        args.precision = "fp64"
+    elif args.workload == "gs":
+        name = {1: "1-matrixless", 2: "2-better-advection"}[args.gs_variant]
+        config = {"workload": f"Gauss-Seidel step {name} on the reference main's scene {args.size}x{args.size}: "
+                              f"density 0.1, dt=0.005, its inflow, 600-sweep cap",
+                  "variant": name, "grid": [args.size, args.size], "precision_form": "fp64",
                   "l2": "flushed between timed steps (512 MiB write)", "scene_data": "the reference's own scene"}
         args.precision = "fp64"
     elif args.workload == "c3":
@@ -785,6 +864,9 @@ def main():
         if args.workload == "flip":
             cb = cpu_baseline_flip(args.size, max(2, min(args.steps, 20)))
             note = "the reference's step-8 algorithm on one host core (oracle port, bit-identical to it)"
+        elif args.workload == "gs":
+            cb = cpu_baseline_gs(args.gs_variant, args.size, max(2, min(args.steps, 10)))
+            note = "the reference's step-1/2 algorithm on one host core (oracle port, bit-identical to it)"
         elif batch:
             cb = cpu_baseline_batch(procs, steps=1)
             note = ("reference algorithm on the host cores (oracle port of the reference sources, "
@@ -808,6 +890,8 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:  # before any GPU work (spawned pool)
         if args.workload == "flip":
             cb = cpu_baseline_flip(args.size, 10)
+        elif args.workload == "gs":
+            cb = cpu_baseline_gs(args.gs_variant, args.size, 5)
         else:
             cb = cpu_baseline_batch(procs) if batch else cpu_baseline(args.size, 1, procs, args.seed)
     if world > 1:
@@ -816,6 +900,8 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     if args.workload == "flip":
         r = run_flip(args, local_rank)
+    elif args.workload == "gs":
+        r = run_gs(args, local_rank)
     else:
         r = run_batch(args, rank, world, local_rank) if batch else run_gpu(args, rank, world, local_rank)
     if rank != 0:
@@ -831,6 +917,8 @@ def main():
         line["batch"] = r["batch"]
         if args.serve_requests > 0 and world == 1:
             line["serving"] = run_serve(args, local_rank)
+    elif args.workload == "gs":
+        line["latency_ms"] = r["latency_ms"]
     elif args.workload == "flip":
         line["particles"] = r["particles"]
         line["particle_steps_per_s"] = r["particle_steps_per_s"]

@@ -7,23 +7,27 @@
 //
 // A lexicographic sweep is a recurrence on the new values of the left and
 // lower cells and the old values of the right and upper cells - the shape of
-// the MIC(0) forward substitution - so it runs as the same strip wavefront
-// and gives the reference's values (and therefore its sweep counts) exactly:
-// one warp per 32-row strip, lane l on row 32s + l, step d visits the cell
-// x = d - l of every lane (one contiguous strip-diagonal line of p and r).
-// The left value is the lane's own previous result, the lower one comes from
-// lane l - 1 by shuffle, or for lane 0 from the strip below once that strip
-// has published the diagonal (a progress counter per strip in shared
-// memory); the right and upper values are still the previous sweep's.  One
-// CTA holds every strip (h <= 1024); sweeps are separated by a CTA barrier
-// and the maximum change is reduced over the CTA.
+// the MIC(0) forward substitution - so it runs as a strip wavefront and gives
+// the reference's values (and therefore its sweep counts) exactly: one warp
+// per 32-row strip, lane l on row 32s + l, step d visits the cell x = d - l of
+// every lane (one contiguous strip-diagonal line of p and r).  The left value
+// is the lane's own previous result, the lower one comes from lane l - 1 by
+// shuffle, or for lane 0 from the strip below once that strip has published
+// the diagonal; the right and upper values are still the previous sweep's.
+//
+// The work per cell is FP64 (GB300 runs FP64 at 1/64 of the FP32 rate), so
+// every strip gets an SM of its own: one single-warp CTA per strip in a
+// cooperative launch, spread one per SM by a shared-memory reservation.
+// Strips hand over through L2 (progress counters, values read with
+// ld.global.cg), sweeps end at a grid barrier and the maximum change is the
+// maximum of the per-strip maxima, which every CTA forms itself.  Every wait
+// is bounded; a timeout sets the status word and an abort word that releases
+// every other wait.
 #include "ifl_device.cuh"
 
 namespace ifl {
 
 namespace {
-
-constexpr int kGsMaxStrips = 32;
 
 struct GsArgs {
     const double *r;
@@ -34,104 +38,141 @@ struct GsArgs {
     PcgOut *out;
     unsigned *flags;
     unsigned long long *iter_total;
+    unsigned long long *prog;  // S progress counters, then the abort word
+    double *smax;              // S per-strip maxima
+    unsigned *bar;             // grid barrier: arrivals, generation
 };
 
-__global__ void __launch_bounds__(1024) gs_kernel(GsArgs A) {
-    const int lane = threadIdx.x & 31, s = threadIdx.x >> 5;
+__device__ __forceinline__ bool gs_aborted(const GsArgs &A) {
+    return *(const volatile unsigned long long *)(A.prog + A.sd.S) != 0ull;
+}
+__device__ __forceinline__ void gs_abort(const GsArgs &A) {
+    atomicOr(A.flags, FLAG_TIMEOUT);
+    *(volatile unsigned long long *)(A.prog + A.sd.S) = 1ull;
+}
+
+// Grid barrier for the single-warp CTAs (lane 0 arrives for the CTA).
+__device__ __forceinline__ void gs_grid_sync(const GsArgs &A, unsigned &gen) {
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) {
+        __threadfence();
+        const unsigned n = gridDim.x;
+        if (atomicAdd(&A.bar[0], 1u) == n - 1) {
+            atomicExch(&A.bar[0], 0u);
+            __threadfence();
+            atomicExch(&A.bar[1], gen + 1);
+        } else {
+            long long spins = 0;
+            while (ld_volatile(&A.bar[1]) == gen && !gs_aborted(A))
+                if (++spins > kSpinLimit) gs_abort(A);
+        }
+        __threadfence();
+    }
+    gen++;
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32) gs_kernel(GsArgs A) {
+    extern __shared__ unsigned char spread[];  // reserves the SM; never touched
+    (void)spread;
+    const int lane = threadIdx.x, s = blockIdx.x, S = A.sd.S;
     const int w = A.sd.W, h = A.sd.H, D = A.sd.D;
     const int y = s * 32 + lane;
     const bool row = y < h;
     const int steps = w + 31;  // diagonals of one strip per sweep
     const double scale = A.scale;
-    __shared__ volatile long long prog[kGsMaxStrips];
-    __shared__ double s_max[kGsMaxStrips];
-    __shared__ volatile int s_abort;
-    __shared__ int s_stop;
-    if (lane == 0) prog[s] = 0;
-    if (threadIdx.x == 0) s_abort = 0;
-    __syncthreads();
+    // diag of the reference: scale added once per existing neighbour, in order
+    const double d2 = scale + scale, d3 = d2 + scale, d4 = d3 + scale;
+    const double *rs = A.r + (size_t)s * D * 32 + lane;
+    double *ps = A.p + (size_t)s * D * 32 + lane;
+    // lane 31 of strip s-1 at diagonal x + 31, lane 0 of strip s+1 at diagonal x
+    const double *below = s > 0 ? A.p + ((size_t)(s - 1) * D + 31) * 32 + 31 : A.p;
+    const double *above = s + 1 < S ? A.p + (size_t)(s + 1) * D * 32 : A.p;
+    unsigned long long *prog_below = A.prog + (s > 0 ? s - 1 : 0);
+    unsigned gen = 0;
 
     double maxDelta = 0.0;
     int sweeps = 0, status = 2;
     for (int it = 0; it < A.limit; it++) {
-        const long long base = (long long)it * steps;
+        const unsigned long long base = (unsigned long long)it * steps;
+        unsigned long long seen = 0;  // last progress read from the strip below
         double lmax = 0.0, prev = 0.0;
+        // operands of step d, loaded one step ahead (old values nobody writes
+        // before this lane's step d)
+        double pold = 0.0, rr = 0.0, right = 0.0, up = 0.0;
+        auto load = [&](int d) {
+            const int x = d - lane;
+            if (row && x >= 0 && x < w) {
+                const size_t k = (size_t)d * 32;
+                pold = ps[k];
+                rr = rs[k];
+                right = x < w - 1 ? ps[k + 32] : 0.0;
+                if (y < h - 1) up = lane < 31 ? ps[k + 33] : __ldcg(above + (size_t)x * 32);
+            }
+        };
+        load(0);
         for (int d = 0; d < steps; d++) {
             const int x = d - lane;
             const bool act = row && x >= 0 && x < w;
             double down = __shfl_up_sync(0xffffffffu, prev, 1);
             if (lane == 0 && s > 0 && x < w) {
-                // wait for strip s-1 to finish its diagonal x + 31 of this sweep
-                const long long need = base + x + 32;
-                long long spins = 0;
-                while (prog[s - 1] < need && !s_abort) {
-                    if (++spins > kSpinLimit) {
-                        atomicOr(A.flags, FLAG_TIMEOUT);
-                        s_abort = 1;
+                // the strip below must have finished its diagonal x + 31 of this sweep
+                const unsigned long long need = base + x + 32;
+                if (seen < need) {
+                    long long spins = 0;
+                    while ((seen = *(const volatile unsigned long long *)prog_below) < need) {
+                        if (gs_aborted(A)) break;
+                        if (++spins > kSpinLimit) gs_abort(A);
                     }
+                    __threadfence();
                 }
-                __threadfence_block();
-                down = *(const volatile double *)(A.p + ((size_t)(s - 1) * D + x + 31) * 32 + 31);
+                down = __ldcg(below + (size_t)x * 32);
             }
-            if (__any_sync(0xffffffffu, s_abort)) break;
+            const double c_pold = pold, c_rr = rr, c_right = right, c_up = up;
+            if (d + 1 < steps) load(d + 1);
             if (act) {
-                const size_t k = ((size_t)s * D + d) * 32 + lane;
-                const double pold = A.p[k], rr = A.r[k];
-                const double right = x < w - 1 ? A.p[k + 32] : 0.0;
-                double up = 0.0;
-                if (y < h - 1)
-                    up = lane < 31 ? A.p[k + 33] : A.p[((size_t)(s + 1) * D + d - 31) * 32];
-                double diag = 0.0, off = 0.0;
-                if (x > 0) {
-                    diag += scale;
-                    off -= scale * prev;
-                }
-                if (y > 0) {
-                    diag += scale;
-                    off -= scale * down;
-                }
-                if (x < w - 1) {
-                    diag += scale;
-                    off -= scale * right;
-                }
-                if (y < h - 1) {
-                    diag += scale;
-                    off -= scale * up;
-                }
-                const double np = (rr - off) / diag;
-                const double delta = fabs(pold - np);
-                lmax = smax(lmax, delta);
-                A.p[k] = np;
+                const int nb = (x > 0) + (y > 0) + (x < w - 1) + (y < h - 1);
+                const double diag = nb == 4 ? d4 : nb == 3 ? d3 : d2;
+                double off = 0.0;
+                if (x > 0) off -= scale * prev;
+                if (y > 0) off -= scale * down;
+                if (x < w - 1) off -= scale * c_right;
+                if (y < h - 1) off -= scale * c_up;
+                const double np = (c_rr - off) / diag;
+                lmax = smax(lmax, fabs(c_pold - np));
+                ps[(size_t)d * 32] = np;
                 prev = np;
             }
-            __syncwarp();
-            if (lane == 31) {
-                __threadfence_block();
-                prog[s] = base + d + 1;
+            // publish every 4 diagonals (the strip above trails by 32): a
+            // device-scope fence per diagonal would lengthen every step
+            if (s + 1 < S && (((d + 1) & 3) == 0 || d + 1 == steps)) {
+                __syncwarp();
+                if (lane == 31) {
+                    __threadfence();
+                    *(volatile unsigned long long *)(A.prog + s) = base + d + 1;
+                }
             }
         }
-        // maximum change over the CTA (max is order-free; NaN changes are
-        // ignored as std::max(maxDelta, NaN) ignores them)
+        // maximum change: per strip, then over the strips (order-free; NaN
+        // changes are ignored as std::max(maxDelta, NaN) ignores them)
         for (int o = 16; o > 0; o >>= 1) lmax = smax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        if (lane == 0) s_max[s] = lmax;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double m = 0.0;
-            for (int i = 0; i < (int)(blockDim.x >> 5); i++) m = smax(m, s_max[i]);
-            s_max[0] = m;
-            s_stop = s_abort || (A.pinned >= 0 ? it + 1 >= A.pinned : m < 1e-5);
-        }
-        __syncthreads();
-        maxDelta = s_max[0];
+        if (lane == 0) *(volatile double *)(A.smax + s) = lmax;
+        gs_grid_sync(A, gen);
+        double m = 0.0;
+        for (int i = lane; i < S; i += 32) m = smax(m, __ldcg(A.smax + i));
+        for (int o = 16; o > 0; o >>= 1) m = smax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        maxDelta = m;
         sweeps = it + 1;
-        const bool stop = s_stop;
-        __syncthreads();
+        const bool aborted = __any_sync(0xffffffffu, gs_aborted(A));
+        const bool stop = aborted || (A.pinned >= 0 ? it + 1 >= A.pinned : m < 1e-5);
+        // nobody may overwrite smax before every CTA has read it
+        gs_grid_sync(A, gen);
         if (stop) {
-            status = (A.pinned < 0 && maxDelta < 1e-5) ? 0 : 2;
+            status = (A.pinned < 0 && m < 1e-5 && !aborted) ? 0 : 2;
             break;
         }
     }
-    if (threadIdx.x == 0) {
+    if (s == 0 && lane == 0) {
         A.out->iterations = sweeps;
         A.out->status = status;
         A.out->max_error = maxDelta;
@@ -139,13 +180,27 @@ __global__ void __launch_bounds__(1024) gs_kernel(GsArgs A) {
     }
 }
 
+constexpr int kSpreadBytes = 120 * 1024;  // one such CTA per SM
+
 }  // namespace
 
-int gs_max_rows() { return 32 * kGsMaxStrips; }
+int gs_max_rows() { return 32 * 4096; }
 
 template <typename F>
 cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st) {
-    if (S.sd.S > kGsMaxStrips) return cudaErrorInvalidValue;
+    const int strips = S.sd.S;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    int smem = strips <= sms ? kSpreadBytes : 0;
+    if (smem) {
+        e = cudaFuncSetAttribute(gs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs_kernel, 32, smem);
+    if (e != cudaSuccess) return e;
+    if ((long)per_sm * sms < strips) return cudaErrorCooperativeLaunchTooLarge;
     GsArgs A;
     A.r = S.r;
     A.p = S.p;
@@ -156,8 +211,14 @@ cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int lim
     A.out = X.out;
     A.flags = S.flags;
     A.iter_total = X.iter_total;
-    gs_kernel<<<1, 32 * S.sd.S, 0, st>>>(A);
-    return cudaGetLastError();
+    A.prog = X.halo;       // strips + 1 words (halo holds 2 x S x D)
+    A.smax = X.partials;   // strips doubles (partials hold 4 x S x D / 16)
+    A.bar = X.barrier;
+    e = cudaMemsetAsync(A.prog, 0, sizeof(unsigned long long) * (strips + 1), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.bar, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    void *args[] = {&A};
+    return cudaLaunchCooperativeKernel((const void *)gs_kernel, dim3(strips), dim3(32), args, (size_t)smem, st);
 }
 
 template cudaError_t launch_gs<double>(const Scene<double> &, const PcgScratch &, double, int, int, cudaStream_t);

@@ -83,7 +83,17 @@ def test_pinned_sweeps(ifl):
     assert o.stats()[0][0] > 37
 
 
-def test_taller_grids_are_rejected(ifl, ):
-    with pytest.raises(ifl.IflError) as e:
-        ifl.FluidSolver(64, 1100, 0.1, variant=ifl.GS_EULER)
-    assert e.value.code == ifl.ERR_UNSUPPORTED
+def test_tall_grid_many_strips_bit_exact(ifl):
+    """35 strips (one CTA each, more strips than 32): the strip hand-over and
+    the grid barrier of the cooperative launch."""
+    w, h = 40, 1100
+    o = O.OracleSolver(2, w, h)
+    g = ifl.FluidSolver(w, h, 0.1, variant=ifl.GS)
+    inflow = (0.3, 0.05, 0.4, 0.02, 1.0, 0.0, 0.0, 3.0)
+    for step in range(2):
+        o.add_inflow(*inflow)
+        g.addInflow(*inflow[:5], *inflow[6:])
+        o.update(DT)
+        g.update(DT)
+        assert g.stats()[0] == o.stats()[0], step
+        _fields(ifl, g, o)
