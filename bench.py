@@ -600,7 +600,7 @@ def run_batch(args, rank, world, local_rank):
             members.append(ifl.FluidSolver(sc.w, sc.h, sc.density, bs, variant=sc.variant, precision=prec,
                                            device=local_rank))
             bodies.append(bs)
-        b = ifl.Batch(members, use_graph=use_graph)
+        b = ifl.Batch(members, use_graph=use_graph, max_team_blocks=args.max_team_blocks)
         for i, sc in enumerate(scs):
             b.set_inflows(i, sc.inflows)
         return b, members, bodies
@@ -813,6 +813,7 @@ def main():
     ap.add_argument("--serve-steps-scale", type=float, default=0.1, help="scale of the U[50,500] steps per request")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget of the serving run")
     ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
+    ap.add_argument("--max-team-blocks", type=int, default=0, help="batch: largest PCG team in blocks (0 = library default)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
     if not args.size:

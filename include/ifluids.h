@@ -304,7 +304,7 @@ typedef struct {
     int32_t threads, strips_per_block, stages;
     int32_t use_graph;        /* 1: replay each step as one CUDA graph (default) */
     int32_t tune_iterations;  /* PCG iterations per autotuning trial (default 8) */
-    int32_t pad_;
+    int32_t max_team_blocks;  /* largest team (blocks working on one scene); 0: 128 */
 } ifl_batch_options;
 
 typedef struct {

@@ -356,6 +356,7 @@ class BatchImpl final : public BatchBase {
         }
         std::string why;
         PcgBatchPlan *P = pcg_batch_create<F>(sc.data(), sx.data(), n_, sh, &why);
+        if (P) pcg_batch_set_max_team(P, opt_.max_team_blocks);
         if (!P) {
             err_ = "batched PCG shape {" + std::to_string(sh.threads) + "," + std::to_string(sh.K) + "," +
                    std::to_string(sh.stages) + "}: " + why;
@@ -597,6 +598,7 @@ int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, 
     }
     if (opt.threads != 0 && opt.threads != 32 && opt.threads != 64 && opt.threads != 128 && opt.threads != 256)
         return IFL_ERR_ARG;
+    if (opt.max_team_blocks < 0) return IFL_ERR_ARG;
     std::vector<SolverBase *> m(members, members + n);
     int e;
     if (p0.precision == IFL_FP32) {

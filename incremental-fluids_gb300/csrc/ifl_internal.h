@@ -173,10 +173,12 @@ size_t pcg_batch_table_bytes(const PcgBatchPlan *P);  // team/queue tables uploa
 int pcg_batch_schedule(PcgBatchPlan *P, const double *work_sweep, const double *work_elem, cudaStream_t st);
 // Team plan (host only): class c holds the scenes whose strips need 2^c
 // blocks; teams[c] teams of tsize[c] blocks serve it; queues[c] = its scenes by
-// decreasing work.  work_elem may be null.  Returns the blocks used, -1 if the
-// grid is too small.
+// decreasing work.  work_elem may be null.  Teams grow up to max_team blocks.
+// Returns the blocks used, -1 if the grid is too small.
 int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
-                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues);
+                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues,
+                   int max_team = 128);
+void pcg_batch_set_max_team(PcgBatchPlan *P, int blocks);
 // Device table of per-scene {pinned pressure, pinned heat, limit pressure, limit heat}.
 int4 *pcg_batch_ctl(PcgBatchPlan *P);
 template <typename F> cudaError_t launch_pcg_batch(PcgBatchPlan *P, const PcgConfig &cfg, cudaStream_t st);

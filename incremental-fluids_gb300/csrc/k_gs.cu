@@ -29,6 +29,8 @@ namespace ifl {
 
 namespace {
 
+constexpr int kGB = 8;  // steps per block of neighbour-strip prefetches
+
 struct GsArgs {
     const double *r;
     double *p;
@@ -107,49 +109,70 @@ __global__ void __launch_bounds__(32) gs_kernel(GsArgs A) {
                 pold = ps[k];
                 rr = rs[k];
                 right = x < w - 1 ? ps[k + 32] : 0.0;
-                if (y < h - 1) up = lane < 31 ? ps[k + 33] : __ldcg(above + (size_t)x * 32);
+                if (y < h - 1 && lane < 31) up = ps[k + 33];  // lane 31: the block's prefetch
             }
         };
         load(0);
-        for (int d = 0; d < steps; d++) {
-            const int x = d - lane;
-            const bool act = row && x >= 0 && x < w;
-            double down = __shfl_up_sync(0xffffffffu, prev, 1);
-            if (lane == 0 && s > 0 && x < w) {
-                // the strip below must have finished its diagonal x + 31 of this sweep
-                const unsigned long long need = base + x + 32;
-                if (seen < need) {
-                    long long spins = 0;
-                    while ((seen = *(const volatile unsigned long long *)prog_below) < need) {
-                        if (gs_aborted(A)) break;
-                        if (++spins > kSpinLimit) gs_abort(A);
+        for (int d0 = 0; d0 < steps; d0 += kGB) {
+            // Values from the neighbouring strips for the kGB steps of this
+            // block, fetched once per block by lanes 0..kGB-1 (one L2 round
+            // trip instead of one per step): the lower row's new values (the
+            // strip below must have finished diagonal x + 31 for each of
+            // them) and the upper row's old values (the strip above trails
+            // this one, so they are still the previous sweep's).
+            double dv = 0.0, uv = 0.0;
+            if (s > 0 && d0 < w) {
+                if (lane == 0) {
+                    const unsigned long long need = base + min(d0 + kGB - 1, w - 1) + 32;
+                    if (seen < need) {
+                        long long spins = 0;
+                        while ((seen = *(const volatile unsigned long long *)prog_below) < need) {
+                            if (gs_aborted(A)) break;
+                            if (++spins > kSpinLimit) gs_abort(A);
+                        }
                     }
-                    __threadfence();
                 }
-                down = __ldcg(below + (size_t)x * 32);
-            }
-            const double c_pold = pold, c_rr = rr, c_right = right, c_up = up;
-            if (d + 1 < steps) load(d + 1);
-            if (act) {
-                const int nb = (x > 0) + (y > 0) + (x < w - 1) + (y < h - 1);
-                const double diag = nb == 4 ? d4 : nb == 3 ? d3 : d2;
-                double off = 0.0;
-                if (x > 0) off -= scale * prev;
-                if (y > 0) off -= scale * down;
-                if (x < w - 1) off -= scale * c_right;
-                if (y < h - 1) off -= scale * c_up;
-                const double np = (c_rr - off) / diag;
-                lmax = smax(lmax, fabs(c_pold - np));
-                ps[(size_t)d * 32] = np;
-                prev = np;
-            }
-            // publish every 4 diagonals (the strip above trails by 32): a
-            // device-scope fence per diagonal would lengthen every step
-            if (s + 1 < S && (((d + 1) & 3) == 0 || d + 1 == steps)) {
                 __syncwarp();
-                if (lane == 31) {
-                    __threadfence();
-                    *(volatile unsigned long long *)(A.prog + s) = base + d + 1;
+                __threadfence();
+                if (lane < kGB && d0 + lane < w) dv = __ldcg(below + (size_t)(d0 + lane) * 32);
+            }
+            if (s + 1 < S && lane < kGB) {
+                const int xu = d0 + lane - 31;  // lane 31's column at step d0 + lane
+                if (xu >= 0 && xu < w && 32 * s + 31 < h - 1) uv = __ldcg(above + (size_t)xu * 32);
+            }
+            if (__any_sync(0xffffffffu, gs_aborted(A))) break;
+            const int dend = min(d0 + kGB, steps);
+            for (int d = d0; d < dend; d++) {
+                const int x = d - lane;
+                const bool act = row && x >= 0 && x < w;
+                double down = __shfl_up_sync(0xffffffffu, prev, 1);
+                const double d_blk = __shfl_sync(0xffffffffu, dv, d - d0);
+                const double u_blk = __shfl_sync(0xffffffffu, uv, d - d0);
+                if (lane == 0) down = d_blk;
+                const double c_pold = pold, c_rr = rr, c_right = right;
+                const double c_up = lane == 31 ? u_blk : up;
+                if (d + 1 < steps) load(d + 1);
+                if (act) {
+                    const int nb = (x > 0) + (y > 0) + (x < w - 1) + (y < h - 1);
+                    const double diag = nb == 4 ? d4 : nb == 3 ? d3 : d2;
+                    double off = 0.0;
+                    if (x > 0) off -= scale * prev;
+                    if (y > 0) off -= scale * down;
+                    if (x < w - 1) off -= scale * c_right;
+                    if (y < h - 1) off -= scale * c_up;
+                    const double np = (c_rr - off) / diag;
+                    lmax = smax(lmax, fabs(c_pold - np));
+                    ps[(size_t)d * 32] = np;
+                    prev = np;
+                }
+                // publish every 4 diagonals (the strip above trails by 32): a
+                // device-scope fence per diagonal would lengthen every step
+                if (s + 1 < S && (((d + 1) & 3) == 0 || d + 1 == steps)) {
+                    __syncwarp();
+                    if (lane == 31) {
+                        __threadfence();
+                        *(volatile unsigned long long *)(A.prog + s) = base + d + 1;
+                    }
                 }
             }
         }

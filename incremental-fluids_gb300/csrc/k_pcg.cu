@@ -1060,6 +1060,7 @@ struct PcgBatchPlan {
     int n = 0;
     PcgShape shape{};
     int grid = 0;      // co-resident blocks of the launch
+    int max_team = 128;  // largest team the planner may form
     size_t smem = 0;
     std::vector<int> strips, diags, cells;
     // device: [jobs pressure][jobs heat][block_team][team][class_range][class_jobs][team_job]
@@ -1263,6 +1264,7 @@ void pcg_batch_destroy(PcgBatchPlan *P) {
 
 int pcg_batch_grid(const PcgBatchPlan *P) { return P->grid; }
 size_t pcg_batch_table_bytes(const PcgBatchPlan *P) { return P->tab_bytes; }
+void pcg_batch_set_max_team(PcgBatchPlan *P, int blocks) { P->max_team = blocks > 0 ? blocks : 128; }
 
 // Teams and queues from the estimated work of each scene: work_sweep (the
 // wavefront part, which more blocks do not shorten) and work_elem (the
@@ -1270,13 +1272,14 @@ size_t pcg_batch_table_bytes(const PcgBatchPlan *P) { return P->tab_bytes; }
 // Scenes go to the class of the smallest power-of-two team that covers their
 // strips; every non-empty class gets one team.  Then, while blocks are left,
 // the class with the latest estimated finish (its work over its teams, or its
-// largest scene) gets one more team or teams twice as large (up to 128
+// largest scene) gets one more team or teams twice as large (up to max_team
 // blocks), whichever shortens that finish most per block spent, as long as it
 // improves.  Each queue is ordered by work, largest first.  teams[c] and
 // tsize[c] give the teams of class c; returns the blocks in teams, or -1 when
 // the classes' first teams alone exceed the grid.
 int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
-                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues) {
+                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues,
+                   int max_team) {
     std::vector<std::vector<int>> members(kMaxClasses);
     for (int i = 0; i < n; i++) {
         const int need = (strips[i] + K - 1) / K;
@@ -1324,7 +1327,7 @@ int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work
         const bool can_add = teams[c] < (int)members[c].size() && size <= left;
         const double fin_add = can_add ? std::max(tot[c] / (teams[c] + 1), big[c]) : bt;
         // every team of the class twice as large
-        const bool can_grow = work_elem && size * 2 <= 128 && teams[c] * size <= left;
+        const bool can_grow = work_elem && size * 2 <= max_team && teams[c] * size <= left;
         double fin_grow = bt;
         if (can_grow) {
             mult[c] *= 2;
@@ -1355,7 +1358,8 @@ int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work
 int pcg_batch_schedule(PcgBatchPlan *P, const double *work_sweep, const double *work_elem, cudaStream_t st) {
     int teams[kMaxClasses], tsize[kMaxClasses];
     std::vector<std::vector<int>> members;
-    if (pcg_plan_teams(P->grid, P->shape.K, P->n, P->strips.data(), work_sweep, work_elem, teams, tsize, &members) <
+    if (pcg_plan_teams(P->grid, P->shape.K, P->n, P->strips.data(), work_sweep, work_elem, teams, tsize, &members,
+                       P->max_team) <
         0)
         return -1;
     // host tables

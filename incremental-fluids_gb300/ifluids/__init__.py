@@ -97,7 +97,7 @@ class Inflow(C.Structure):
 
 class BatchOptions(C.Structure):
     _fields_ = [("threads", C.c_int32), ("strips_per_block", C.c_int32), ("stages", C.c_int32),
-                ("use_graph", C.c_int32), ("tune_iterations", C.c_int32), ("pad_", C.c_int32)]
+                ("use_graph", C.c_int32), ("tune_iterations", C.c_int32), ("max_team_blocks", C.c_int32)]
 
 
 class BatchInfo(C.Structure):
@@ -532,7 +532,7 @@ class Batch:
     """
 
     def __init__(self, solvers: Sequence[FluidSolver], threads: int = 0, strips_per_block: int = 0,
-                 stages: int = 0, use_graph: bool = True, tune_iterations: int = 8):
+                 stages: int = 0, use_graph: bool = True, tune_iterations: int = 8, max_team_blocks: int = 0):
         self._L = load_library()
         self.solvers = list(solvers)
         o = BatchOptions()
@@ -540,6 +540,7 @@ class Batch:
         o.threads, o.strips_per_block, o.stages = int(threads), int(strips_per_block), int(stages)
         o.use_graph = 1 if use_graph else 0
         o.tune_iterations = int(tune_iterations)
+        o.max_team_blocks = int(max_team_blocks)
         arr = (C.c_void_p * len(self.solvers))(*[s._h for s in self.solvers])
         h_ = C.c_void_p()
         rc = self._L.ifl_batch_create(arr, len(self.solvers), C.byref(o), C.byref(h_))
