@@ -25,8 +25,10 @@ cell-steps/s = sum of w*h over the scenes x steps per second.
 --workload single: the single solid-boundary scene at 1024 x 1024 (3 seeded
 bodies) instead.  --workload flip: step 8 (FLIP particles) on the reference
 main()'s own scene (rotated box, its fixed inflow, rhoAir 0.1, rhoSoot 0.25,
-diffusion 0.01, dt 0.0025) at --size (128, the reference's grid), FP64,
-one handle; its CPU baseline is the oracle's step-8 restatement.
+diffusion 0.01, dt 0.0025) at --size (128, the reference's grid), one
+handle: FP64 fields and particles, FP32-form solves (--precision fp64: the
+FP64 drop-in, which is also timed beside it); its CPU baseline is the
+oracle's step-8 restatement.
 --workload gs [--gs-variant 1|2]: the Gauss-Seidel steps on their reference
 main() scene (128^2 by default), FP64, one handle.  --impl reference times the reference's CPU algorithm (the
 oracle port; the reference's own sources are not present on the GPU host) on
@@ -422,9 +424,12 @@ def run_flip(args, local_rank):
     import ifluids as ifl
     n = args.size
 
-    def make():
+    prec = ifl.FP32 if args.precision == "fp32" else ifl.FP64
+
+    def make(precision=None):
         box = ifl.SolidBox(*FLIP_BOX)
-        return ifl.FluidSolver(n, n, *FLIP_RHO, [box], variant=ifl.FLIP, device=local_rank)
+        return ifl.FluidSolver(n, n, *FLIP_RHO, [box], variant=ifl.FLIP, device=local_rank,
+                               precision=prec if precision is None else precision)
 
     def step(s):
         s.addInflow(*FLIP_INFLOW)
@@ -453,8 +458,27 @@ def run_flip(args, local_rank):
             "pcg_iterations_last_step": [pit, hit]}
     g.close()
     dev_ms = T["dev_ms"]
+    fp64 = None
+    if prec == ifl.FP32 and args.fp64_steps > 0:  # the FP64 drop-in of the same scene beside it
+        import torch
+        g64 = make(ifl.FP64)
+        for _ in range(2):
+            step(g64)
+        g64.synchronize()
+        s64 = torch.cuda.ExternalStream(g64.stream, device=torch.device("cuda", local_rank))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s64):
+            e0.record(s64)
+        for _ in range(args.fp64_steps):
+            step(g64)
+        with torch.cuda.stream(s64):
+            e1.record(s64)
+        g64.synchronize()
+        fp64 = {"value": cells * args.fp64_steps / (e0.elapsed_time(e1) / 1e3), "unit": METRIC,
+                "steps": args.fp64_steps}
+        g64.close()
     return {"value": cells * args.steps / (dev_ms / 1e3), "ms_per_step": dev_ms / args.steps, "e2e": T["e2e"],
-            "roofline": roof, "gpu_launches": T["launches"], "clocks": T["clocks"], "fp64_dropin": None,
+            "roofline": roof, "gpu_launches": T["launches"], "clocks": T["clocks"], "fp64_dropin": fp64,
             "particles": particles, "particle_steps_per_s": particles * args.steps / (dev_ms / 1e3),
             "latency_ms": {"p50": round(statistics.median(T["step_ms"]), 3), "max": round(max(T["step_ms"]), 3)}}
 
@@ -835,9 +859,9 @@ def main():
         config = {"workload": f"FLIP particles (8-flip) on the reference main's scene {args.size}x{args.size}: "
                               f"rotated box, fixed inflow d=1 T=294 K, rhoAir 0.1, rhoSoot 0.25, diffusion 0.01, "
                               f"dt=0.0025",
-                  "variant": "8-flip", "grid": [args.size, args.size], "precision_form": "fp64",
+                  "variant": "8-flip", "grid": [args.size, args.size], "precision_form": args.precision,
+                  "precision_note": "FP64 fields and particles in both forms; fp32 = FP32-form solves",
                   "l2": "flushed between timed steps (512 MiB write)", "scene_data": "the reference's own scene"}
-        args.precision = "fp64"
     elif args.workload == "gs":
         name = {1: "1-matrixless", 2: "2-better-advection"}[args.gs_variant]
         config = {"workload": f"Gauss-Seidel step {name} on the reference main's scene {args.size}x{args.size}: "

@@ -58,7 +58,9 @@ enum {
     IFL_HEAT = 6,     /* 6-heat: + temperature, heat diffusion, buoyancy       */
     IFL_VARDENS = 7,  /* 7-variable-density: + per-face density               */
     IFL_FLIP = 8      /* 8-flip: step 7's grid solve; FLIP particles carry d,
-                         T, u, v instead of semi-Lagrangian advection (FP64) */
+                         T, u, v instead of semi-Lagrangian advection.  Fields
+                         and particles are FP64 in both forms; IFL_FP32 selects
+                         FP32-form solves                                     */
 };
 
 /* Storage / arithmetic form. */

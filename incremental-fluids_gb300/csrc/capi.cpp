@@ -105,7 +105,6 @@ int ifl_create(const ifl_params *p, ifl_solver **out) {
     if (p->w < 2 || p->h < 2 || p->w > 32768 || p->h > 32768) return IFL_ERR_ARG;
     if (p->variant <= IFL_GS && p->h > ifl::gs_max_rows()) return IFL_ERR_UNSUPPORTED;  // one CTA of strips
     if (p->precision != IFL_FP64 && p->precision != IFL_FP32) return IFL_ERR_ARG;
-    if (p->variant == IFL_FLIP && p->precision != IFL_FP64) return IFL_ERR_UNSUPPORTED;  // particles are FP64
     if (p->variant == IFL_FLIP && (int64_t)p->w * p->h * 12 > 0x7fffffff) return IFL_ERR_UNSUPPORTED;
     if (p->device < 0) return IFL_ERR_ARG;
     if (p->max_iter_pressure < 0 || p->max_iter_heat < 0) return IFL_ERR_ARG;

@@ -154,6 +154,14 @@ template <typename F> void launch_render(const Scene<F> &S, unsigned char *rgba,
 template <typename F> cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &c,
                                              cudaStream_t st, int *blocks_used);
 template <typename F> int pcg_max_blocks();
+// FP32-form solves of an FP64 scene (step 8 with IFL_FP32): FP32 matrix,
+// MIC(0) apply records and PCG vectors beside the scene's FP64 r, p, A*s and
+// factor; the matrix is rounded from the scene's FP64 one at each factor.
+struct PcgF32 {
+    float *adiag, *ax, *ay, *mic, *rf, *z, *sa, *sb;
+};
+cudaError_t launch_pcg_f32(const Scene<double> &S, const PcgF32 &M, const PcgScratch &X, const PcgConfig &c,
+                           cudaStream_t st, int *blocks_used);
 // Gauss-Seidel solve of steps 1-2 (k_gs.cu): one CTA, h <= gs_max_rows().
 template <typename F>
 cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st);

@@ -1026,30 +1026,87 @@ PcgArgs<F> make_args(const Scene<F> &S, const PcgScratch &X, int heat) {
 }
 }  // namespace
 
+namespace {
+// FP32-form work arrays of an FP64 scene, and the conversion of its matrix.
+PcgArgs<float> make_args_f32(const Scene<double> &S, const PcgF32 &M, const PcgScratch &X, int heat) {
+    PcgArgs<float> A;
+    std::memset(&A, 0, sizeof A);
+    A.sd = S.sd;
+    A.adiag = M.adiag;
+    A.ax = M.ax;
+    A.ay = M.ay;
+    A.pc = S.pc;
+    A.mic = M.mic;
+    A.nb = S.nb;
+    A.r = S.r;
+    A.p = S.p;
+    A.as = S.as;
+    A.rf = M.rf;
+    A.z = M.z;
+    A.sa = M.sa;
+    A.sb = M.sb;
+    A.partials = X.partials;
+    A.barrier = X.barrier;
+    A.halo = X.halo;
+    A.fl = Flags{S.flags, S.flags};
+    A.out = X.out + (heat ? 1 : 0);
+    A.iter_total = X.iter_total;
+    A.rowsum_zero = heat ? 0 : 1;
+    return A;
+}
+__global__ void matrix_to_f32_kernel(const double *a, const double *b, const double *c, float *fa, float *fb,
+                                     float *fc, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        fa[i] = (float)a[i];
+        fb[i] = (float)b[i];
+        fc[i] = (float)c[i];
+    }
+}
+}  // namespace
+
+template <typename F>
+cudaError_t launch_pcg_with(PcgArgs<F> A, const SDIdx &sd, const PcgScratch &X, const PcgConfig &cfg,
+                            cudaStream_t st, int *blocks_used);
+
 template <typename F>
 cudaError_t launch_pcg(const Scene<F> &S, const PcgScratch &X, const PcgConfig &cfg, cudaStream_t st,
                        int *blocks_used) {
-    PcgArgs<F> A = make_args(S, X, cfg.heat);
+    return launch_pcg_with<F>(make_args(S, X, cfg.heat), S.sd, X, cfg, st, blocks_used);
+}
+
+cudaError_t launch_pcg_f32(const Scene<double> &S, const PcgF32 &M, const PcgScratch &X, const PcgConfig &cfg,
+                           cudaStream_t st, int *blocks_used) {
+    if (cfg.mode & PCG_FACTOR) {  // the FP32 form stores the matrix in FP32 (rounded once)
+        const size_t n = S.sd.total();
+        matrix_to_f32_kernel<<<(int)std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, st>>>(
+            S.adiag, S.ax, S.ay, M.adiag, M.ax, M.ay, n);
+    }
+    return launch_pcg_with<float>(make_args_f32(S, M, X, cfg.heat), S.sd, X, cfg, st, blocks_used);
+}
+
+template <typename F>
+cudaError_t launch_pcg_with(PcgArgs<F> A, const SDIdx &sd, const PcgScratch &X, const PcgConfig &cfg,
+                            cudaStream_t st, int *blocks_used) {
     A.mode = cfg.mode;
     A.limit = cfg.limit;
     A.pinned = cfg.pinned;
     A.K = strips_per_block<F>();
-    if (A.K > S.sd.S) A.K = S.sd.S;
+    if (A.K > sd.S) A.K = sd.S;
     A.stages = kStages;
-    const size_t smem = smem_bytes<F>(A.K, S.sd.D);
+    const size_t smem = smem_bytes<F>(A.K, sd.D);
     const int threads = 512;
     const void *fn = (const void *)pcg_kernel<F, 512>;
     int maxb = max_coresident<F, 512>(smem);
     if (maxb > X.max_blocks) maxb = X.max_blocks;
-    const int need = (S.sd.S + A.K - 1) / A.K;  // blocks that own strips
+    const int need = (sd.S + A.K - 1) / A.K;  // blocks that own strips
     if (maxb < need) return cudaErrorInvalidConfiguration;
-    const long long slots = (long long)S.sd.total();
+    const long long slots = (long long)sd.total();
     int want = (int)((slots + threads * 4 - 1) / (threads * 4));
     if (want < need) want = need;
     int G = want < maxb ? want : maxb;
     if (blocks_used) *blocks_used = G;
     cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
-    cudaMemsetAsync(X.halo, 0xff, 2 * (size_t)S.sd.S * S.sd.D * sizeof(unsigned long long), st);
+    cudaMemsetAsync(X.halo, 0xff, 2 * (size_t)sd.S * sd.D * sizeof(unsigned long long), st);
     void *args[] = {&A};
     return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(threads), args, smem, st);
 }

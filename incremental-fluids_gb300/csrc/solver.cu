@@ -519,6 +519,18 @@ class SolverImpl final : public SolverBase {
         S_.bodies = d_bodies_;
         S_.nbodies = 0;
         S_.flags = c.take<unsigned>(base, 8);
+        M_ = PcgF32{};
+        f32_solves_ = prm_.variant == IFL_FLIP && prm_.precision == IFL_FP32;
+        if (f32_solves_) {  // FP32-form solves beside the FP64 fields and particles
+            M_.adiag = c.take<float>(base, NS);
+            M_.ax = c.take<float>(base, NS);
+            M_.ay = c.take<float>(base, NS);
+            M_.mic = c.take<float>(base, 4 * NS);
+            M_.rf = c.take<float>(base, NS);
+            M_.z = c.take<float>(base, NS);
+            M_.sa = c.take<float>(base, NS);
+            M_.sb = c.take<float>(base, NS);
+        }
         X_ = FlipState{};
         if (prm_.variant == IFL_FLIP) {
             const int w = prm_.w, h = prm_.h, cells = w * h;
@@ -594,7 +606,13 @@ class SolverImpl final : public SolverBase {
         cfg.heat = heat ? 1 : 0;
         int G = 0;
         int t = tbegin(IFL_K_PCG);
-        cudaError_t e = launch_pcg<F>(S_, scratch_, cfg, stream_, &G);
+        cudaError_t e;
+        if constexpr (std::is_same<F, double>::value) {
+            e = f32_solves_ ? launch_pcg_f32(S_, M_, scratch_, cfg, stream_, &G)
+                            : launch_pcg<F>(S_, scratch_, cfg, stream_, &G);
+        } else {
+            e = launch_pcg<F>(S_, scratch_, cfg, stream_, &G);
+        }
         tend(t);
         if (check(e, "pcg launch")) return IFL_ERR_CUDA;
         launches_++;
@@ -645,6 +663,8 @@ class SolverImpl final : public SolverBase {
     }
 
     Scene<F> S_{};
+    PcgF32 M_{};
+    bool f32_solves_ = false;  // step 8 with IFL_FP32: FP32-form PCG, FP64 everything else
     FlipState X_{};
     bool flip_ready_ = false;
     std::vector<std::array<double, 8>> pending_;  // FLIP inflows of the next update
@@ -854,13 +874,15 @@ int SolverBase::write_field(int field, const void *host, size_t bytes, int dtype
     return IFL_OK;
 }
 
+// Step 8 keeps FP64 fields and particles in both forms; IFL_FP32 selects its
+// FP32-form solves only.
 size_t solver_device_bytes(const ifl_params &p, int max_blocks) {
-    if (p.precision == IFL_FP32) return SolverImpl<float>::arena_size(p, max_blocks);
+    if (p.precision == IFL_FP32 && p.variant != IFL_FLIP) return SolverImpl<float>::arena_size(p, max_blocks);
     return SolverImpl<double>::arena_size(p, max_blocks);
 }
 
 std::unique_ptr<SolverBase> make_solver(const ifl_params &p) {
-    if (p.precision == IFL_FP32) return std::unique_ptr<SolverBase>(new SolverImpl<float>(p));
+    if (p.precision == IFL_FP32 && p.variant != IFL_FLIP) return std::unique_ptr<SolverBase>(new SolverImpl<float>(p));
     return std::unique_ptr<SolverBase>(new SolverImpl<double>(p));
 }
 

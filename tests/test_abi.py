@@ -59,13 +59,17 @@ def test_create_rejects_bad_parameters_without_touching_the_gpu(ifl, lib, field,
     assert not h.value
 
 
-def test_flip_is_fp64_only(ifl, lib):
+def test_flip_fp32_form_adds_only_solver_arrays(ifl, lib):
+    """Step 8 keeps FP64 fields and particles in both forms; IFL_FP32 adds the
+    FP32-form PCG arrays (no GPU needed: the byte count is computed on the host)."""
     p = ifl.Params()
-    lib.ifl_default_params(C.byref(p), ifl.FLIP, 16, 16)
+    lib.ifl_default_params(C.byref(p), ifl.FLIP, 64, 64)
+    lib.ifl_device_bytes.restype = C.c_int64
+    b64 = lib.ifl_device_bytes(C.byref(p))
     p.precision = ifl.FP32
-    h = C.c_void_p()
-    assert lib.ifl_create(C.byref(p), C.byref(h)) == ifl.ERR_UNSUPPORTED
-    assert not h.value
+    b32 = lib.ifl_device_bytes(C.byref(p))
+    assert b64 > 0 and b32 > b64
+    assert b32 - b64 < 11 * 4 * 4 * 64 * 96 * 32  # the FP32 matrix, records and vectors only
 
 
 def test_null_handles_are_rejected(ifl, lib):

@@ -170,3 +170,56 @@ def test_to_image_marks_empty_cells(ifl):
         a, b = g.to_image(heat), o.to_image(heat)
         assert np.array_equal(a, b), heat
     assert (g.to_image(False)[6, 12] == [255, 0, 0, 255]).all()
+
+
+# The reference main's scene (its solves converge and its flow is developed).
+# The moving sphere in a closed domain makes the pressure system inconsistent:
+# the reference's own PCG runs into its cap while p drifts along the null
+# space (to ~1e12 after four steps), where FP32 search vectors cannot carry
+# the gradient - outside the FP32 form's envelope.  The body-free scene has
+# no flow yet (velocities at rounding level, the pressure solve returns on its
+# initial residual), so it has nothing to compare.
+FP32_SCENES = [s for s in FC.SCENES if s[0] == "main_48"]
+
+
+@pytest.mark.parametrize("scene", FP32_SCENES, ids=[s[0] for s in FP32_SCENES])
+def test_fp32_form_solves_from_the_oracle_state(ifl, scene):
+    """IFL_FP32 on a step-8 handle: FP32-form heat and pressure solves, FP64
+    fields and particles.  One update from the state of an oracle run (fields,
+    particles, frand() state): mean-free pressure (fluid cells) and velocity
+    within 1e-4 relative of the FP64 oracle, the same particle count,
+    positions within 1e-6 cells (the only difference is the solves' rounding)."""
+    _, w, h, bodies, steps = scene
+    o = O.OracleSolver(O.FLIP, w, h, FC.RHO_AIR, FC.RHO_SOOT, FC.DIFFUSION)
+    if bodies:
+        o.set_bodies(bodies)
+    for _ in range(steps):
+        o.add_inflow(*FC.INFLOW)
+        o.update(FC.DT)
+        o.advance_bodies(FC.DT)
+    objs = [ifl.SolidBox(*b[1:]) if b[0] == 0 else ifl.SolidSphere(b[1], b[2], b[3], *b[5:]) for b in o.bodies()]
+    g = ifl.FluidSolver(w, h, FC.RHO_AIR, FC.RHO_SOOT, FC.DIFFUSION, objs, variant=ifl.FLIP, precision=ifl.FP32)
+    for q in QUANTS:
+        g.write_field(ifl.field_id(q, ifl.A_SRC), o.array(q, O.A_SRC).copy())
+    g.set_particles([o.particles(k).copy() for k in range(6)])
+    g.rng_state = o.rng_state
+    o.add_inflow(*FC.INFLOW)
+    g.addInflow(*FC.INFLOW)
+    o.update(FC.DT)
+    g.update(FC.DT)
+    assert g.stats()[2] & 1 == 0
+    # The pressure is compared without its mean: with a moving body the
+    # closed-domain system is inconsistent and CG drifts along the constant
+    # null space (here to ~1e12 in the reference itself), a drift the FP32
+    # form follows differently and the velocities never see.
+    fluid = o.bytes(O.QD, O.B_CELL) == 0
+    p_ref = o.array(0, O.A_P)[fluid]
+    p_gpu = g.read_field("p")[fluid]
+    p_ref, p_gpu = p_ref - p_ref.mean(), p_gpu - p_gpu.mean()
+    ep = np.abs(p_gpu - p_ref).max() / max(np.abs(p_ref).max(), 1e-300)
+    vmax = max(np.abs(o.array(O.QU, O.A_SRC)).max(), np.abs(o.array(O.QV, O.A_SRC)).max())
+    ev = max(np.abs(g.read_field(name) - o.array(q, O.A_SRC)).max() for name, q in (("u", O.QU), ("v", O.QV))) / vmax
+    assert ep <= 1e-4 and ev <= 1e-4, (ep, ev)
+    assert g.particle_count() == o.particle_count()
+    for k in (O.P_X, O.P_Y):
+        assert np.abs(g.particles(k) - o.particles(k)).max() <= 1e-6
