@@ -624,7 +624,9 @@ def run_batch(args, rank, world, local_rank):
             members.append(ifl.FluidSolver(sc.w, sc.h, sc.density, bs, variant=sc.variant, precision=prec,
                                            device=local_rank))
             bodies.append(bs)
-        b = ifl.Batch(members, use_graph=use_graph, max_team_blocks=args.max_team_blocks)
+        t, k, st = (int(v) for v in args.shape.split(",")) if args.shape else (0, 0, 0)
+        b = ifl.Batch(members, use_graph=use_graph, max_team_blocks=args.max_team_blocks, threads=t,
+                      strips_per_block=k, stages=st)
         for i, sc in enumerate(scs):
             b.set_inflows(i, sc.inflows)
         return b, members, bodies
@@ -838,6 +840,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget of the serving run")
     ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
     ap.add_argument("--max-team-blocks", type=int, default=0, help="batch: largest PCG team in blocks (0 = library default)")
+    ap.add_argument("--shape", default="", help="batch: fixed PCG shape threads,strips_per_block,stages (default: autotuned)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
     if not args.size:

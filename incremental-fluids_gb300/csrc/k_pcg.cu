@@ -24,7 +24,7 @@
 //    diagonal), so the lower (upper) neighbour's value arrives from lane l-1
 //    (l+1) through a register shuffle.  Operands stream through a per-warp
 //    shared-memory ring filled by bulk asynchronous copies (cp.async.bulk,
-//    completion on an mbarrier), one contiguous block of kSweepBlock diagonals
+//    completion on an mbarrier), one contiguous block of kB diagonals
 //    per array.  A strip hands its boundary row to the neighbouring strip
 //    through a halo row: in shared memory between warps of one block, in
 //    global memory between blocks; each entry is written once per sweep with
@@ -54,7 +54,11 @@ extern __shared__ __align__(128) char g_smem[];
 // compact launch used when many scenes run concurrently.
 constexpr int kMaxWarps = 16;
 constexpr int kChunk = kPcgChunk;  // diagonals per reduction chunk of the elementwise phases
-constexpr int kB = kSweepBlock;                  // diagonals per bulk-copy block
+// Diagonals per bulk-copy block of a sweep ring (the layout's padding unit).
+// Halving it lets 16 single-warp blocks share an SM, which measured slower on
+// full batch steps (30.7 M against 36.5 M cell-steps/s): the second warp of a
+// 64-thread block, which works only in the elementwise passes, pays for more.
+constexpr int kB = kSweepBlock;
 constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
 constexpr double kTau = 0.97, kSigma = 0.25, kTol = 1e-5;
