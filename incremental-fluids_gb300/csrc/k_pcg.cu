@@ -139,9 +139,11 @@ __device__ __forceinline__ void set_timeout(const Flags &f) {
     if (f.all != f.scene) atomicOr(f.all, FLAG_TIMEOUT);
 }
 
-// Team barrier: arrival counter + generation word, bounded wait.
+// Team barrier: arrival counter + generation word, bounded wait.  A team of
+// one block needs only the block barrier.
 __device__ void team_barrier(const Team &T, const Flags &fl) {
     __syncthreads();
+    if (T.size == 1) return;
     if (threadIdx.x == 0) {
         unsigned *bar = T.barrier;
         unsigned g = ld_volatile(bar + 1);
@@ -1104,6 +1106,8 @@ cudaError_t launch_pcg_with(PcgArgs<F> A, const SDIdx &sd, const PcgScratch &X, 
     if (maxb > X.max_blocks) maxb = X.max_blocks;
     const int need = (sd.S + A.K - 1) / A.K;  // blocks that own strips
     if (maxb < need) return cudaErrorInvalidConfiguration;
+    // one block per 2048 slots (fewer blocks for small grids measured slower:
+    // the elementwise passes lose more than the cheaper barriers save)
     const long long slots = (long long)sd.total();
     int want = (int)((slots + threads * 4 - 1) / (threads * 4));
     if (want < need) want = need;
