@@ -58,9 +58,10 @@ class SolidSphere : public SolidBody {
 
 class FluidSolver {
   public:
-    // 3-conjugate-gradients
-    FluidSolver(int w, int h, double density, int precision = IFL_FP64) {
-        init(IFL_PLAIN, w, h, density, 1.0, 0.01, precision);
+    // 3-conjugate-gradients (variant = IFL_GS_EULER / IFL_GS for 1-matrixless /
+    // 2-better-advection, the same constructor in the reference)
+    FluidSolver(int w, int h, double density, int precision = IFL_FP64, int variant = IFL_PLAIN) {
+        init(variant, w, h, density, 1.0, 0.01, precision);
     }
     // 4-solid-boundaries (variant = IFL_CURVED for 5-curved-boundaries)
     FluidSolver(int w, int h, double density, const std::vector<const SolidBody *> &bodies,
