@@ -20,6 +20,8 @@
 //
 // The particle count and the LCG state live on the device (FlipState::ctl),
 // so a whole update is launched without a host round trip.
+#include <algorithm>
+
 #include "ifl_device.cuh"
 
 namespace ifl {
