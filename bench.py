@@ -31,7 +31,7 @@ FP64 drop-in, which is also timed beside it); its CPU baseline is the
 oracle's step-8 restatement.
 --workload gs [--gs-variant 1|2]: the Gauss-Seidel steps on their reference
 main() scene (128^2 by default), FP64, one handle.  --impl reference times the reference's CPU algorithm (the
-oracle port; the reference's own sources are not present on the GPU host) on
+oracle port; the reference's own sources are not part of this repository) on
 the same workload.  Multi-GPU (torchrun): each rank runs an independent
 replica ("replicas only": scenes do not exchange data), barrier + max over
 ranks.
