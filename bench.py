@@ -102,6 +102,38 @@ def whole_job_rate(units_per_rank: float, steps: int, world: int, t_max_ms: floa
     return world * units_per_rank * steps / (t_max_ms / 1e3)
 
 
+def sum_over_ranks(x: float, world: int, device=None) -> float:
+    """Sum of a per-rank value over all ranks (identity for one rank)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def scene_work(w: int, h: int) -> float:
+    """Relative cost of one update of a w x h scene: cells x PCG iterations, and the
+    iterations grow about linearly with the longer side (about 70 at 128^2 and 640
+    at 1024^2 in the reference's MIC(0)-PCG)."""
+    return float(w) * h * max(w, h)
+
+
+def shard_scenes(work, rank: int, world: int):
+    """Disjoint, balanced share of scene indices for `rank`: scenes by decreasing
+    estimated work onto the least-loaded rank (ties to the lower rank and index),
+    so every rank computes the same partition without exchanging anything."""
+    order = sorted(range(len(work)), key=lambda i: (-work[i], i))
+    load = [0.0] * world
+    share = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        share[r].append(i)
+        load[r] += work[i]
+    return sorted(share[rank])
+
+
 def load_peaks():
     for path in (os.path.join(ROOT, "MEASURED_PEAKS.json"),):
         try:
@@ -172,33 +204,55 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline
-def _cpu_worker(args):
-    variant, n, steps, seed = args
+def cpu_kind() -> str:
+    """'reference' when the reference's own solver was compiled on this host
+    (oracle/_ref, built by __graft_entry__.build() from the staged sources),
+    else 'port' (the oracle, pinned bit-for-bit to it)."""
     from oracle import oracle as O
+    return "reference" if O.ref_available(4) else "port"
+
+
+def cpu_solver(kind: str):
+    from oracle import oracle as O
+    return O.RefSolver if kind == "reference" else O.OracleSolver
+
+
+def cpu_kind_text(kind: str) -> str:
+    return ("the reference's own FluidSolver (its Fluid.cpp compiled on this host, -O2 -ffp-contract=off)"
+            if kind == "reference" else "the oracle (C restatement of the reference, bit-identical to it)")
+
+
+def _cpu_worker(args):
+    variant, n, steps, warmup, seed, kind = args
     from ifluids import scenes
     sc = scenes.config1(n=n, seed=seed, variant=variant)
-    o = O.OracleSolver(variant, n, n)
+    o = cpu_solver(kind)(variant, n, n)
     o.set_bodies(sc.bodies)
-    t0 = time.perf_counter()
-    its = []
-    for _ in range(steps):
+    spent, its = 0.0, []
+    for k in range(warmup + steps):
         o.add_inflow(*sc.inflows[0])
+        t0 = time.perf_counter()
         o.update(sc.dt)
+        if k >= warmup:
+            spent += time.perf_counter() - t0
+            its.append(o.stats()[0][0])
         o.advance_bodies(sc.dt)
-        its.append(o.stats()[0][0])
-    return time.perf_counter() - t0, its
+    return spent, its
 
 
-def cpu_baseline(n: int, steps: int, procs: int, seed: int):
-    """The oracle on `procs` host cores, one independent scene per process."""
+def cpu_baseline(n: int, steps: int, warmup: int, procs: int, seed: int):
+    """The CPU solver on `procs` host cores, one independent copy of the scene per
+    process, timed at the same step indices as the GPU (after `warmup` updates)."""
+    kind = cpu_kind()
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_worker, [(4, n, steps, seed)] * procs)
+        res = pool.map(_cpu_worker, [(4, n, steps, warmup, seed, kind)] * procs)
     t = max(r[0] for r in res)
-    return {"value": procs * n * n * steps / t, "unit": METRIC, "cores": procs, "kind": "port",
-            "sample": f"{steps} update() of the {n}x{n} solid-boundary scene from its initial state "
-                      f"(PCG iterations {res[0][1]}) in each of {procs} processes, FP64 oracle",
-            "seconds": round(t, 2)}
+    return {"value": procs * n * n * steps / t, "unit": METRIC, "cores": procs, "kind": kind,
+            "sample": f"updates {warmup + 1}..{warmup + steps} (after {warmup} untimed) of the {n}x{n} "
+                      f"solid-boundary scene (PCG iterations {res[0][1]}) in each of {procs} processes, "
+                      f"{cpu_kind_text(kind)}, FP64",
+            "seconds": round(t, 2), "steps": steps, "warmup": warmup}
 
 
 # ----------------------------------------------------------------- GPU arm
@@ -278,6 +332,14 @@ def run_gpu(args, rank, world, local_rank):
     (pit, pst, perr), _, flags = g.stats()
     if flags & 1:
         raise RuntimeError("device-side wait timed out during the benchmark")
+    check = None
+    if args.field_check > 0 and rank == 0:  # one more (untimed) step against the FP64 reference
+        job = (sc.variant, sc.w, sc.h, gpu_state(ifl, g, sc.variant), [b.as_tuple() for b in bodies],
+               sc.inflows[:1], sc.dt)  # the scene generators use the reference's densities and diffusion
+        step_host(g, sc, bodies)
+        out = gpu_result(ifl, g, sc.variant)
+        check = field_error_check([job], [out], [g.stats()[0][0]], 1)
+        check["sample"] = f"the scene at update {args.warmup + args.steps + 1}"
 
     t_max = dev_ms
     if world > 1:
@@ -339,6 +401,7 @@ def run_gpu(args, rank, world, local_rank):
         g64.close()
     g.close()
     return {"value": value, "ms_per_step": t_max / args.steps, "e2e": e2e, "roofline": roof,
+            "field_error": check,
             "gpu_launches": launches, "clocks": clk.summary(), "pcg_iterations_last": pit,
             "pcg_status_last": pst, "fp64_dropin": fp64, "cells": cells, "scene": sc}
 
@@ -350,22 +413,25 @@ FLIP_RHO = (0.1, 0.25, 0.01)                                     # 8-flip/Fluid.
 FLIP_DT = 0.0025
 
 
-def cpu_baseline_flip(n: int, steps: int):
-    """The oracle's step-8 restatement (single thread, as the reference) on the same scene."""
+def cpu_baseline_flip(n: int, steps: int, warmup: int):
+    """Step 8 on one host core (single thread, as the reference) on the same scene,
+    timed after `warmup` updates (the first places the particles)."""
     from oracle import oracle as O
-    s = O.OracleSolver(O.FLIP, n, n, *FLIP_RHO)
+    kind = "reference" if O.ref_available(8) else "port"
+    s = cpu_solver(kind)(O.FLIP, n, n, *FLIP_RHO)
     s.set_bodies([(0,) + FLIP_BOX])
-    s.add_inflow(*FLIP_INFLOW)
-    s.update(FLIP_DT)  # first update places the particles (not timed)
+    for _ in range(max(1, warmup)):
+        s.add_inflow(*FLIP_INFLOW)
+        s.update(FLIP_DT)
     t0 = time.perf_counter()
     for _ in range(steps):
         s.add_inflow(*FLIP_INFLOW)
         s.update(FLIP_DT)
     t = time.perf_counter() - t0
-    return {"value": n * n * steps / t, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": f"{steps} update() of the {n}x{n} FLIP scene after its first step, FP64 oracle "
-                      f"(bit-identical to the reference's step-8 code), {s.particle_count()} particles",
-            "seconds": round(t, 3), "steps": steps, "particles": s.particle_count()}
+    return {"value": n * n * steps / t, "unit": METRIC, "cores": 1, "kind": kind,
+            "sample": f"updates {max(1, warmup) + 1}..{max(1, warmup) + steps} of the {n}x{n} FLIP scene, "
+                      f"{cpu_kind_text(kind)}, {s.particle_count()} particles",
+            "seconds": round(t, 3), "steps": steps, "warmup": max(1, warmup), "particles": s.particle_count()}
 
 
 def time_handle(args, local_rank, make, step, cells):
@@ -489,14 +555,17 @@ GS_INFLOW = {1: (0.45, 0.2, 0.1, 0.01, 1.0, 0.0, 3.0),      # 1-matrixless/Fluid
 GS_DT = 0.005
 
 
-def cpu_baseline_gs(variant: int, n: int, steps: int):
-    """The oracle's step-1/2 restatement (single thread, as the reference) on the same scene."""
+def cpu_baseline_gs(variant: int, n: int, steps: int, warmup: int):
+    """Steps 1-2 on one host core (single thread, as the reference) on the same
+    scene, timed after `warmup` updates."""
     from oracle import oracle as O
-    s = O.OracleSolver(variant, n, n)
+    kind = "reference" if O.ref_available(variant) else "port"
+    s = cpu_solver(kind)(variant, n, n)
     d, u, v = GS_INFLOW[variant][4:]
     x, y, w, h = GS_INFLOW[variant][:4]
-    s.add_inflow(x, y, w, h, d, 0.0, u, v)
-    s.update(GS_DT)
+    for _ in range(max(1, warmup)):
+        s.add_inflow(x, y, w, h, d, 0.0, u, v)
+        s.update(GS_DT)
     t0 = time.perf_counter()
     sweeps = 0
     for _ in range(steps):
@@ -504,10 +573,10 @@ def cpu_baseline_gs(variant: int, n: int, steps: int):
         s.update(GS_DT)
         sweeps += s.stats()[0][0]
     t = time.perf_counter() - t0
-    return {"value": n * n * steps / t, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": f"{steps} update() of the {n}x{n} step-{variant} scene after its first step "
-                      f"({sweeps} Gauss-Seidel sweeps), FP64 oracle (bit-identical to the reference)",
-            "seconds": round(t, 3), "steps": steps}
+    return {"value": n * n * steps / t, "unit": METRIC, "cores": 1, "kind": kind,
+            "sample": f"updates {max(1, warmup) + 1}..{max(1, warmup) + steps} of the {n}x{n} step-{variant} "
+                      f"scene ({sweeps} Gauss-Seidel sweeps), {cpu_kind_text(kind)}",
+            "seconds": round(t, 3), "steps": steps, "warmup": max(1, warmup)}
 
 
 def run_gs(args, local_rank):
@@ -554,23 +623,62 @@ def stratified(scs, k):
     return [order[int((j + 0.5) * len(order) / k)] for j in range(k)]
 
 
-def _cpu_batch_worker(args):
-    idx, steps, count, seed = args
+# ------------------------------------------------ per-field error check
+# The benchmark spec reports every field with its error against the reference's
+# own FP64 solve from the same state.  After the timed region the GPU state of
+# a sample of scenes is taken just before one more update; the reference's own
+# solver (oracle/_ref, built on this host from the staged sources; else the
+# oracle, pinned bit-for-bit to it) then runs that update in spawned processes
+# and the GPU's fields are compared with its result.  Nothing here is timed.
+def gpu_state(ifl, g, variant):
+    qs = [0, 2, 3] + ([1] if variant >= 6 else [])
+    return {(q, a): np.asarray(g.read_field(ifl.field_id(q, a)), dtype=np.float64) for q in qs for a in (0, 1)}
+
+
+def gpu_result(ifl, g, variant):
+    qs = [0, 2, 3] + ([1] if variant >= 6 else [])
+    out = {q: np.asarray(g.read_field(ifl.field_id(q, 0)), dtype=np.float64) for q in qs}
+    out["p"] = np.asarray(g.read_field("p"), dtype=np.float64)
+    return out
+
+
+def field_error_check(jobs, outs, gpu_iters, procs):
+    """Per-field max-norm errors of the GPU steps against the FP64 reference steps."""
     from oracle import oracle as O
+    kind = "reference" if O.ref_available(jobs[0][0]) else "oracle"
+    jobs = [j + (kind,) for j in jobs]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(max(1, min(procs, len(jobs)))) as pool:
+        refs = pool.starmap(O.step_from_state, jobs)
+    per = []
+    for j, out, ref, it in zip(jobs, outs, refs, gpu_iters):
+        e = O.field_errors(out, ref, j[0])
+        per.append({"grid": [j[1], j[2]], "pcg_iterations": {"gpu": it, "fp64": ref["stats"][0][0]},
+                    **{k: float(f"{v:.3e}") for k, v in e.items()}})
+    worst = {k: max(x[k] for x in per) for k in per[0] if k not in ("grid", "pcg_iterations")}
+    return {"against": "the reference's own FP64 solver" if kind == "reference" else
+            "the FP64 oracle (pinned bit-for-bit to the reference)",
+            "method": "one update from the GPU's state; max-norm error: p over fluid cells / max|p|, u and v / "
+                      "the largest velocity component, d / max d",
+            "max": worst, "scenes": per, "seconds": round(time.perf_counter() - t0, 1)}
+
+
+def _cpu_batch_worker(args):
+    idx, steps, warmup, count, seed, kind = args
     from ifluids import scenes
     scs = scenes.batch_scenes(count=count, seed=seed)
     spent, cells, its = 0.0, 0, []
     for i in idx:
         sc = scs[i]
-        o = O.OracleSolver(sc.variant, sc.w, sc.h)
+        o = cpu_solver(kind)(sc.variant, sc.w, sc.h)
         if sc.bodies:
             o.set_bodies(sc.bodies)
-        for k in range(1 + steps):  # one warm-up update, then the timed ones
+        for k in range(warmup + steps):  # untimed warm-up updates, then the timed ones
             for r in sc.inflows:
                 o.add_inflow(*r)
             t0 = time.perf_counter()
             o.update(sc.dt)
-            if k:
+            if k >= warmup:
                 spent += time.perf_counter() - t0
                 cells += sc.cells
                 its.append(o.stats()[0][0])
@@ -578,9 +686,12 @@ def _cpu_batch_worker(args):
     return spent, cells, its
 
 
-def cpu_baseline_batch(procs: int, steps: int = 1, sample: int = 32):
-    """The oracle over a size-stratified sample of the batch, `procs` processes."""
+def cpu_baseline_batch(procs: int, steps: int = 1, warmup: int = 3, sample: int = 32):
+    """The CPU solver over a size-stratified sample of the batch on `procs`
+    processes, timed at the GPU's step indices: every sampled scene runs
+    `warmup` untimed updates, then `steps` timed ones."""
     from ifluids import scenes
+    kind = cpu_kind()
     scs = scenes.batch_scenes(count=BATCH_COUNT, seed=BATCH_SEED)
     pick = stratified(scs, sample)
     pick.sort(key=lambda i: -scs[i].cells)
@@ -590,7 +701,7 @@ def cpu_baseline_batch(procs: int, steps: int = 1, sample: int = 32):
         j = load.index(min(load))
         shares[j].append(i)
         load[j] += scs[i].cells
-    jobs = [(sh, steps, BATCH_COUNT, BATCH_SEED) for sh in shares if sh]
+    jobs = [(sh, steps, warmup, BATCH_COUNT, BATCH_SEED, kind) for sh in shares if sh]
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(len(jobs)) as pool:
@@ -598,11 +709,13 @@ def cpu_baseline_batch(procs: int, steps: int = 1, sample: int = 32):
     wall = time.perf_counter() - t0
     slowest = max(r[0] for r in res)
     cells = sum(r[1] for r in res)
-    return {"value": cells / slowest, "unit": METRIC, "cores": len(jobs), "kind": "port",
-            "sample": f"{len(pick)} of the {BATCH_COUNT} batch scenes (size-stratified), one warm-up "
-                      f"update then {steps} timed update(s) each, FP64 oracle, scenes spread over "
-                      f"{len(jobs)} processes (value = timed cells / slowest process's timed seconds)",
-            "seconds": round(slowest, 2), "wall_seconds": round(wall, 2)}
+    return {"value": cells / slowest, "unit": METRIC, "cores": len(jobs), "kind": kind,
+            "sample": f"{len(pick)} of the {BATCH_COUNT} batch scenes (size-stratified), updates "
+                      f"{warmup + 1}..{warmup + steps} of each (after {warmup} untimed), {cpu_kind_text(kind)}, "
+                      f"FP64, scenes spread over {len(jobs)} processes (value = timed cells / slowest "
+                      f"process's timed seconds)",
+            "seconds": round(slowest, 2), "wall_seconds": round(wall, 2), "steps": steps, "warmup": warmup,
+            "sample_cells": cells // max(1, steps)}
 
 
 def run_batch(args, rank, world, local_rank):
@@ -614,8 +727,14 @@ def run_batch(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     prec = ifl.FP32 if args.precision == "fp32" else ifl.FP64
     fbytes = 4 if prec == ifl.FP32 else 8
-    scs = scenes.batch_scenes(count=args.count, seed=BATCH_SEED)
+    # N ranks: the generator's first count x N scenes, split into disjoint,
+    # balanced shares (per-GPU work stays about one count-scene batch: weak
+    # scaling); scenes exchange nothing, so no collective touches the data path
+    allscs = scenes.batch_scenes(count=args.count * world, seed=BATCH_SEED)
+    mine = shard_scenes([scene_work(x.w, x.h) for x in allscs], rank, world) if world > 1 else range(len(allscs))
+    scs = [allscs[i] for i in mine]
     cells = sum(s.cells for s in scs)
+    cells_all = sum_over_ranks(float(cells), world, dev)
 
     def build(use_graph=True):
         members, bodies = [], []
@@ -667,7 +786,18 @@ def run_batch(args, rank, world, local_rank):
     iters = [x[0][0] for x in b.stats()]
     dev_ms = sum(step_ms)
     t_max = max_over_ranks(dev_ms, world, dev)
-    value = whole_job_rate(cells, args.steps, world, t_max)
+    value = cells_all * args.steps / (t_max / 1e3)
+
+    # ---- per-field error of one more (untimed) step of a size-stratified sample
+    check = None
+    if args.field_check > 0 and rank == 0:
+        pick = stratified(scs, args.field_check)
+        jobs = [(scs[i].variant, scs[i].w, scs[i].h, gpu_state(ifl, members[i], scs[i].variant),
+                 [x.as_tuple() for x in bodies[i]], scs[i].inflows, dt) for i in pick]
+        step(b, bodies, dt)
+        st = b.stats()
+        outs = [gpu_result(ifl, members[i], scs[i].variant) for i in pick]
+        check_args = (jobs, outs, [st[i][0][0] for i in pick])
 
     # ---- end to end through the public API: pinned density readback of every scene
     host = [torch.empty((sc.h, sc.w), dtype=torch.float32, pin_memory=True).numpy() for sc in scs]
@@ -681,7 +811,7 @@ def run_batch(args, rank, world, local_rank):
         for m, hb in zip(members_e, host):
             m.read_field("d", dtype=np.float32, out=hb)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
-    e2e = {"value": whole_job_rate(cells, args.steps, world, e2e_s * 1e3), "unit": METRIC,
+    e2e = {"value": cells_all * args.steps / e2e_s, "unit": METRIC,
            "h2d_bytes_per_step": int(h2d / args.steps),
            "d2h_bytes_per_step": int(cells * 4 + be.info()["d2h_bytes_last_step"])}
     be.close()
@@ -738,9 +868,15 @@ def run_batch(args, rank, world, local_rank):
                 "sample": f"{len(pick)} of the {len(scs)} scenes (size-stratified), FP64 drop-in "
                           f"(ifl_update), one scene at a time, second update of each timed"}
     b.close()
+    if args.field_check > 0 and rank == 0:
+        check = field_error_check(*check_args, procs=min(16, os.cpu_count() or 1))
+        check["sample"] = (f"{len(check_args[0])} size-stratified scenes of the batch at update "
+                           f"{args.warmup + args.steps + 1}")
     lat = sorted(step_ms)
     pct = lambda q: lat[min(len(lat) - 1, int(math.ceil(q * len(lat))) - 1)]
     return {"value": value, "ms_per_step": t_max / args.steps, "e2e": e2e, "roofline": roof,
+            "field_error": check, "shard": {"scenes": len(scs), "of": len(allscs), "cells": cells,
+                                            "cells_all_ranks": int(cells_all)},
             "gpu_launches": launches, "clocks": clk.summary(), "fp64_dropin": fp64, "cells": cells,
             "latency_ms": {"p50": round(pct(0.50), 1), "p99": round(pct(0.99), 1)},
             "batch": {k: info[k] for k in ("members", "threads", "strips_per_block", "stages", "grid", "graph",
@@ -846,13 +982,28 @@ def main():
     ap.add_argument("--serve-steps-scale", type=float, default=0.1, help="scale of the U[50,500] steps per request")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget of the serving run")
     ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
+    ap.add_argument("--cpu-sample", type=int, default=32, help="batch: scenes of the CPU sample (size-stratified)")
     ap.add_argument("--max-team-blocks", type=int, default=0, help="batch: largest PCG team in blocks (0 = library default)")
     ap.add_argument("--shape", default="", help="batch: fixed PCG shape threads,strips_per_block,stages (default: autotuned)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--field-check", type=int, default=-1,
+                    help="scenes whose next update is compared with the FP64 reference after the timed region "
+                         "(default: 8 for the batch, 1 for the 1024^2 scene, 0 otherwise)")
     args = ap.parse_args()
     if not args.size:
         args.size = {"c3": 2048, "flip": 128, "gs": 128}.get(args.workload, 1024)
+    if args.field_check < 0:
+        args.field_check = {"batch": 8, "single": 1}.get(args.workload, 0)
 
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: start the ranks through torch.distributed.run
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr=127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+        sys.exit(subprocess.call(cmd))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -863,6 +1014,8 @@ def main():
                               f"[64, 1024], 1-3 inflow rectangles, 0-4 seeded bodies), 4-solid-boundaries, "
                               f"dt=0.0025 (configs[2])",
                   "variant": "4-solid-boundaries", "scenes": args.count, "seed": BATCH_SEED,
+                  "sharding": "one GPU per rank; N ranks split the generator's first count x N scenes into "
+                              "disjoint shares balanced by estimated work (no collective on the data path)",
                   "precision_form": args.precision,
                   "l2": "inputs larger than L2 (about 6 GB of scene state)", "scene_data": "seeded synthetic scenes"}
     elif args.workload == "flip":
@@ -895,24 +1048,25 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        steps = max(1, min(args.steps, 2))
+        # Each step is a bounded sample of the workload, timed at the same step
+        # indices as the GPU arm (after args.warmup untimed updates).
         if args.workload == "flip":
-            cb = cpu_baseline_flip(args.size, max(2, min(args.steps, 20)))
-            note = "the reference's step-8 algorithm on one host core (oracle port, bit-identical to it)"
+            cb = cpu_baseline_flip(args.size, args.steps, args.warmup)
+            note = "step 8 on one host core, as the reference runs"
         elif args.workload == "gs":
-            cb = cpu_baseline_gs(args.gs_variant, args.size, max(2, min(args.steps, 10)))
-            note = "the reference's step-1/2 algorithm on one host core (oracle port, bit-identical to it)"
+            cb = cpu_baseline_gs(args.gs_variant, args.size, args.steps, args.warmup)
+            note = "steps 1-2 on one host core, as the reference runs"
         elif batch:
-            cb = cpu_baseline_batch(procs, steps=1)
-            note = ("reference algorithm on the host cores (oracle port of the reference sources, "
-                    "bit-identical to them where they compile) over a size-stratified sample of the batch")
+            cb = cpu_baseline_batch(procs, steps=args.steps, warmup=args.warmup, sample=args.cpu_sample)
+            note = ("one reference solver per sampled scene, the sample spread over the host cores; "
+                    "ms_per_step is one step of the sample on its slowest process")
         else:
-            cb = cpu_baseline(args.size, steps, procs, args.seed)
-            note = ("reference algorithm on the host cores (oracle port of the reference sources, "
-                    "bit-identical to them where they compile); each step a full update of the scene "
-                    "in every process; steps capped to keep the run within minutes")
+            steps = max(1, min(args.steps, 2))  # one update of this scene takes ~25 s per process
+            cb = cpu_baseline(args.size, steps, args.warmup, procs, args.seed)
+            note = ("one copy of the scene per host core; steps capped at 2 to keep the run within minutes; "
+                    "ms_per_step is one update on the slowest process")
         line = {"metric": METRIC, "value": cb["value"], "unit": METRIC, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * cb["seconds"] / cb.get("steps", 1),
+                "steps": cb["steps"], "warmup": cb["warmup"], "ms_per_step": 1e3 * cb["seconds"] / cb["steps"],
                 "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
                 "impl": "reference", "cpu_baseline": cb,
@@ -924,11 +1078,13 @@ def main():
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu:  # before any GPU work (spawned pool)
         if args.workload == "flip":
-            cb = cpu_baseline_flip(args.size, 10)
+            cb = cpu_baseline_flip(args.size, 10, args.warmup)
         elif args.workload == "gs":
-            cb = cpu_baseline_gs(args.gs_variant, args.size, 5)
+            cb = cpu_baseline_gs(args.gs_variant, args.size, 5, args.warmup)
+        elif batch:
+            cb = cpu_baseline_batch(procs, steps=1, warmup=args.warmup, sample=args.cpu_sample)
         else:
-            cb = cpu_baseline_batch(procs) if batch else cpu_baseline(args.size, 1, procs, args.seed)
+            cb = cpu_baseline(args.size, 1, args.warmup, procs, args.seed)
     if world > 1:
         import torch.distributed as dist
         import torch
@@ -947,9 +1103,12 @@ def main():
             "data": "synthetic", "config": config, "e2e": r["e2e"], "roofline": r["roofline"],
             "cpu_baseline": cb, "gpu_launches": r["gpu_launches"], "clocks": r["clocks"],
             "fp64_dropin": r["fp64_dropin"]}
+    if r.get("field_error") is not None:
+        line["field_error"] = r["field_error"]
     if batch:
         line["latency_ms"] = r["latency_ms"]
         line["batch"] = r["batch"]
+        line["shard"] = r["shard"]
         if args.serve_requests > 0 and world == 1:
             line["serving"] = run_serve(args, local_rank)
     elif args.workload == "gs":

@@ -225,6 +225,15 @@ int ifl_get_stats(ifl_solver *s, ifl_step_stats *out);
  * iterations (separates rounding drift from a flip of the termination test). */
 int ifl_set_pinned_iterations(ifl_solver *s, int pressure, int heat);
 
+/* Failure detection: every device-side wait of a solve (a strip waiting for
+ * its neighbour's boundary row, a team barrier, a Gauss-Seidel progress
+ * counter) gives up after `polls` polls; the solve then runs to its end without
+ * waiting, the handle's status word gets bit 0 and ifl_get_stats returns
+ * IFL_ERR_TIMEOUT.  0 restores the default (about a second of polling).  A
+ * batch waits with the limit of its first member.  No counterpart in the
+ * reference, which has no device waits. */
+int ifl_set_wait_limit(ifl_solver *s, int64_t polls);
+
 /* Kernel timing.  When on, every kernel group launched by the handle is
  * bracketed by CUDA events on the handle's stream (no host synchronisation);
  * ifl_get_timing synchronises, returns the accumulated device time per group
@@ -270,8 +279,12 @@ int ifl_get_timing(ifl_solver *s, ifl_timing *out);
  * array, which keeps the last call's contents: calls whose work overlaps on
  * the GPU (different streams, or different host threads) race and must be
  * serialised by the caller.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture. */
+ * array's device address (cudaGetSymbolAddress) with that device current.
+ * Under CUDA's lazy module loading (the default) that lookup is also when the
+ * driver loads this library's device code and reserves the array on that
+ * device, so a caller that must not allocate while it runs should make one
+ * call per device at start-up (any grid, e.g. a 2 x 2 solve), and before any
+ * stream capture. */
 int ifl_pcg_solve_noalloc(int w, int h, const double *adiag, const double *aplusx,
                           const double *aplusy, const double *rhs, double *p, int max_iter,
                           ifl_pcg_stats *stats, void *stream);

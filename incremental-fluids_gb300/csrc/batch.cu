@@ -330,17 +330,36 @@ class BatchImpl final : public BatchBase {
 
     // Estimated PCG time of each scene: iterations x (two wavefront sweeps,
     // D + lag per strip steps each; the elementwise passes over its team).
+    // Estimated time of scene i's solves on a team of g blocks, in wavefront
+    // steps: per PCG iteration two sweeps, the elementwise passes (rows per
+    // thread, weighted 4) and the team barriers.  A sweep of S strips by P
+    // warps (strips taken round-robin) finishes after
+    //   max((S-1)*lag + D, (S-1)/P * D + ((S-1) mod P)*lag + D)
+    // steps: strip s starts lag steps after strip s-1 (the boundary-row
+    // hand-over) and not before its warp finished strip s-P.
+    double plan_cost(int i, int g) const {
+        constexpr double kLag = 48.0, kBarriers = 60.0;
+        const Scene<F> &S = scene(i);
+        const int P = g * shape_.K, Sn = S.sd.S;
+        const double D = S.sd.D;
+        const double sweep = std::max((Sn - 1) * kLag + D, ((Sn - 1) / P) * D + ((Sn - 1) % P) * kLag + D);
+        const double elem = 4.0 * (double)S.w * S.h / ((double)g * shape_.threads);
+        return iters_[i] * (2.0 * sweep + elem + kBarriers);
+    }
+
     int schedule() {
-        std::vector<double> ws(n_), we(n_);
+        // Each scene starts in the class of the smallest team that gives each
+        // of its strips its own sweeping warp; the planner then adds teams or
+        // doubles team sizes where the finish time needs them.
+        std::vector<int> cls(n_);
         for (int i = 0; i < n_; i++) {
-            const Scene<F> &S = scene(i);
-            const int g = pow2ceil((S.sd.S + shape_.K - 1) / shape_.K);
-            // wavefront steps of both sweeps (D plus ~48 steps per strip hand-over)
-            // and elementwise rows per thread of the smallest team, in comparable units
-            ws[i] = iters_[i] * 2.0 * (S.sd.D + 48.0 * (S.sd.S - 1));
-            we[i] = iters_[i] * 4.0 * (double)S.w * S.h / ((double)g * shape_.threads);
+            const int cover = pow2ceil((scene(i).sd.S + shape_.K - 1) / shape_.K);
+            int c = 0;
+            while ((1 << c) < cover && (1 << c) < 128) c++;
+            cls[i] = c;
         }
-        if (pcg_batch_schedule(plan_, ws.data(), we.data(), st_) != 0) {
+        const PlanWork work = [this](int i, int g) { return plan_cost(i, g); };
+        if (pcg_batch_schedule(plan_, cls.data(), work, st_) != 0) {
             err_ = "batched PCG schedule failed";
             return IFL_ERR_CUDA;
         }
@@ -374,6 +393,7 @@ class BatchImpl final : public BatchBase {
 
     int pcg(int heat) {
         PcgConfig cfg{PCG_FACTOR | PCG_SOLVE, 0, -2, heat};
+        cfg.wait_limit = m_[0]->wait_limit();  // the launch waits with its first member's limit
         if (check(launch_pcg_batch<F>(plan_, cfg, st_), "batched PCG launch")) return IFL_ERR_CUDA;
         launches_++;
         return IFL_OK;

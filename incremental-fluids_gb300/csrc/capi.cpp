@@ -240,6 +240,14 @@ int ifl_set_pinned_iterations(ifl_solver *s, int pressure, int heat) {
     });
 }
 
+int ifl_set_wait_limit(ifl_solver *s, int64_t polls) {
+    if (polls < 0) return IFL_ERR_ARG;
+    return guarded(s, [&](ifl::SolverBase &v) {
+        v.set_wait_limit((long long)polls);
+        return (int)IFL_OK;
+    });
+}
+
 int ifl_set_timing(ifl_solver *s, int on) {
     return guarded(s, [&](ifl::SolverBase &v) { return v.set_timing(on != 0); });
 }

@@ -19,6 +19,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -127,6 +128,7 @@ struct PcgConfig {
     int limit;
     int pinned;
     int heat;  // 1: writes to the heat PcgOut slot
+    long long wait_limit = 0;  // polls of one device-side wait before it gives up; 0: about a second
 };
 
 // Launch shape of the batched PCG kernel (chosen by the batch autotuner).
@@ -164,7 +166,8 @@ cudaError_t launch_pcg_f32(const Scene<double> &S, const PcgF32 &M, const PcgScr
                            cudaStream_t st, int *blocks_used);
 // Gauss-Seidel solve of steps 1-2 (k_gs.cu): one CTA, h <= gs_max_rows().
 template <typename F>
-cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st);
+cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st,
+                      long long wait_limit = 0);
 int gs_max_rows();
 
 // Batched PCG: many scenes in one cooperative launch (k_pcg.cu).  The plan
@@ -176,13 +179,21 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
 void pcg_batch_destroy(PcgBatchPlan *P);
 int pcg_batch_grid(const PcgBatchPlan *P);
 size_t pcg_batch_table_bytes(const PcgBatchPlan *P);  // team/queue tables uploaded per schedule
-// Rebuilds teams and queues from the estimated work per scene: the wavefront
-// part and the elementwise part at the smallest team (stream-ordered upload).
-int pcg_batch_schedule(PcgBatchPlan *P, const double *work_sweep, const double *work_elem, cudaStream_t st);
-// Team plan (host only): class c holds the scenes whose strips need 2^c
-// blocks; teams[c] teams of tsize[c] blocks serve it; queues[c] = its scenes by
-// decreasing work.  work_elem may be null.  Teams grow up to max_team blocks.
-// Returns the blocks used, -1 if the grid is too small.
+// Estimated time of scene i's solves on a team of g blocks (planner cost model).
+using PlanWork = std::function<double(int i, int g)>;
+// Rebuilds teams and queues (stream-ordered upload): scene i starts in class
+// first_class[i] (teams of 2^c blocks; a team sweeps its scene's strips
+// round-robin, so any team size serves any scene).
+int pcg_batch_schedule(PcgBatchPlan *P, const int *first_class, const PlanWork &work, cudaStream_t st);
+// Team plan (host only): class c holds the scenes that start in it; teams[c]
+// teams of tsize[c] blocks serve it; queues[c] = its scenes by decreasing
+// work.  Teams grow up to max_team blocks.  Returns the blocks used, -1 if
+// the grid is too small.
+int pcg_plan_teams_fn(int grid, int n, const int *first_class, const PlanWork &work, int *teams, int *tsize,
+                      std::vector<std::vector<int>> *queues, int max_team = 128);
+// The same with scenes in the class of the smallest team that gives each of
+// their strips its own sweeping warp, work = work_sweep + work_elem scaled by
+// the team size (work_elem may be null).
 int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
                    const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues,
                    int max_team = 128);

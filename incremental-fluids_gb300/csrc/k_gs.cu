@@ -48,6 +48,7 @@ struct GsArgs {
     SDIdx sd;
     double scale;  // timestep / (density * hx * hx)
     int limit, pinned;
+    long long spin_limit;  // polls of one progress-counter wait before the solve gives up
     PcgOut *out;
     unsigned *flags;
     unsigned long long *iter_total;
@@ -68,7 +69,7 @@ __device__ __forceinline__ void gs_wait(const GsArgs &A, int i, unsigned long lo
     long long spins = 0;
     while ((seen = *(const volatile unsigned long long *)(A.prog + i)) < need) {
         if (gs_aborted(A)) return;
-        if (++spins > kSpinLimit) gs_abort(A);
+        if (++spins > A.spin_limit) gs_abort(A);
     }
 }
 // Whole warp: every strip has done `need` steps (finished a sweep).
@@ -252,7 +253,8 @@ constexpr int kSpreadBytes = 120 * 1024;  // one such CTA per SM
 int gs_max_rows() { return 32 * 4096; }
 
 template <typename F>
-cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st) {
+cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int limit, int pinned, cudaStream_t st,
+                      long long wait_limit) {
     const int strips = S.sd.S;
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -274,6 +276,7 @@ cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int lim
     A.scale = dt / (S.rho_air * S.hx * S.hx);
     A.limit = limit;
     A.pinned = pinned;
+    A.spin_limit = wait_limit > 0 ? wait_limit : kSpinLimit;
     A.out = X.out;
     A.flags = S.flags;
     A.iter_total = X.iter_total;
@@ -285,7 +288,9 @@ cudaError_t launch_gs(const Scene<F> &S, const PcgScratch &X, double dt, int lim
     return cudaLaunchCooperativeKernel((const void *)gs_kernel, dim3(strips), dim3(32), args, (size_t)smem, st);
 }
 
-template cudaError_t launch_gs<double>(const Scene<double> &, const PcgScratch &, double, int, int, cudaStream_t);
-template cudaError_t launch_gs<float>(const Scene<float> &, const PcgScratch &, double, int, int, cudaStream_t);
+template cudaError_t launch_gs<double>(const Scene<double> &, const PcgScratch &, double, int, int, cudaStream_t,
+                                       long long);
+template cudaError_t launch_gs<float>(const Scene<float> &, const PcgScratch &, double, int, int, cudaStream_t,
+                                      long long);
 
 }  // namespace ifl

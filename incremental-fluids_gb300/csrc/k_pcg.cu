@@ -59,7 +59,12 @@ constexpr int kChunk = kPcgChunk;  // diagonals per reduction chunk of the eleme
 // full batch steps (30.7 M against 36.5 M cell-steps/s): the second warp of a
 // 64-thread block, which works only in the elementwise passes, pays for more.
 constexpr int kB = kSweepBlock;
-constexpr long long kWaitLimit = 1ll << 22;      // ~1 s of polling
+// Default polls of a halo-word or barrier wait (about a second); the host may
+// set another limit per solve (PcgConfig::wait_limit).  The mbarrier waits of
+// the bulk-copy rings keep their own fixed limit: they wait for copies this
+// warp issued from this GPU's memory, which always complete, and a timed-out
+// sweep still waits for every copy it issued before it leaves.
+constexpr long long kWaitLimit = 1ll << 22;
 constexpr long long kMbarWaitLimit = 1ll << 20;  // try_wait suspends between polls
 constexpr double kTau = 0.97, kSigma = 0.25, kTol = 1e-5;
 constexpr unsigned long long kSentinel = ~0ull;
@@ -70,6 +75,7 @@ constexpr unsigned FULL = 0xffffffffu;
 // wait marks both, so every later wait of the launch stops waiting.
 struct Flags {
     unsigned *scene, *all;
+    long long limit;  // polls of one halo or barrier wait before it gives up
 };
 
 // The blocks that solve one scene: ranks 0..size-1, their barrier words and
@@ -156,7 +162,7 @@ __device__ void team_barrier(const Team &T, const Flags &fl) {
         } else {
             long long n = 0;
             while (ld_volatile(bar + 1) == g) {
-                if (++n > kWaitLimit || timed_out(fl)) {
+                if (++n > fl.limit || timed_out(fl)) {
                     set_timeout(fl);
                     break;
                 }
@@ -220,7 +226,7 @@ __device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, un
     while (v == kSentinel) {
         v = hload(c, x);
         if (v != kSentinel) break;
-        if (++n > kWaitLimit || timed_out(flags)) {
+        if (++n > flags.limit || timed_out(flags)) {
             set_timeout(flags);
             v = 0;
             break;
@@ -240,6 +246,8 @@ __device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, un
 // ly = aPlusY*pc, pc = precon, storage precision; written by the factor).
 // ii / ci count issued / consumed blocks over the whole kernel, so buffer =
 // count % stages and mbarrier parity = (count/stages) & 1.
+// A ring is `dead` once one of its mbarrier waits ran out (a copy that never
+// completed): it then issues and waits for nothing more.
 template <typename F>
 struct Ring {
     static constexpr unsigned kSlot = kB * 32 * sizeof(F);
@@ -248,24 +256,35 @@ struct Ring {
     unsigned bars;  // byte offset of this warp's mbarriers in g_smem
     int stages;
     unsigned ii, ci;
+    bool dead;
     __device__ __forceinline__ uint64_t *bar(unsigned st) const { return (uint64_t *)(g_smem + bars) + st; }
 };
 
+// Wait for the oldest issued block.  A timeout elsewhere in the launch does not
+// shorten this wait: the copy was issued by this warp from this GPU's memory
+// and completes, and a stage is re-armed only after its previous phase
+// completed, so the ring never leaves a bulk copy writing shared memory behind
+// (every sweep consumes every block it issued).
 template <typename F>
 __device__ __forceinline__ void ring_wait(Ring<F> &R, const Flags &flags) {
     const unsigned st = R.ci % R.stages, parity = (R.ci / R.stages) & 1u;
     long long n = 0;
-    while (!mbar_try_wait(R.bar(st), parity)) {
-        if (++n > kMbarWaitLimit || timed_out(flags)) {
+    while (!R.dead && !mbar_try_wait(R.bar(st), parity)) {
+        if (++n > kMbarWaitLimit) {
             set_timeout(flags);
-            break;
+            R.dead = true;
         }
     }
+    R.dead = __any_sync(FULL, R.dead);  // the whole warp issues and waits alike
     R.ci++;
 }
 
 template <int KIND, typename F>
 __device__ __forceinline__ void ring_issue(Ring<F> &R, const PcgArgs<F> &A, int s, int blk) {
+    if (R.dead) {
+        R.ii++;
+        return;
+    }
     constexpr unsigned S1 = Ring<F>::kSlot;
     const int D = A.sd.D;
     const int d0 = (KIND == 2) ? D - (blk + 1) * kB : blk * kB;
@@ -533,28 +552,46 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
     __syncwarp();
 }
 
-// Sweep of all strips of this block; the halo rows between its own warps live
-// in shared memory, those to neighbouring blocks in global memory.
+// Sweep of all strips of this block.  The team's T.size*K sweeping warps take
+// the strips round-robin: warp `base` sweeps strips base, base + P, base + 2P,
+// ... (P = T.size*K), in increasing order for the factor and the forward
+// solve and in decreasing order for the backward solve, so that every strip
+// waits only on a strip that is swept earlier by its own warp or by another
+// warp in the same or an earlier round (no cycle).  A team therefore needs
+// fewer blocks than its scene has strips: while a tall scene's pipeline fills
+// and drains, the warps that would idle in a one-strip-per-warp schedule sweep
+// their next strip.  When every warp has a single strip, the halo rows between
+// the warps of one block live in shared memory; otherwise every strip hands its
+// boundary row over through its own global row (a shared row would be reused
+// by the next round while its reader may still need it).
 // hsm_off: byte offset in g_smem of the K-1 shared halo rows (D words each).
 template <int KIND, typename F>
 __device__ void sweep(const PcgArgs<F> &A, const Team &T, Ring<F> &R, unsigned hsm_off, int nstrips_blk) {
     const int w = threadIdx.x >> 5;
     if (w >= nstrips_blk) return;
     const SDIdx sd = A.sd;
-    const int s = T.rank * A.K + w;
+    const int P = T.size * A.K;
+    const int base = T.rank * A.K + w;
     const size_t D = sd.D;
     unsigned long long *up = A.halo, *down = A.halo + (size_t)sd.S * D;
     auto smem_row = [&](int k) { return Chan{hsm_off + 8u * (unsigned)(k * D), nullptr, true, true}; };
     auto glob_row = [&](unsigned long long *row) { return Chan{0u, row, false, true}; };
-    Chan in{0u, nullptr, false, false}, out{0u, nullptr, false, false};
-    if (KIND != 2) {  // rows travel upward: strip s takes from s-1, gives to s+1
-        if (s > 0) in = (w > 0) ? smem_row(w - 1) : glob_row(up + (size_t)(s - 1) * D);
-        if (s + 1 < sd.S) out = (w + 1 < nstrips_blk) ? smem_row(w) : glob_row(up + (size_t)s * D);
-    } else {          // downward: strip s takes from s+1, gives to s-1
-        if (s + 1 < sd.S) in = (w + 1 < nstrips_blk) ? smem_row(w) : glob_row(down + (size_t)(s + 1) * D);
-        if (s > 0) out = (w > 0) ? smem_row(w - 1) : glob_row(down + (size_t)s * D);
+    const bool one_round = sd.S <= P;
+    const int nmine = (sd.S - base + P - 1) / P;  // strips of this warp
+    for (int j0 = 0; j0 < nmine; j0++) {
+        const int s = base + (KIND == 2 ? nmine - 1 - j0 : j0) * P;
+        Chan in{0u, nullptr, false, false}, out{0u, nullptr, false, false};
+        if (KIND != 2) {  // rows travel upward: strip s takes from s-1, gives to s+1
+            if (s > 0) in = (one_round && w > 0) ? smem_row(w - 1) : glob_row(up + (size_t)(s - 1) * D);
+            if (s + 1 < sd.S)
+                out = (one_round && w + 1 < nstrips_blk) ? smem_row(w) : glob_row(up + (size_t)s * D);
+        } else {          // downward: strip s takes from s+1, gives to s-1
+            if (s + 1 < sd.S)
+                in = (one_round && w + 1 < nstrips_blk) ? smem_row(w) : glob_row(down + (size_t)(s + 1) * D);
+            if (s > 0) out = (one_round && w > 0) ? smem_row(w - 1) : glob_row(down + (size_t)s * D);
+        }
+        sweep_strip<KIND, F>(A, s, R, in, out);
     }
-    sweep_strip<KIND, F>(A, s, R, in, out);
 }
 
 // Shared-memory layout of a PCG block: mbarriers (32 bytes per warp) | the
@@ -572,6 +609,7 @@ __device__ void ring_init(Ring<F> &R, int K, int stages) {
     R.bars = 32u * warp;
     R.stages = stages;
     R.ii = R.ci = 0;
+    R.dead = false;
     if (warp < K && lane == 0) {
         for (int k = 0; k < stages; k++) mbar_init(R.bar(k), 1);
         fence_mbar_init();
@@ -616,6 +654,7 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
         __syncthreads();
         return r;
     };
+    // sweeping warps of this block that own at least one strip
     int nstrips_blk = sd.S - T.rank * A.K;
     nstrips_blk = nstrips_blk < 0 ? 0 : (nstrips_blk > A.K ? A.K : nstrips_blk);
     constexpr bool kF32 = !std::is_same<F, double>::value;
@@ -899,6 +938,7 @@ struct BatchTeams {
     unsigned *grid_bar;       // two barrier words over the whole grid (zero at launch)
     unsigned *remap_fail;     // set when a block could not be placed (zero at launch)
     int nsm, per, remap;
+    long long wait_limit;     // polls of one halo or barrier wait
 };
 
 // At most 128 registers per thread whatever the block size.
@@ -908,7 +948,7 @@ __global__ void __launch_bounds__(kThreads, 512 / kThreads)
     __shared__ double sm[kMaxWarps + 1];
     __shared__ PcgArgs<F> sA;
     __shared__ int s_slot;
-    const Flags launch_fl{B.all, B.all};
+    const Flags launch_fl{B.all, B.all, B.wait_limit};
     if (threadIdx.x == 0) {
         int slot = (int)blockIdx.x;
         if (B.remap) {
@@ -954,6 +994,7 @@ __global__ void __launch_bounds__(kThreads, 512 / kThreads)
             sA.K = K;
             sA.stages = stages;
             sA.fl.all = B.all;
+            sA.fl.limit = B.wait_limit;
         }
         // halo rows start at the sentinel: the shared rows of this block
         // (their length changes with the scene) and the scene's global rows
@@ -1099,6 +1140,7 @@ cudaError_t launch_pcg_with(PcgArgs<F> A, const SDIdx &sd, const PcgScratch &X, 
     A.K = strips_per_block<F>();
     if (A.K > sd.S) A.K = sd.S;
     A.stages = kStages;
+    A.fl.limit = cfg.wait_limit > 0 ? cfg.wait_limit : kWaitLimit;
     const size_t smem = smem_bytes<F>(A.K, sd.D);
     const int threads = 512;
     const void *fn = (const void *)pcg_kernel<F, 512>;
@@ -1113,8 +1155,10 @@ cudaError_t launch_pcg_with(PcgArgs<F> A, const SDIdx &sd, const PcgScratch &X, 
     if (want < need) want = need;
     int G = want < maxb ? want : maxb;
     if (blocks_used) *blocks_used = G;
-    cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
-    cudaMemsetAsync(X.halo, 0xff, 2 * (size_t)sd.S * sd.D * sizeof(unsigned long long), st);
+    cudaError_t e = cudaMemsetAsync(X.barrier, 0, 2 * sizeof(unsigned), st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(X.halo, 0xff, 2 * (size_t)sd.S * sd.D * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
     void *args[] = {&A};
     return cudaLaunchCooperativeKernel(fn, dim3(G), dim3(threads), args, smem, st);
 }
@@ -1174,15 +1218,8 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
         shape.K > shape.threads / 32 ||
         shape.stages < 2 || shape.stages > 4)
         return fail("unsupported batched PCG shape");
-    int dmax = 0, smax_ = 0;
-    for (int i = 0; i < n; i++) {
-        dmax = std::max(dmax, scenes[i]->sd.D);
-        smax_ = std::max(smax_, scenes[i]->sd.S);
-    }
-    const int need_max = (smax_ + shape.K - 1) / shape.K;
-    int cls = 0;
-    while ((1 << cls) < need_max) cls++;
-    if (cls >= kMaxClasses) return fail("scene too tall for the batched PCG shape");
+    int dmax = 0;
+    for (int i = 0; i < n; i++) dmax = std::max(dmax, scenes[i]->sd.D);
     const size_t smem = smem_bytes<F>(shape.K, dmax, shape.stages);
     const void *fn = batch_fn<F>(shape.threads);
     int dev = 0, sms = 0, per = 0, optin = 0;
@@ -1198,10 +1235,7 @@ PcgBatchPlan *pcg_batch_create(const Scene<F> *const *scenes, const PcgScratch *
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, shape.threads, smem);
     const int grid = sms * per;
-    // every class may need a team of its size
-    int need_all = 0;
-    for (int c = 0; c <= cls; c++) need_all += 1 << c;
-    if (grid < need_all) return fail("too few co-resident blocks for the batched PCG shape");
+    if (grid < 1) return fail("too few co-resident blocks for the batched PCG shape");
 
     PcgBatchPlan *P = new PcgBatchPlan;
     P->precision = (int)sizeof(F);
@@ -1331,43 +1365,38 @@ int pcg_batch_grid(const PcgBatchPlan *P) { return P->grid; }
 size_t pcg_batch_table_bytes(const PcgBatchPlan *P) { return P->tab_bytes; }
 void pcg_batch_set_max_team(PcgBatchPlan *P, int blocks) { P->max_team = blocks > 0 ? blocks : 128; }
 
-// Teams and queues from the estimated work of each scene: work_sweep (the
-// wavefront part, which more blocks do not shorten) and work_elem (the
-// elementwise part at the smallest team, which shrinks with the team).
-// Scenes go to the class of the smallest power-of-two team that covers their
-// strips; every non-empty class gets one team.  Then, while blocks are left,
-// the class with the latest estimated finish (its work over its teams, or its
-// largest scene) gets one more team or teams twice as large (up to max_team
-// blocks), whichever shortens that finish most per block spent, as long as it
-// improves.  Each queue is ordered by work, largest first.  teams[c] and
-// tsize[c] give the teams of class c; returns the blocks in teams, or -1 when
-// the classes' first teams alone exceed the grid.
-int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
-                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues,
-                   int max_team) {
+// Teams and queues from a cost model: work(i, g) = estimated time of scene i's
+// solves on a team of g blocks.  Scene i starts in class first_class[i] (teams
+// of 2^c blocks).  Every non-empty class gets one team; then, while blocks are
+// left, the class with the latest estimated finish (its work over its teams,
+// or its largest scene) gets one more team or teams twice as large (up to
+// max_team blocks), whichever shortens that finish most per block spent, as
+// long as it improves.  Each queue is ordered by work, largest first.
+// teams[c] and tsize[c] give the teams of class c; returns the blocks in
+// teams, or -1 when the classes' first teams alone exceed the grid.
+int pcg_plan_teams_fn(int grid, int n, const int *first_class, const PlanWork &work, int *teams, int *tsize,
+                      std::vector<std::vector<int>> *queues, int max_team) {
     std::vector<std::vector<int>> members(kMaxClasses);
     for (int i = 0; i < n; i++) {
-        const int need = (strips[i] + K - 1) / K;
-        int c = 0;
-        while ((1 << c) < need) c++;
-        if (c >= kMaxClasses) return -1;
+        const int c = first_class[i];
+        if (c < 0 || c >= kMaxClasses) return -1;
         members[c].push_back(i);
     }
-    auto w = [&](int i, int mult) { return work_sweep[i] + (work_elem ? work_elem[i] / mult : 0.0); };
-    int mult[kMaxClasses];
+    int size[kMaxClasses];
     double tot[kMaxClasses], big[kMaxClasses];
-    auto account = [&](int c) {
-        tot[c] = big[c] = 0.0;
+    auto account = [&](int c, int g, double *t, double *b) {
+        *t = *b = 0.0;
         for (int i : members[c]) {
-            tot[c] += w(i, mult[c]);
-            big[c] = std::max(big[c], w(i, mult[c]));
+            const double v = work(i, g);
+            *t += v;
+            *b = std::max(*b, v);
         }
     };
     for (int c = 0; c < kMaxClasses; c++) {
-        mult[c] = 1;
+        size[c] = 1 << c;
         std::stable_sort(members[c].begin(), members[c].end(),
-                         [&](int a, int b) { return w(a, 1) > w(b, 1); });
-        account(c);
+                         [&](int a, int b) { return work(a, 1 << c) > work(b, 1 << c); });
+        account(c, size[c], &tot[c], &big[c]);
     }
     int left = grid;
     for (int c = 0; c < kMaxClasses; c++) {
@@ -1387,46 +1416,63 @@ int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work
             }
         }
         if (best < 0) break;
-        const int c = best, size = (1 << c) * mult[c];
+        const int c = best, sz = size[c];
         // one more team of the current size
-        const bool can_add = teams[c] < (int)members[c].size() && size <= left;
+        const bool can_add = teams[c] < (int)members[c].size() && sz <= left;
         const double fin_add = can_add ? std::max(tot[c] / (teams[c] + 1), big[c]) : bt;
         // every team of the class twice as large
-        const bool can_grow = work_elem && size * 2 <= max_team && teams[c] * size <= left;
-        double fin_grow = bt;
+        const bool can_grow = sz * 2 <= max_team && teams[c] * sz <= left;
+        double fin_grow = bt, tg = 0.0, bg = 0.0;
         if (can_grow) {
-            mult[c] *= 2;
-            account(c);
-            fin_grow = std::max(tot[c] / teams[c], big[c]);
-            mult[c] /= 2;
-            account(c);
+            account(c, 2 * sz, &tg, &bg);
+            fin_grow = std::max(tg / teams[c], bg);
         }
         // the option that shortens the finish most per block spent
-        const double gain_add = can_add ? (bt - fin_add) / size : 0.0;
-        const double gain_grow = can_grow ? (bt - fin_grow) / ((double)teams[c] * size) : 0.0;
+        const double gain_add = can_add ? (bt - fin_add) / sz : 0.0;
+        const double gain_grow = can_grow ? (bt - fin_grow) / ((double)teams[c] * sz) : 0.0;
         if (gain_add > 0.0 && gain_add >= gain_grow) {
             teams[c]++;
-            left -= size;
+            left -= sz;
         } else if (gain_grow > 0.0) {
-            left -= teams[c] * size;
-            mult[c] *= 2;
-            account(c);
+            left -= teams[c] * sz;
+            size[c] = 2 * sz;
+            tot[c] = tg;
+            big[c] = bg;
         } else {
             break;
         }
     }
-    for (int c = 0; c < kMaxClasses; c++) tsize[c] = (1 << c) * mult[c];
+    for (int c = 0; c < kMaxClasses; c++) tsize[c] = size[c];
     if (queues) *queues = std::move(members);
     return grid - left;
 }
 
-int pcg_batch_schedule(PcgBatchPlan *P, const double *work_sweep, const double *work_elem, cudaStream_t st) {
+// Host preview and the original model: scenes go to the class of the
+// smallest power-of-two team that covers their strips (one sweeping warp per
+// strip); work = work_sweep (the wavefront part, which more blocks do not
+// shorten) + work_elem (the elementwise part at that smallest team, which
+// shrinks with the team).
+int pcg_plan_teams(int grid, int K, int n, const int *strips, const double *work_sweep,
+                   const double *work_elem, int *teams, int *tsize, std::vector<std::vector<int>> *queues,
+                   int max_team) {
+    std::vector<int> cls(n);
+    for (int i = 0; i < n; i++) {
+        const int need = (strips[i] + K - 1) / K;
+        int c = 0;
+        while ((1 << c) < need) c++;
+        if (c >= kMaxClasses) return -1;
+        cls[i] = c;
+    }
+    const PlanWork w = [&](int i, int g) {
+        return work_sweep[i] + (work_elem ? work_elem[i] * (double)(1 << cls[i]) / g : 0.0);
+    };
+    return pcg_plan_teams_fn(grid, n, cls.data(), w, teams, tsize, queues, max_team);
+}
+
+int pcg_batch_schedule(PcgBatchPlan *P, const int *first_class, const PlanWork &work, cudaStream_t st) {
     int teams[kMaxClasses], tsize[kMaxClasses];
     std::vector<std::vector<int>> members;
-    if (pcg_plan_teams(P->grid, P->shape.K, P->n, P->strips.data(), work_sweep, work_elem, teams, tsize, &members,
-                       P->max_team) <
-        0)
-        return -1;
+    if (pcg_plan_teams_fn(P->grid, P->n, first_class, work, teams, tsize, &members, P->max_team) < 0) return -1;
     // host tables
     if (cudaEventSynchronize(P->uploaded) != cudaSuccess) return -2;  // staging free again
     char *h = P->host;
@@ -1468,6 +1514,7 @@ cudaError_t launch_pcg_batch(PcgBatchPlan *P, const PcgConfig &cfg, cudaStream_t
     if (e != cudaSuccess) return e;
     const PcgArgs<F> *jobs = (const PcgArgs<F> *)P->jobs[cfg.heat ? 1 : 0];
     BatchTeams B = P->B;
+    B.wait_limit = cfg.wait_limit > 0 ? cfg.wait_limit : kWaitLimit;
     int mode = cfg.mode, heat = cfg.heat, pinned = cfg.pinned, K = P->shape.K, stages = P->shape.stages;
     void *args[] = {&jobs, &B, &mode, &heat, &pinned, &K, &stages};
     return cudaLaunchCooperativeKernel(batch_fn<F>(P->shape.threads), dim3(P->grid), dim3(P->shape.threads), args,

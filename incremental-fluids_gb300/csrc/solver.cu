@@ -604,6 +604,7 @@ class SolverImpl final : public SolverBase {
         cfg.limit = heat ? prm_.max_iter_heat : prm_.max_iter_pressure;
         cfg.pinned = heat ? pinned_heat_ : pinned_;
         cfg.heat = heat ? 1 : 0;
+        cfg.wait_limit = wait_limit_;
         int G = 0;
         int t = tbegin(IFL_K_PCG);
         cudaError_t e;
@@ -622,7 +623,7 @@ class SolverImpl final : public SolverBase {
     // project() of steps 1-2: Gauss-Seidel sweeps on p, which persists between steps.
     int gauss_seidel(double dt) {
         int t = tbegin(IFL_K_PCG);
-        cudaError_t e = launch_gs<F>(S_, scratch_, dt, prm_.max_iter_pressure, pinned_, stream_);
+        cudaError_t e = launch_gs<F>(S_, scratch_, dt, prm_.max_iter_pressure, pinned_, stream_, wait_limit_);
         tend(t);
         if (check(e, "gauss-seidel launch")) return IFL_ERR_CUDA;
         launches_++;

@@ -61,6 +61,8 @@ class SolverBase {
         pinned_ = pressure;
         pinned_heat_ = heat;
     }
+    void set_wait_limit(long long polls) { wait_limit_ = polls; }
+    long long wait_limit() const { return wait_limit_; }
     int set_timing(bool on);
     int get_timing(ifl_timing *out);
     virtual int read_iteration_total(long long *out) = 0;
@@ -92,6 +94,7 @@ class SolverBase {
     std::vector<ifl_body> bodies_;
     bool bodies_dirty_ = false;
     int pinned_ = -1, pinned_heat_ = -1;
+    long long wait_limit_ = 0;  // polls of one device-side wait; 0: the default (about a second)
     uint32_t steps_ = 0;
     int64_t launches_ = 0;
     std::string err_;

@@ -42,7 +42,7 @@ EXPORTS = ("ifl_default_params", "ifl_create", "ifl_destroy", "ifl_set_bodies", 
            "ifl_field_shape", "ifl_read_field", "ifl_write_field", "ifl_render", "ifl_flip", "ifl_get_stats",
            "ifl_flip_init", "ifl_particle_count", "ifl_read_particles", "ifl_write_particles",
            "ifl_set_particle_count", "ifl_get_rng_state", "ifl_set_rng_state",
-           "ifl_set_pinned_iterations", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
+           "ifl_set_pinned_iterations", "ifl_set_wait_limit", "ifl_synchronize", "ifl_stream", "ifl_launch_count",
            "ifl_set_timing", "ifl_get_timing", "ifl_pcg_solve_noalloc",
            "ifl_batch_default_options", "ifl_batch_create", "ifl_batch_destroy", "ifl_batch_set_inflows",
            "ifl_batch_update", "ifl_batch_get_stats", "ifl_batch_get_info", "ifl_batch_stream",
@@ -176,6 +176,7 @@ def load_library(path: str = LIB_PATH):
     L.ifl_render.argtypes = [vp, i, vp, sz, i]
     L.ifl_get_stats.argtypes = [vp, C.POINTER(StepStats)]
     L.ifl_set_pinned_iterations.argtypes = [vp, i, i]
+    L.ifl_set_wait_limit.argtypes = [vp, C.c_int64]
     L.ifl_synchronize.argtypes = [vp]
     L.ifl_set_timing.argtypes = [vp, i]
     L.ifl_pcg_solve_noalloc.argtypes = [i, i, vp, vp, vp, vp, vp, i, vp, vp]
@@ -477,6 +478,10 @@ class FluidSolver:
     def set_pinned_iterations(self, pressure: int, heat: int = -1):
         """-1: stop on the residual test; k >= 0: run exactly k PCG iterations."""
         self._check(self._L.ifl_set_pinned_iterations(self._h, pressure, heat), "pinned")
+
+    def set_wait_limit(self, polls: int):
+        """Polls of one device-side wait before the solve reports IFL_ERR_TIMEOUT (0: about a second)."""
+        self._check(self._L.ifl_set_wait_limit(self._h, int(polls)), "wait_limit")
 
     def stats(self):
         st = StepStats()

@@ -10,8 +10,8 @@ Two back-ends with one interface:
   only where the reference checkout was available at build time and is used to
   pin ``OracleSolver`` bit-for-bit.
 
-Only tests, ``__graft_entry__.smoke`` and bench.py's CPU-baseline leg may use
-this module.  Bodies are plain tuples
+Only tests, ``__graft_entry__.smoke`` and bench.py's CPU-baseline leg and
+its untimed per-field error check may use this module, as the checker.  Bodies are plain tuples
 ``(type, pos_x, pos_y, scale_x, scale_y, theta, vel_x, vel_y, vel_theta)``
 with type 0 = box (full side lengths) and 1 = sphere (diameter in scale_x).
 """
@@ -381,3 +381,58 @@ class RefSolver:
             m = C.c_int()
             ptr = self.L.ref_particles(self.p, k, C.byref(m))
             np.ctypeslib.as_array(ptr, shape=(cap,))[:n] = np.asarray(a, dtype=np.float64)
+
+
+# ------------------------------------------------------ one step from a state
+def step_from_state(variant: int, w: int, h: int, state, bodies=(), inflows=(), dt: float = 0.0025,
+                    kind: str = "oracle", density: float = 0.1, density_soot: float = 1.0,
+                    diffusion: float = 0.01, pinned: int = -1):
+    """One FP64 update() from a given state, as the per-step parity checks need it.
+
+    A fresh solver (kind "oracle": the C restatement; "reference": the
+    reference's own solver from oracle/_ref) gets `state` — a dict
+    {(quantity, A_SRC or A_DST): 2-D array} holding every advected quantity's
+    source and target buffers, the whole state that update() carries from one
+    step to the next (the pressure starts at zero inside project()) — then the
+    bodies (tuples, their state for this step), the inflow rectangles in call
+    order and one update(dt).  Returns the pressure, the advected quantities,
+    the fluid mask of the pressure grid (solid variants: the reference keeps
+    stale pressure at solid cells) and the PCG outcome.  Runs in any process
+    (picklable arguments and result), e.g. a spawned pool.
+    """
+    S = RefSolver if kind == "reference" else OracleSolver
+    o = S(variant, w, h, density, density_soot, diffusion)
+    if bodies:
+        o.set_bodies([tuple(b) for b in bodies])
+    for (q, a), arr in state.items():
+        o.array(q, a)[...] = np.asarray(arr, dtype=np.float64)
+    if pinned >= 0:
+        o.set_pinned_iterations(pinned, pinned)
+    for r in inflows:
+        o.add_inflow(*r)
+    o.update(dt)
+    qs = [QD, QU, QV] + ([QT] if variant >= HEAT else [])
+    out = {q: o.array(q, A_SRC).copy() for q in qs}
+    out["p"] = o.array(0, A_P).copy()
+    out["fluid"] = (o.bytes(QD, B_CELL) == 0) if variant >= SOLID else np.ones((h, w), dtype=bool)
+    out["stats"] = o.stats()
+    return out
+
+
+def field_errors(gpu, ref, variant: int):
+    """Max-norm errors of a GPU step against a reference step from the same state.
+
+    p over fluid cells relative to the reference's largest |p| there; u and v
+    relative to the largest velocity component (the velocity field's scale);
+    d (and T) relative to their own largest value."""
+    def rel(a, b, den):
+        return float(np.abs(a - b).max() / den) if a.size else 0.0
+    m = ref["fluid"]
+    pden = max(float(np.abs(ref["p"][m]).max()) if m.any() else 0.0, 1e-300)
+    vden = max(float(np.abs(ref[QU]).max()), float(np.abs(ref[QV]).max()), 1e-300)
+    out = {"p": rel(gpu["p"][m], ref["p"][m], pden),
+           "u": rel(gpu[QU], ref[QU], vden), "v": rel(gpu[QV], ref[QV], vden),
+           "d": rel(gpu[QD], ref[QD], max(float(np.abs(ref[QD]).max()), 1e-300))}
+    if variant >= HEAT:
+        out["T"] = rel(gpu[QT], ref[QT], max(float(np.abs(ref[QT]).max()), 1e-300))
+    return out
