@@ -248,6 +248,10 @@ __device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, un
 // count % stages and mbarrier parity = (count/stages) & 1.
 // A ring is `dead` once one of its mbarrier waits ran out (a copy that never
 // completed): it then issues and waits for nothing more.
+//
+// The same warp state carries the staging area of the elementwise passes:
+// sbuf/sbytes (this warp's share of the block's ring memory, idle outside the
+// sweeps), the staging mbarrier at sbar and its completed phases sphase.
 template <typename F>
 struct Ring {
     static constexpr unsigned kSlot = kB * 32 * sizeof(F);
@@ -257,7 +261,10 @@ struct Ring {
     int stages;
     unsigned ii, ci;
     bool dead;
+    unsigned sbuf, sbytes, sbar, sphase;
+    bool sdead;
     __device__ __forceinline__ uint64_t *bar(unsigned st) const { return (uint64_t *)(g_smem + bars) + st; }
+    __device__ __forceinline__ uint64_t *stage_bar() const { return (uint64_t *)(g_smem + sbar); }
 };
 
 // Wait for the oldest issued block.  A timeout elsewhere in the launch does not
@@ -594,15 +601,17 @@ __device__ void sweep(const PcgArgs<F> &A, const Team &T, Ring<F> &R, unsigned h
     }
 }
 
-// Shared-memory layout of a PCG block: mbarriers (32 bytes per warp) | the
-// K-1 halo rows between its strips (D words each) | the per-warp rings.
-__device__ __forceinline__ unsigned halo_offset(int K) { return 32u * K; }
-__device__ __forceinline__ unsigned ring_offset(int K, int D) {
+// Shared-memory layout of a PCG block: ring mbarriers (32 bytes per sweeping
+// warp) | staging mbarriers (8 bytes per warp, kMaxWarps) | the K-1 halo rows
+// between its strips (D words each) | the per-warp rings.
+constexpr unsigned kStageBars = 8u * kMaxWarps;
+__host__ __device__ __forceinline__ unsigned halo_offset(int K) { return 32u * K + kStageBars; }
+__host__ __device__ __forceinline__ unsigned ring_offset(int K, int D) {
     const size_t nh = (size_t)(K > 1 ? K - 1 : 0) * D;
-    return (unsigned)(((32 * (size_t)K + nh * 8 + 127) / 128) * 128);
+    return (unsigned)(((halo_offset(K) + nh * 8 + 127) / 128) * 128);
 }
 
-// Per-warp ring state; the mbarriers are initialised once per launch.
+// Per-warp ring and staging state; the mbarriers are initialised once per launch.
 template <typename F>
 __device__ void ring_init(Ring<F> &R, int K, int stages) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -610,10 +619,66 @@ __device__ void ring_init(Ring<F> &R, int K, int stages) {
     R.stages = stages;
     R.ii = R.ci = 0;
     R.dead = false;
-    if (warp < K && lane == 0) {
-        for (int k = 0; k < stages; k++) mbar_init(R.bar(k), 1);
+    R.sbar = 32u * K + 8u * warp;
+    R.sphase = 0;
+    R.sdead = false;
+    if (lane == 0) {
+        if (warp < K)
+            for (int k = 0; k < stages; k++) mbar_init(R.bar(k), 1);
+        mbar_init(R.stage_bar(), 1);
         fence_mbar_init();
     }
+}
+
+// ------------------------------------------------ staged elementwise passes
+// The elementwise passes stream their operands through shared memory: for each
+// unit of U consecutive diagonals (U a power of two dividing the 16-diagonal
+// reduction chunk) lane 0 issues one bulk copy per array (completion on the
+// warp's staging mbarrier), so that the warp has its whole unit (6-12 KB) in
+// flight at once, not the few loads its registers hold; the lanes then compute
+// from shared memory.  Per-cell arithmetic and each lane's accumulation order
+// are those of a direct pass over the same cells.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Largest unit (rows of 32 slots) whose staged bytes fit the warp's area.
+__device__ __forceinline__ int unit_rows(unsigned area, unsigned bytes_per_row) {
+    int U = kChunk;
+    while (U > 1 && (unsigned)U * bytes_per_row > area) U >>= 1;
+    return U;
+}
+// Wait for the unit in flight.  Like the ring, a timeout elsewhere does not
+// shorten it (the copies complete); a copy that never completes marks the
+// staging area dead, after which the warp issues and waits for nothing more.
+template <typename F>
+__device__ __forceinline__ void stage_wait(Ring<F> &R, const Flags &flags) {
+    long long n = 0;
+    while (!R.sdead && !mbar_try_wait(R.stage_bar(), R.sphase & 1u)) {
+        if (++n > kMbarWaitLimit) {
+            set_timeout(flags);
+            R.sdead = true;
+        }
+    }
+    R.sdead = __any_sync(FULL, R.sdead);
+    R.sphase++;
+}
+// Rows [lo, hi) of a strip-diagonal array (clipped to [0, rows)) into shared
+// memory at dst, where row `base` lands at slot 0; returns the bytes copied.
+template <typename T>
+__device__ __forceinline__ unsigned stage_rows(unsigned dst, const T *src, int base, int lo, int hi, int rows,
+                                               uint64_t *bar) {
+    lo = lo < 0 ? 0 : lo;
+    hi = hi > rows ? rows : hi;
+    if (hi <= lo) return 0u;
+    const unsigned bytes = (unsigned)(hi - lo) * 32u * sizeof(T);
+    bulk_g2s(g_smem + dst + (unsigned)(lo - base) * 32u * sizeof(T), src + (size_t)lo * 32, bytes, bar);
+    return bytes;
+}
+template <typename T>
+__device__ __forceinline__ unsigned clipped_bytes(int lo, int hi, int rows) {
+    lo = lo < 0 ? 0 : lo;
+    hi = hi > rows ? rows : hi;
+    return hi > lo ? (unsigned)(hi - lo) * 32u * sizeof(T) : 0u;
 }
 
 // One complete solve (factor and/or PCG, by A.mode) of one scene by team T.
@@ -641,11 +706,22 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
         v = is_max ? warp_max(v) : warp_sum(v);
         if (lane == 0) A.partials[(size_t)slot * nchunk + c] = v;
     };
+    // Lane l adds the partials of chunks l, l+32, l+64, ... in that order; the
+    // loads (from L2: other blocks wrote them before the team barrier) are
+    // issued eight at a time, so a scene of thousands of chunks costs a few
+    // memory latencies, not one per 32 chunks.
     auto chunk_total = [&](int slot, bool is_max) -> double {
         if (threadIdx.x < 32) {
             double acc = 0.0;
-            const volatile double *pt = A.partials + (size_t)slot * nchunk;
-            for (int c = lane; c < nchunk; c += 32) acc = is_max ? smax(acc, (double)pt[c]) : acc + pt[c];
+            const double *pt = A.partials + (size_t)slot * nchunk;
+            for (int c0 = lane; c0 < nchunk; c0 += 32 * 8) {
+                double v[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) v[j] = c0 + 32 * j < nchunk ? __ldcg(pt + c0 + 32 * j) : 0.0;
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (c0 + 32 * j < nchunk) acc = is_max ? smax(acc, v[j]) : acc + v[j];
+            }
             acc = is_max ? warp_max(acc) : warp_sum(acc);
             if (lane == 0) sm[kMaxWarps] = acc;
         }
@@ -661,33 +737,246 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     const unsigned hsm_off = halo_offset(A.K);
     R.buf = ring_offset(A.K, D) + (unsigned)warp * A.stages * Ring<F>::kStageBytes;
 
+    // Staging area of this warp: its share of the block's ring memory.
+    R.sbytes = (A.K * A.stages * Ring<F>::kStageBytes / kWarps) & ~127u;
+    R.sbuf = ring_offset(A.K, D) + (unsigned)warp * R.sbytes;
+    // Lane 0 of a warp starts a unit's copies: the warp's reads of the previous
+    // unit are done (syncwarp), then a proxy fence orders them before the
+    // asynchronous writes into the same shared memory.
+    auto unit_begin = [&]() -> bool {
+        __syncwarp();
+        if (lane != 0 || R.sdead) return false;
+        fence_proxy_async_shared();
+        return true;
+    };
+
     // sigma = z . r over the red cells (3-conjugate-gradients/Fluid.cpp:356, 376):
     // a separate pass keeps the FP64 products off the backward sweep's chain.
+    // Staged: z, r and the neighbour bits of a unit.
     auto dot_zr = [&]() {
-        const F *__restrict__ zp = A.z;
-        const double *__restrict__ rp = A.r;
-        const uint8_t *__restrict__ nbp = A.nb;
-        constexpr int kUD = kF32 ? 16 : 8;
+        constexpr unsigned kRow = 32u * (sizeof(F) + 8 + 1);
+        const int U = unit_rows(R.sbytes, kRow);
+        const unsigned oz = R.sbuf, orr = oz + U * 32u * sizeof(F), onb = orr + U * 32u * 8u;
+        if (lane == 0) fence_proxy_async_global();  // generic-proxy writes of the sweeps -> bulk copies
         for (int c = c_begin; c < c_end; c++) {
-            const int cb = c * kChunk, ce = min(rows, cb + kChunk);
             double acc = 0.0;
-            for (int row0 = cb; row0 < ce; row0 += kUD) {
-                F vz[kUD];
-                double vr[kUD];
-                unsigned vn[kUD];
-#pragma unroll
-                for (int u = 0; u < kUD; u++) {
-                    const int row = row0 + u < ce ? row0 + u : row0;
-                    const size_t i = (size_t)row * 32 + lane;
-                    vn[u] = row0 + u < ce ? nbp[i] : 0u;
-                    vz[u] = zp[i];
-                    vr[u] = rp[i];
+            for (int r0 = c * kChunk; r0 < (c + 1) * kChunk; r0 += U) {
+                if (unit_begin()) {
+                    mbar_expect_tx(R.stage_bar(), U * kRow);
+                    stage_rows(oz, A.z, r0, r0, r0 + U, rows, R.stage_bar());
+                    stage_rows(orr, A.r, r0, r0, r0 + U, rows, R.stage_bar());
+                    stage_rows(onb, A.nb, r0, r0, r0 + U, rows, R.stage_bar());
                 }
-#pragma unroll
-                for (int u = 0; u < kUD; u++)
-                    if (vn[u] & NB_RED) acc += (double)vz[u] * vr[u];
+                stage_wait(R, A.fl);
+                const F *sz = (const F *)(g_smem + oz);
+                const double *sr = (const double *)(g_smem + orr);
+                const uint8_t *snb = (const uint8_t *)(g_smem + onb);
+                for (int u = 0; u < U; u++) {
+                    const int k = u * 32 + lane;
+                    // FP32 form: one rounding per product-add (fused)
+                    if (snb[k] & NB_RED) acc = kF32 ? fma((double)sz[k], sr[k], acc) : acc + (double)sz[k] * sr[k];
+                }
             }
             chunk_put(2, c, acc, false);
+        }
+    };
+
+    // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s over a
+    // unit of U diagonals of one strip (3-conjugate-gradients/Fluid.cpp:361-362,
+    // 375, 315-332).  Staged: z, s, neighbour bits of the diagonals r0-1 ..
+    // r0+U (left/down and right/up neighbours inside the strip), aPlusX and
+    // aPlusY of r0-1 .. r0+U-1, aDiag of the unit.  The lower neighbour of lane
+    // 0 and the upper neighbour of lane 31 live in the adjacent strips; lanes
+    // 0..U-1 and 16..16+U-1 load them and hand them over by shuffle.
+    auto matvec = [&](int iter, double beta) -> void {
+        const F fbeta = (F)beta;
+        auto need = [](int v) {
+            return (unsigned)(v + 2) * 32u * (2u * sizeof(F) + 1u) + (unsigned)v * 32u * sizeof(F) +
+                   2u * (unsigned)(v + 1) * 32u * sizeof(F);
+        };
+        int U = kChunk;
+        while (U > 1 && need(U) > R.sbytes) U >>= 1;
+        const unsigned rz = (unsigned)(U + 2) * 32u * sizeof(F), rn = (unsigned)(U + 2) * 32u,
+                       ra = (unsigned)U * 32u * sizeof(F), rxy = (unsigned)(U + 1) * 32u * sizeof(F);
+        const unsigned oz = R.sbuf, os = oz + rz, onb = os + rz, oad = onb + rn, oax = oad + ra, oay = oax + rxy;
+        const F *__restrict__ zp = A.z;
+        const F *__restrict__ so = (iter & 1) ? A.sb : A.sa;
+        F *__restrict__ sn = (iter & 1) ? A.sa : A.sb;
+        double *__restrict__ asp = A.as;
+        if (lane == 0) fence_proxy_async_global();
+        for (int c = c_begin; c < c_end; c++) {
+            double dacc = 0.0;
+            const int s = (c * kChunk) / D;  // a chunk lies inside one strip (D is a multiple of it)
+            for (int r0 = c * kChunk; r0 < (c + 1) * kChunk; r0 += U) {
+                const int d0 = r0 - s * D;
+                if (unit_begin()) {
+                    uint64_t *bar = R.stage_bar();
+                    const unsigned tx = 2u * clipped_bytes<F>(r0 - 1, r0 + U + 1, rows) +
+                                        clipped_bytes<uint8_t>(r0 - 1, r0 + U + 1, rows) +
+                                        clipped_bytes<F>(r0, r0 + U, rows) + 2u * clipped_bytes<F>(r0 - 1, r0 + U, rows);
+                    mbar_expect_tx(bar, tx);
+                    stage_rows(oz, zp, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
+                    stage_rows(os, so, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
+                    stage_rows(onb, A.nb, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
+                    stage_rows(oad, A.adiag, r0, r0, r0 + U, rows, bar);
+                    stage_rows(oax, A.ax, r0 - 1, r0 - 1, r0 + U, rows, bar);
+                    stage_rows(oay, A.ay, r0 - 1, r0 - 1, r0 + U, rows, bar);
+                }
+                // neighbours in the adjacent strips (loaded while the copies fly)
+                F xz = F(0), xs = F(0), xa = F(0);
+                unsigned xn = 0u;
+                {
+                    const int j = lane & 15, d = d0 + j;
+                    if (j < U && lane < 16 && s > 0 && d < W && 32 * s < H) {  // below lane 0 of diagonal d
+                        const size_t k = sd.slot(d, 32 * s - 1);
+                        xz = zp[k];
+                        xs = so[k];
+                        xn = A.nb[k];
+                        xa = A.ay[k];
+                    } else if (j < U && lane >= 16 && d - 31 >= 0 && d - 31 < W && 32 * s + 32 < H) {  // above lane 31
+                        const size_t k = sd.slot(d - 31, 32 * s + 32);
+                        xz = zp[k];
+                        xs = so[k];
+                        xn = A.nb[k];
+                    }
+                }
+                stage_wait(R, A.fl);
+                const F *szv = (const F *)(g_smem + oz);
+                const F *ssv = (const F *)(g_smem + os);
+                const uint8_t *snb = (const uint8_t *)(g_smem + onb);
+                const F *sad = (const F *)(g_smem + oad);
+                const F *sax = (const F *)(g_smem + oax);
+                const F *say = (const F *)(g_smem + oay);
+                for (int u = 0; u < U; u++) {
+                    const F dz = __shfl_sync(FULL, xz, u), ds = __shfl_sync(FULL, xs, u), da = __shfl_sync(FULL, xa, u);
+                    const unsigned dn = __shfl_sync(FULL, xn, u);
+                    const F uz = __shfl_sync(FULL, xz, 16 + u), us = __shfl_sync(FULL, xs, 16 + u);
+                    const unsigned un = __shfl_sync(FULL, xn, 16 + u);
+                    const int x = d0 + u - lane, y = s * 32 + lane;
+                    const bool in = x >= 0 && x < W && y < H;
+                    const bool hl = in && x > 0, hd = in && y > 0, hr = in && x < W - 1, hu = in && y < H - 1;
+                    const int k0 = (u + 1) * 32 + lane;  // the cell (z, s, bits)
+                    const int kl = u * 32 + lane, kr = (u + 2) * 32 + lane;
+                    const int kd = u * 32 + lane - 1, ku = (u + 2) * 32 + lane + 1;
+                    // a missing neighbour takes the cell's own values and is not used
+                    F vz[5], vs[5], va[5];
+                    unsigned vn[5];
+                    vz[0] = szv[k0]; vs[0] = ssv[k0]; vn[0] = snb[k0];
+                    vz[1] = hl ? szv[kl] : vz[0]; vs[1] = hl ? ssv[kl] : vs[0]; vn[1] = hl ? snb[kl] : vn[0];
+                    if (lane > 0) {
+                        vz[2] = hd ? szv[kd] : vz[0]; vs[2] = hd ? ssv[kd] : vs[0]; vn[2] = hd ? snb[kd] : vn[0];
+                        va[2] = hd ? say[u * 32 + lane - 1] : F(0);
+                    } else {
+                        vz[2] = hd ? dz : vz[0]; vs[2] = hd ? ds : vs[0]; vn[2] = hd ? dn : vn[0];
+                        va[2] = hd ? da : F(0);
+                    }
+                    vz[3] = hr ? szv[kr] : vz[0]; vs[3] = hr ? ssv[kr] : vs[0]; vn[3] = hr ? snb[kr] : vn[0];
+                    if (lane < 31) {
+                        vz[4] = hu ? szv[ku] : vz[0]; vs[4] = hu ? ssv[ku] : vs[0]; vn[4] = hu ? snb[ku] : vn[0];
+                    } else {
+                        vz[4] = hu ? uz : vz[0]; vs[4] = hu ? us : vs[0]; vn[4] = hu ? un : vn[0];
+                    }
+                    va[0] = sad[u * 32 + lane];
+                    va[1] = sax[u * 32 + lane];        // aPlusX of the left neighbour (row r0+u-1)
+                    va[3] = sax[(u + 1) * 32 + lane];  // aPlusX of the cell
+                    va[4] = say[(u + 1) * 32 + lane];  // aPlusY of the cell
+                    const unsigned fl = (in ? 2u : 0u) | (hl ? 4u : 0u) | (hd ? 8u : 0u) | (hr ? 16u : 0u) |
+                                        (hu ? 32u : 0u);
+                    F sv[5];
+#pragma unroll
+                    for (int q = 0; q < 5; q++)
+                        sv[q] = iter == 0 ? vz[q] : ((vn[q] & NB_RED) ? F(vz[q] + vs[q] * fbeta) : vs[q]);
+                    // FP64 form: FP64 accumulation in the reference's order.  FP32
+                    // form: an error-free float-float sum on the FP32 pipes (GB300
+                    // runs FP64 at 1/64 of the FP32 rate), and for the pressure
+                    // matrices, whose rows sum to zero in the reference
+                    // (aDiag = sum of the face factors, each off-diagonal = -factor),
+                    // the form sum_j a_ij (s_j - s_i), which keeps that property
+                    // exactly: the FP32-rounded aDiag no longer matches its
+                    // off-diagonals, and the resulting tiny, non-zero eigenvalue made
+                    // CG stagnate on some scenes (up to the 2000-iteration cap).
+                    double t;
+                    if constexpr (kF32) {
+                        FF acc;
+                        if (A.rowsum_zero) {
+                            acc = FF{0.f, 0.f};
+#pragma unroll
+                            for (int q = 1; q < 5; q++)
+                                if (fl & (2u << q)) acc = ff_add(acc, ff_prod(va[q], sv[q] - sv[0]));
+                        } else {
+                            acc = ff_prod(va[0], sv[0]);
+#pragma unroll
+                            for (int q = 1; q < 5; q++)
+                                if (fl & (2u << q)) acc = ff_add(acc, ff_prod(va[q], sv[q]));
+                        }
+                        t = (double)acc.hi + (double)acc.lo;
+                    } else {
+                        t = (double)va[0] * (double)sv[0];
+#pragma unroll
+                        for (int q = 1; q < 5; q++)
+                            t = (fl & (2u << q)) ? t + (double)va[q] * (double)sv[q] : t;
+                    }
+                    const size_t i = (size_t)(r0 + u) * 32 + lane;
+                    sn[i] = in ? sv[0] : F(0);
+                    asp[i] = in ? t : 0.0;
+                    if (in && (vn[0] & NB_RED))
+                        dacc = kF32 ? fma(t, (double)sv[0], dacc) : dacc + t * (double)sv[0];
+                }
+            }
+            chunk_put(1, c, dacc, false);
+        }
+    };
+
+    // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366), staged
+    // p, r, A*s, s and the neighbour bits of a unit.
+    auto axpy = [&](int iter, double alpha) -> void {
+        constexpr unsigned kRow = 32u * (8u + 8u + 8u + sizeof(F) + 1u);
+        const int U = unit_rows(R.sbytes, kRow);
+        const unsigned op = R.sbuf, orr = op + U * 256u, oas = orr + U * 256u, osn = oas + U * 256u,
+                       onb = osn + U * 32u * sizeof(F);
+        const F *__restrict__ snp = (iter & 1) ? A.sa : A.sb;  // the s this iteration's matvec wrote
+        double *__restrict__ pp = A.p;
+        double *__restrict__ rp = A.r;
+        F *rfp = A.rf;  // aliases r in the FP64 form (not written there)
+        if (lane == 0) fence_proxy_async_global();
+        for (int c = c_begin; c < c_end; c++) {
+            unsigned long long mx = 0ull;  // bits of the largest |r| so far
+            for (int r0 = c * kChunk; r0 < (c + 1) * kChunk; r0 += U) {
+                if (unit_begin()) {
+                    uint64_t *bar = R.stage_bar();
+                    mbar_expect_tx(bar, U * kRow);
+                    stage_rows(op, A.p, r0, r0, r0 + U, rows, bar);
+                    stage_rows(orr, A.r, r0, r0, r0 + U, rows, bar);
+                    stage_rows(oas, A.as, r0, r0, r0 + U, rows, bar);
+                    stage_rows(osn, snp, r0, r0, r0 + U, rows, bar);
+                    stage_rows(onb, A.nb, r0, r0, r0 + U, rows, bar);
+                }
+                stage_wait(R, A.fl);
+                const double *sp = (const double *)(g_smem + op);
+                const double *sr = (const double *)(g_smem + orr);
+                const double *sas = (const double *)(g_smem + oas);
+                const F *ssn = (const F *)(g_smem + osn);
+                const uint8_t *snb = (const uint8_t *)(g_smem + onb);
+                for (int u = 0; u < U; u++) {
+                    const int k = u * 32 + lane;
+                    if (snb[k] & NB_RED) {
+                        const size_t i = (size_t)(r0 + u) * 32 + lane;
+                        // FP32 form: one rounding per update (fused); FP64 form: the
+                        // reference's two
+                        pp[i] = kF32 ? fma((double)ssn[k], alpha, sp[k]) : sp[k] + (double)ssn[k] * alpha;
+                        const double rn = kF32 ? fma(sas[k], -alpha, sr[k]) : sr[k] + sas[k] * -alpha;
+                        rp[i] = rn;
+                        if (kF32) rfp[i] = (F)rn;
+                        // std::max(maxError, |r|) on the bit patterns: non-negative
+                        // doubles order as unsigned integers; a NaN (above +inf) is
+                        // skipped, as (maxError < NaN) is false
+                        const unsigned long long b =
+                            (unsigned long long)__double_as_longlong(rn) & 0x7fffffffffffffffull;
+                        if (b <= 0x7ff0000000000000ull && b > mx) mx = b;
+                    }
+                }
+            }
+            chunk_put(0, c, __longlong_as_double((long long)mx), true);
         }
     };
 
@@ -725,150 +1014,17 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     } else {
         status = 2;
         double beta = 0.0;
-        F *s_old = A.sa, *s_new = A.sb;
+        // the search direction alternates between sa and sb (the matvec reads one
+        // and writes the other): iteration k writes sb when k is even
         for (int iter = 0; iter < A.limit; iter++) {
             // block-uniform: every thread of the block leaves together
             if (__syncthreads_or(threadIdx.x == 0 && timed_out(A.fl))) break;
             // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
-            const F fbeta = (F)beta;
-            // Four diagonals per warp and pass, their loads issued together
-            // (the pointers do not alias), in the same per-lane order as a
-            // plain strided loop.
-            const F *__restrict__ zp = A.z;
-            const F *__restrict__ so = s_old;
-            const uint8_t *__restrict__ nbp = A.nb;
-            const F *__restrict__ adp = A.adiag;
-            const F *__restrict__ axp = A.ax;
-            const F *__restrict__ ayp = A.ay;
-            F *__restrict__ sn = s_new;
-            double *__restrict__ asp = A.as;
-            // Groups of kUA diagonals: all loads of a group first, then the
-            // arithmetic and the stores, so one memory latency covers the group.
-            constexpr int kUA = 2;
-            for (int c = c_begin; c < c_end; c++) {
-            const int cb = c * kChunk, ce = min(rows, cb + kChunk);
-            double dacc = 0.0;
-            for (int row0 = cb; row0 < ce; row0 += kUA) {
-                F vz[kUA][5], vs[kUA][5], va[kUA][5];
-                unsigned vn[kUA][5];
-                unsigned fl[kUA];
-                size_t vi[kUA];
-#pragma unroll
-                for (int u = 0; u < kUA; u++) {
-                    const bool valid = row0 + u < ce;
-                    const int row = valid ? row0 + u : row0;
-                    const int s = row / D, dd = row - s * D;
-                    const int x = dd - lane, y = s * 32 + lane;
-                    const size_t i = (size_t)row * 32 + lane;
-                    const bool in = valid && x >= 0 && x < W && y < H;
-                    const bool hl = in && x > 0, hd = in && y > 0, hr = in && x < W - 1, hu = in && y < H - 1;
-                    // a missing neighbour reads the cell itself and is not used
-                    const size_t idx[5] = {i, hl ? i - 32 : i, hd ? (lane > 0 ? i - 33 : sd.slot(x, y - 1)) : i,
-                                           hr ? i + 32 : i, hu ? (lane < 31 ? i + 33 : sd.slot(x, y + 1)) : i};
-#pragma unroll
-                    for (int c = 0; c < 5; c++) {
-                        vz[u][c] = zp[idx[c]];
-                        vs[u][c] = so[idx[c]];
-                        vn[u][c] = nbp[idx[c]];
-                    }
-                    va[u][0] = adp[i];
-                    va[u][1] = axp[idx[1]];
-                    va[u][2] = ayp[idx[2]];
-                    va[u][3] = axp[i];
-                    va[u][4] = ayp[i];
-                    vi[u] = i;
-                    fl[u] = (valid ? 1u : 0u) | (in ? 2u : 0u) | (hl ? 4u : 0u) | (hd ? 8u : 0u) | (hr ? 16u : 0u) |
-                            (hu ? 32u : 0u);
-                }
-#pragma unroll
-                for (int u = 0; u < kUA; u++) {
-                    if (!(fl[u] & 1u)) continue;
-                    const size_t i = vi[u];
-                    const bool in = fl[u] & 2u;
-                    F sv[5];
-#pragma unroll
-                    for (int c = 0; c < 5; c++)
-                        sv[c] = iter == 0 ? vz[u][c] : ((vn[u][c] & NB_RED) ? F(vz[u][c] + vs[u][c] * fbeta) : vs[u][c]);
-                    // FP64 form: FP64 accumulation in the reference's order.  FP32
-                    // form: an error-free float-float sum on the FP32 pipes (GB300
-                    // runs FP64 at 1/64 of the FP32 rate), and for the pressure
-                    // matrices, whose rows sum to zero in the reference
-                    // (aDiag = sum of the face factors, each off-diagonal = -factor),
-                    // the form sum_j a_ij (s_j - s_i), which keeps that property
-                    // exactly: the FP32-rounded aDiag no longer matches its
-                    // off-diagonals, and the resulting tiny, non-zero eigenvalue made
-                    // CG stagnate on some scenes (up to the 2000-iteration cap).
-                    double t;
-                    if constexpr (kF32) {
-                        FF acc;
-                        if (A.rowsum_zero) {
-                            acc = FF{0.f, 0.f};
-#pragma unroll
-                            for (int c = 1; c < 5; c++)
-                                if (fl[u] & (2u << c)) acc = ff_add(acc, ff_prod(va[u][c], sv[c] - sv[0]));
-                        } else {
-                            acc = ff_prod(va[u][0], sv[0]);
-#pragma unroll
-                            for (int c = 1; c < 5; c++)
-                                if (fl[u] & (2u << c)) acc = ff_add(acc, ff_prod(va[u][c], sv[c]));
-                        }
-                        t = (double)acc.hi + (double)acc.lo;
-                    } else {
-                        t = (double)va[u][0] * (double)sv[0];
-#pragma unroll
-                        for (int c = 1; c < 5; c++)
-                            t = (fl[u] & (2u << c)) ? t + (double)va[u][c] * (double)sv[c] : t;
-                    }
-                    sn[i] = in ? sv[0] : F(0);
-                    asp[i] = in ? t : 0.0;
-                    if (in && (vn[u][0] & NB_RED)) dacc += t * (double)sv[0];
-                }
-            }
-            chunk_put(1, c, dacc, false);
-            }
+            matvec(iter, beta);
             team_barrier(T, A.fl);
             const double alpha = sigma / chunk_total(1, false);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
-            {
-                double *__restrict__ pp = A.p;
-                double *__restrict__ rp = A.r;
-                const double *__restrict__ asp2 = A.as;
-                const F *__restrict__ sn2 = s_new;
-                const uint8_t *__restrict__ nbp2 = A.nb;
-                F *rfp = A.rf;  // aliases r in the FP64 form (not written there)
-                constexpr int kUB = kF32 ? 8 : 4;
-                for (int c = c_begin; c < c_end; c++) {
-                const int cb = c * kChunk, ce = min(rows, cb + kChunk);
-                double mx = 0.0;
-                for (int row0 = cb; row0 < ce; row0 += kUB) {
-                    double vp[kUB], vr[kUB], vas[kUB];
-                    F vsn[kUB];
-                    unsigned vnb[kUB];
-#pragma unroll
-                    for (int u = 0; u < kUB; u++) {
-                        const int row = row0 + u < ce ? row0 + u : row0;
-                        const size_t i = (size_t)row * 32 + lane;
-                        vnb[u] = row0 + u < ce ? nbp2[i] : 0u;
-                        vp[u] = pp[i];
-                        vr[u] = rp[i];
-                        vas[u] = asp2[i];
-                        vsn[u] = sn2[i];
-                    }
-#pragma unroll
-                    for (int u = 0; u < kUB; u++) {
-                        const size_t i = (size_t)(row0 + u) * 32 + lane;
-                        if (vnb[u] & NB_RED) {
-                            pp[i] = vp[u] + (double)vsn[u] * alpha;
-                            const double rn = vr[u] + vas[u] * -alpha;
-                            rp[i] = rn;
-                            if (kF32) rfp[i] = (F)rn;
-                            mx = smax(mx, fabs(rn));
-                        }
-                    }
-                }
-                chunk_put(0, c, mx, true);
-                }
-            }
+            axpy(iter, alpha);
             team_barrier(T, A.fl);
             maxError = chunk_total(0, true);
             iterations = iter + 1;
@@ -886,9 +1042,6 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             const double sigmaNew = chunk_total(2, false);
             beta = sigmaNew / sigma;
             sigma = sigmaNew;
-            F *tmp = s_old;
-            s_old = s_new;
-            s_new = tmp;
         }
         if (status == 2) iterations = A.limit;
     }
@@ -1019,8 +1172,7 @@ int strips_per_block() {
 constexpr int kStages = 3;
 template <typename F>
 size_t smem_bytes(int K, int D, int stages = kStages) {
-    const size_t nh = (size_t)(K > 1 ? K - 1 : 0) * D;
-    return ((32 * (size_t)K + nh * 8 + 127) / 128) * 128 + (size_t)K * stages * Ring<F>::kStageBytes;
+    return ring_offset(K, D) + (size_t)K * stages * Ring<F>::kStageBytes;
 }
 
 template <typename F, int kThreads>
