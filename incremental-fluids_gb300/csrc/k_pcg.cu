@@ -191,49 +191,61 @@ template <> __device__ __forceinline__ double hdec<double>(unsigned long long w)
 }
 template <> __device__ __forceinline__ float hdec<float>(unsigned long long w) { return __uint_as_float((unsigned)w); }
 
-// Halo rows: shared memory (relaxed, CTA scope) inside a block, global memory
-// (relaxed, GPU scope) between blocks.  One 8-byte access is single-copy
-// atomic, so a reader sees either the sentinel or the whole value.  A halo
-// word carries its value itself, so no other memory access has to be ordered
-// around it: the asm statements are volatile (kept, in program order) but do
-// not clobber memory, which would stop the compiler from keeping loaded
-// operands and pointers in registers across them.
+// Halo rows: shared memory between warps of one block, global memory between
+// blocks.  A channel holds the row's generic address, so one instruction
+// serves both spaces (relaxed, GPU scope; stronger than a shared row needs).
+// One 8-byte access is single-copy atomic, so a reader sees either the
+// sentinel or the whole word.  A halo word carries its value itself, so no
+// other memory access has to be ordered around it: the asm statements are
+// volatile (kept, in program order) but do not clobber memory.  Loads and
+// stores are predicated inside the asm: a sweep step never branches around a
+// halo access.
 struct Chan {
-    unsigned soff;             // byte offset in g_smem when shared
-    unsigned long long *g;     // global row when not shared
-    bool shared, valid;
+    unsigned long long *row;  // generic address of the row (word x at row + x)
+    bool valid;
 };
 __device__ __forceinline__ unsigned long long hload(const Chan &c, int x) {
     unsigned long long v;
-    if (c.shared)
-        asm volatile("ld.relaxed.cta.shared.u64 %0, [%1];" : "=l"(v) : "r"(smem_u32(g_smem) + c.soff + 8u * x));
-    else
-        asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(c.g + x));
+    asm volatile("ld.relaxed.gpu.u64 %0, [%1];" : "=l"(v) : "l"(c.row + x));
     return v;
 }
-__device__ __forceinline__ void hstore(const Chan &c, int x, unsigned long long v) {
-    if (c.shared)
-        asm volatile("st.relaxed.cta.shared.u64 [%0], %1;" ::"r"(smem_u32(g_smem) + c.soff + 8u * x), "l"(v));
-    else
-        asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(c.g + x), "l"(v));
+// The word at x where p holds, else `other`.
+__device__ __forceinline__ unsigned long long hload_if(const Chan &c, int x, bool p, unsigned long long other) {
+    unsigned long long v = other;
+    asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n @q ld.relaxed.gpu.u64 %0, [%1];\n}\n"
+                 : "+l"(v)
+                 : "l"(c.row + x), "r"((unsigned)p));
+    return v;
+}
+__device__ __forceinline__ void hstore_if(const Chan &c, int x, unsigned long long v, bool p) {
+    asm volatile("{\n .reg .pred q;\n setp.ne.u32 q, %2, 0;\n @q st.relaxed.gpu.u64 [%0], %1;\n}\n" ::"l"(c.row + x),
+                 "l"(v), "r"((unsigned)p));
 }
 
-// Take a halo word (bounded poll), then put the sentinel back for the next sweep.
-__device__ __forceinline__ unsigned long long halo_take(const Chan &c, int x, unsigned long long pre,
-                                                        const Flags &flags) {
-    unsigned long long v = pre;
-    long long n = 0;
-    while (v == kSentinel) {
-        v = hload(c, x);
-        if (v != kSentinel) break;
-        if (++n > flags.limit || timed_out(flags)) {
-            set_timeout(flags);
-            v = 0;
-            break;
+// Halo words of one sub-block: lane l < n needs the word at column xs[l]
+// (need), prefetched in w.  Lanes whose word is still the sentinel poll it
+// (bounded; the whole warp loops together, only in this slow path); then the
+// sentinel goes back for the next sweep.  A timed-out wait yields 0.
+__device__ __forceinline__ unsigned long long halo_take_warp(const Chan &c, int x, bool need, unsigned long long w,
+                                                             const Flags &flags) {
+    if (__any_sync(FULL, need && w == kSentinel)) {
+        long long n = 0;
+        bool given_up = false;
+        for (;;) {
+            const bool wait = need && w == kSentinel && !given_up;
+            if (!__any_sync(FULL, wait)) break;
+            if (wait) {
+                w = hload(c, x);
+                if (w == kSentinel && (++n > flags.limit || timed_out(flags))) {
+                    set_timeout(flags);
+                    given_up = true;
+                }
+            }
         }
+        if (given_up) w = 0ull;
     }
-    hstore(c, x, kSentinel);
-    return v;
+    hstore_if(c, x, kSentinel, need);
+    return w;
 }
 
 // --------------------------------------------------------------- sweeps
@@ -361,15 +373,26 @@ __device__ __forceinline__ float nb_word(unsigned b, float) { return __uint_as_f
 __device__ __forceinline__ double nb_word(unsigned b, double) { return __longlong_as_double((long long)b); }
 
 // One strip of a wavefront sweep.  `in` is the halo row written by the
-// neighbouring strip this one depends on (nullptr: none), `out` the row this
-// strip hands on (nullptr: none).  Each sub-block of kHB steps first stages
-// its operands from the ring into registers, then runs the dependency chain
-// (registers and shuffles only), then issues its stores.
-template <int KIND, typename F>
+// neighbouring strip this one depends on (IN says at compile time whether it
+// exists: a strip without one carries no halo code), `out` the row this strip
+// hands on (valid or not).  Each sub-block of kHB steps stages its operands
+// from the ring into registers, takes the sub-block's halo words (lanes
+// 0..kHB-1 one column each, prefetched one sub-block ahead), runs the
+// dependency chain (registers and shuffles only; the handing-on lane stores
+// each boundary value as soon as the chain computes it) and issues its
+// stores.
+//
+// Halo words: the FP32 forward sweep hands over the pair (q, aPlusY*precon)
+// of the strip's top cell packed in one 8-byte word, so the strip above needs
+// no load of its lower neighbour's MIC(0) record; the other sweeps hand over
+// the value alone (the factor and the FP64 forward sweep load the lower
+// neighbour's coefficients with the prefetch).
+template <int KIND, typename F, bool IN>
 __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan in, const Chan out) {
     using V = typename std::conditional<KIND == 0, double, F>::type;
     constexpr int kHB = sizeof(F) == 8 ? 4 : 8;
     constexpr bool bwd = KIND == 2;
+    constexpr bool kPair = KIND == 1 && sizeof(F) == 4;  // packed (q, ly) words
     constexpr unsigned S1 = Ring<F>::kSlot;
     const int lane = threadIdx.x & 31;
     const SDIdx sd = A.sd;
@@ -377,7 +400,6 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
     const int y = s * 32 + lane;
     const bool rowok = y < H;
     const int nblk = D / kB;
-    const bool has_in = in.valid;
     const bool producer = out.valid && lane == (bwd ? 0 : 31);
     // pointers in registers for the whole sweep
     F *const zout = A.z;
@@ -390,21 +412,24 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
     F prev_a = F(0), prev_b = F(0);  // forward: lx, ly of that cell; factor: ax, ay
 
     // Halo prefetch: lane l < kHB holds the word of the column that the
-    // waiting lane (0 forward, 31 backward) reaches at step t0 + l.
+    // waiting lane reaches at step t0 + l, and where needed the lower
+    // neighbour's coefficients.
     unsigned long long hpre = kSentinel;
     F spre_a = F(0), spre_b = F(0);
     auto halo_col = [&](int t) { return bwd ? D - 32 - t : t; };
     auto prefetch = [&](int t0) {
-        hpre = kSentinel;
-        if (has_in && lane < kHB) {
+        if constexpr (IN) {
             const int xc = halo_col(t0 + lane);
-            if (xc >= 0 && xc < W) {
-                hpre = hload(in, xc);
-                if constexpr (KIND == 0) {
+            const bool need = lane < kHB && xc >= 0 && xc < W;
+            hpre = hload_if(in, xc, need, kSentinel);
+            if constexpr (KIND == 0) {
+                if (need) {
                     const size_t k = sd.slot(xc, s * 32 - 1);
                     spre_a = axp[k];
                     spre_b = ayp[k];
-                } else if constexpr (KIND == 1) {
+                }
+            } else if constexpr (KIND == 1 && !kPair) {
+                if (need) {
                     F a, b, c, d;
                     ld4(micp + 4 * sd.slot(xc, s * 32 - 1), a, b, c, d);
                     spre_b = b;  // ly of the cell below
@@ -434,23 +459,9 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
         const uint8_t *gnb = (const uint8_t *)(sbuf + 3 * S1);
         for (int sub = 0; sub < kB / kHB; sub++) {
             const int t0 = blk * kB + sub * kHB;
-            // halo words of this sub-block, then the next sub-block's prefetch
-            V hv = V(0);
-            F ha = F(0), hb = F(0);
-            if (has_in && lane < kHB) {
-                const int xc = halo_col(t0 + lane);
-                if (xc >= 0 && xc < W) {
-                    hv = hdec<V>(halo_take(in, xc, hpre, A.fl));
-                    ha = spre_a;
-                    hb = spre_b;
-                }
-            }
-            prefetch(t0 + kHB);
             // stage this sub-block's operands in registers
             F o0[kHB], o1[kHB], o2[kHB], o3[kHB];
             unsigned ob[kHB];
-            V hvv[kHB];
-            F hav[kHB], hbv[kHB];
 #pragma unroll
             for (int jj = 0; jj < kHB; jj++) {
                 const int j = sub * kHB + jj;
@@ -461,20 +472,24 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                     o2[jj] = g2[e];
                     ob[jj] = gnb[e];
                     o3[jj] = F(0);
-                } else if constexpr (KIND == 1) {
-                    F w3;
-                    o0[jj] = g0[e];
-                    ld4(g2 + 4 * e, o1[jj], o2[jj], o3[jj], w3);
-                    ob[jj] = nb_of(w3);
                 } else {
                     F w3;
                     o0[jj] = g0[e];
                     ld4(g2 + 4 * e, o1[jj], o2[jj], o3[jj], w3);
                     ob[jj] = nb_of(w3);
                 }
-                hvv[jj] = __shfl_sync(FULL, hv, jj);
-                hav[jj] = __shfl_sync(FULL, ha, jj);
-                hbv[jj] = __shfl_sync(FULL, hb, jj);
+            }
+            // this sub-block's halo words, then the next sub-block's prefetch
+            unsigned long long hw = 0ull;
+            F ha = F(0), hb = F(0);
+            if constexpr (IN) {
+                const int xc = halo_col(t0 + lane);
+                const bool need = lane < kHB && xc >= 0 && xc < W;
+                hw = halo_take_warp(in, xc, need, hpre, A.fl);
+                if (!need) hw = 0ull;
+                ha = spre_a;
+                hb = spre_b;
+                prefetch(t0 + kHB);
             }
             // dependency chain
             V res[kHB];
@@ -487,10 +502,14 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                     double pc_d = __shfl_up_sync(FULL, prev, 1);
                     F ax_d = __shfl_up_sync(FULL, prev_a, 1);
                     F ay_d = __shfl_up_sync(FULL, prev_b, 1);
-                    if (lane == 0) {
-                        pc_d = hvv[jj];
-                        ax_d = hav[jj];
-                        ay_d = hbv[jj];
+                    if constexpr (IN) {
+                        const double hpc = hdec<double>(__shfl_sync(FULL, hw, jj));
+                        const F hax = __shfl_sync(FULL, ha, jj), hay = __shfl_sync(FULL, hb, jj);
+                        if (lane == 0) {
+                            pc_d = hpc;
+                            ax_d = hax;
+                            ay_d = hay;
+                        }
                     }
                     const double diag = (double)o0[jj];
                     double ev = diag;
@@ -510,10 +529,23 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                     prev_b = o2[jj];
                 } else if constexpr (KIND == 1) {
                     // forward substitution (3-conjugate-gradients/Fluid.cpp:276-287)
-                    const F q_sh = __shfl_up_sync(FULL, prev, 1);
-                    const F ly_sh = __shfl_up_sync(FULL, prev_b, 1);
-                    const F q_d = lane == 0 ? hvv[jj] : q_sh;
-                    const F ly_d = lane == 0 ? hbv[jj] : ly_sh;
+                    F q_d = __shfl_up_sync(FULL, prev, 1);
+                    F ly_d = __shfl_up_sync(FULL, prev_b, 1);
+                    if constexpr (IN) {
+                        F hq, hly;
+                        if constexpr (kPair) {
+                            const unsigned long long wj = __shfl_sync(FULL, hw, jj);
+                            hq = __uint_as_float((unsigned)wj);
+                            hly = __uint_as_float((unsigned)(wj >> 32));
+                        } else {
+                            hq = hdec<F>(__shfl_sync(FULL, hw, jj));
+                            hly = __shfl_sync(FULL, hb, jj);
+                        }
+                        if (lane == 0) {
+                            q_d = hq;
+                            ly_d = hly;
+                        }
+                    }
                     F tt = o0[jj];
                     tt = (b & NB_LEFT) ? msub(tt, prev_a, prev) : tt;
                     tt = (b & NB_DOWN) ? msub(tt, ly_d, q_d) : tt;
@@ -522,8 +554,11 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                     prev_b = o2[jj];
                 } else {
                     // backward substitution (3-conjugate-gradients/Fluid.cpp:289-303)
-                    const F z_sh = __shfl_down_sync(FULL, prev, 1);
-                    const F z_u = lane == 31 ? hvv[jj] : z_sh;
+                    F z_u = __shfl_down_sync(FULL, prev, 1);
+                    if constexpr (IN) {
+                        const F hz = hdec<F>(__shfl_sync(FULL, hw, jj));
+                        if (lane == 31) z_u = hz;
+                    }
                     F tt = o0[jj];
                     tt = (b & NB_RIGHT) ? msub(tt, o1[jj], prev) : tt;
                     tt = (b & NB_UP) ? msub(tt, o2[jj], z_u) : tt;
@@ -531,6 +566,17 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                 }
                 res[jj] = val;
                 prev = val;
+                // hand the boundary value on at once (one predicated store)
+                {
+                    const int t = t0 + jj;
+                    const int x = (bwd ? D - 1 - t : t) - lane;
+                    unsigned long long wv;
+                    if constexpr (kPair)
+                        wv = (unsigned long long)__float_as_uint(val) | ((unsigned long long)__float_as_uint(o2[jj]) << 32);
+                    else
+                        wv = henc(val);
+                    hstore_if(out, x, wv, producer && rowok && x >= 0 && x < W);
+                }
             }
             // stores
 #pragma unroll
@@ -551,12 +597,18 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                     } else {
                         if (b & NB_SELF) zout[i] = res[jj];
                     }
-                    if (producer) hstore(out, x, henc(res[jj]));
                 }
             }
         }
     }
     __syncwarp();
+}
+
+template <int KIND, typename F>
+__device__ __forceinline__ void sweep_strip_any(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan in,
+                                                const Chan out) {
+    if (in.valid) sweep_strip<KIND, F, true>(A, s, R, in, out);
+    else sweep_strip<KIND, F, false>(A, s, R, in, out);
 }
 
 // Sweep of all strips of this block.  The team's T.size*K sweeping warps take
@@ -581,13 +633,15 @@ __device__ void sweep(const PcgArgs<F> &A, const Team &T, Ring<F> &R, unsigned h
     const int base = T.rank * A.K + w;
     const size_t D = sd.D;
     unsigned long long *up = A.halo, *down = A.halo + (size_t)sd.S * D;
-    auto smem_row = [&](int k) { return Chan{hsm_off + 8u * (unsigned)(k * D), nullptr, true, true}; };
-    auto glob_row = [&](unsigned long long *row) { return Chan{0u, row, false, true}; };
+    auto smem_row = [&](int k) {
+        return Chan{(unsigned long long *)(g_smem + hsm_off + 8u * (unsigned)(k * D)), true};
+    };
+    auto glob_row = [&](unsigned long long *row) { return Chan{row, true}; };
     const bool one_round = sd.S <= P;
     const int nmine = (sd.S - base + P - 1) / P;  // strips of this warp
     for (int j0 = 0; j0 < nmine; j0++) {
         const int s = base + (KIND == 2 ? nmine - 1 - j0 : j0) * P;
-        Chan in{0u, nullptr, false, false}, out{0u, nullptr, false, false};
+        Chan in{nullptr, false}, out{nullptr, false};
         if (KIND != 2) {  // rows travel upward: strip s takes from s-1, gives to s+1
             if (s > 0) in = (one_round && w > 0) ? smem_row(w - 1) : glob_row(up + (size_t)(s - 1) * D);
             if (s + 1 < sd.S)
@@ -597,7 +651,7 @@ __device__ void sweep(const PcgArgs<F> &A, const Team &T, Ring<F> &R, unsigned h
                 in = (one_round && w + 1 < nstrips_blk) ? smem_row(w) : glob_row(down + (size_t)(s + 1) * D);
             if (s > 0) out = (one_round && w > 0) ? smem_row(w - 1) : glob_row(down + (size_t)s * D);
         }
-        sweep_strip<KIND, F>(A, s, R, in, out);
+        sweep_strip_any<KIND, F>(A, s, R, in, out);
     }
 }
 
