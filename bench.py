@@ -963,13 +963,41 @@ def run_serve(args, local_rank):
                                             "drop-in update time (second update of its scene)"}}
 
 
+# ------------------------------------------------------- profiler case
+def run_profile_case(args):
+    """A small, reproducible batched-PCG launch for profiler captures (not a
+    benchmark): the tall scenes (more than 512 rows) among the first
+    --case-pool scenes of the batched-form generator (the class that dominates
+    a full step), every PCG solve pinned to --case-iterations iterations so a
+    launch is short and identical from run to run, three updates; prints the
+    PCG time of each update."""
+    import ifluids as ifl
+    from ifluids import scenes
+    threads, k, stages = (int(x) for x in (args.shape or "64,1,2").split(","))
+    sc = [x for x in scenes.batch_scenes(count=args.case_pool, seed=BATCH_SEED) if x.h > 512][:args.count]
+    print("scenes", len(sc), "cells", sum(x.w * x.h for x in sc), flush=True)
+    members = [ifl.FluidSolver(x.w, x.h, x.density, body_objs(ifl, x), precision=ifl.FP32) for x in sc]
+    for m in members:
+        m.set_pinned_iterations(args.case_iterations, -1)
+    b = ifl.Batch(members, threads=threads, strips_per_block=k, stages=stages, use_graph=False)
+    for i, x in enumerate(sc):
+        b.set_inflows(i, x.inflows)
+    for u in range(3):
+        b.update(sc[0].dt)
+        print(u, round(b.info()["last_pcg_ms"], 3), "ms", [x[0][0] for x in b.stats()], flush=True)
+    b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--workload", choices=("batch", "single", "c3", "flip", "gs"), default="batch")
+    ap.add_argument("--workload", choices=("batch", "single", "c3", "flip", "gs", "case"), default="batch",
+                    help="case: the small pinned batch used for profiler captures (prints timings, no bench line)")
+    ap.add_argument("--case-pool", type=int, default=64, help="case: generator scenes the tall ones are taken from")
+    ap.add_argument("--case-iterations", type=int, default=20, help="case: PCG iterations per solve")
     ap.add_argument("--gs-variant", type=int, choices=(1, 2), default=1, help="gs workload: tutorial step 1 or 2")
     ap.add_argument("--count", type=int, default=BATCH_COUNT, help="scenes of the batched workload")
     ap.add_argument("--size", type=int, default=0, help="side of the single-scene workload (1024; c3: 2048)")
@@ -990,6 +1018,11 @@ def main():
                     help="scenes whose next update is compared with the FP64 reference after the timed region "
                          "(default: 8 for the batch, 1 for the 1024^2 scene, 0 otherwise)")
     args = ap.parse_args()
+    if args.workload == "case":
+        if args.count == BATCH_COUNT:
+            args.count = 8
+        run_profile_case(args)
+        return
     if not args.size:
         args.size = {"c3": 2048, "flip": 128, "gs": 128}.get(args.workload, 1024)
     if args.field_check < 0:

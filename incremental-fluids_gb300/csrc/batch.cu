@@ -330,27 +330,37 @@ class BatchImpl final : public BatchBase {
 
     // Estimated PCG time of each scene: iterations x (two wavefront sweeps,
     // D + lag per strip steps each; the elementwise passes over its team).
-    // Estimated time of scene i's solves on a team of g blocks, in wavefront
-    // steps: per PCG iteration two sweeps, the elementwise passes (rows per
-    // thread, weighted 4) and the team barriers.  A sweep of S strips by P
-    // warps (strips taken round-robin) finishes after
-    //   max((S-1)*lag + D, (S-1)/P * D + ((S-1) mod P)*lag + D)
-    // steps: strip s starts lag steps after strip s-1 (the boundary-row
-    // hand-over) and not before its warp finished strip s-P.
+    // Estimated time (microseconds) of scene i's solve on a team of g blocks:
+    // per PCG iteration a forward and a backward sweep, the elementwise passes
+    // and the team barriers.  A sweep of S strips by P = g*K warps (strips taken
+    // round-robin) finishes after
+    //   max((S-1)*lag + D*tau, (S-1)/P * D*tau + ((S-1) mod P)*lag + D*tau):
+    // strip s starts a hand-over (lag) after strip s-1 and not before its warp
+    // finished strip s-P.  The elementwise passes cost a fixed time per cell
+    // and warp; a team of more than one block adds its barriers, which grow
+    // with its size.  Constants fitted to per-phase timers in the batched
+    // kernel on GB300 (512-scene batch, FP32 form, 64-thread blocks, teams of
+    // 1 to 64 blocks): tau = 0.11 us per wavefront step, lag = 6.4 us per
+    // strip, 27.4 ns per cell per two-warp block, barriers 15 + 6 log2(g) us
+    // per iteration.
     double plan_cost(int i, int g) const {
-        constexpr double kLag = 48.0, kBarriers = 60.0;
+        constexpr double kTau = 0.11, kLag = 6.4, kElemNs = 27.4;
         const Scene<F> &S = scene(i);
         const int P = g * shape_.K, Sn = S.sd.S;
-        const double D = S.sd.D;
-        const double sweep = std::max((Sn - 1) * kLag + D, ((Sn - 1) / P) * D + ((Sn - 1) % P) * kLag + D);
-        const double elem = 4.0 * (double)S.w * S.h / ((double)g * shape_.threads);
-        return iters_[i] * (2.0 * sweep + elem + kBarriers);
+        const double Dt = S.sd.D * kTau * (sizeof(F) == 8 ? 3.0 : 1.0);
+        const double sweep = std::max((Sn - 1) * kLag + Dt, ((Sn - 1) / P) * Dt + ((Sn - 1) % P) * kLag + Dt);
+        const double elem = 1e-3 * kElemNs * (double)S.w * S.h / g * (64.0 / shape_.threads);
+        const double bars = g == 1 ? 2.0 : 15.0 + 6.0 * std::log2((double)g);
+        return iters_[i] * (2.0 * sweep + elem + bars);
     }
 
     int schedule() {
         // Each scene starts in the class of the smallest team that gives each
         // of its strips its own sweeping warp; the planner then adds teams or
-        // doubles team sizes where the finish time needs them.
+        // doubles team sizes where the finish time needs them.  (Choosing
+        // smaller, round-robin teams for the step time the grid could hold
+        // spent fewer block-microseconds but packed worse on GB300: 1.12-1.24 s
+        // against 1.00 s per step of the 512-scene batch.)
         std::vector<int> cls(n_);
         for (int i = 0; i < n_; i++) {
             const int cover = pow2ceil((scene(i).sd.S + shape_.K - 1) / shape_.K);

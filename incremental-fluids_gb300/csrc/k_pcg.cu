@@ -36,6 +36,7 @@
 // Every wait is bounded: on timeout the status word gets FLAG_TIMEOUT, later
 // waits stop waiting, the kernel runs to its end and the host reports an error.
 #include <algorithm>
+#include <functional>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -1574,10 +1575,10 @@ void pcg_batch_set_max_team(PcgBatchPlan *P, int blocks) { P->max_team = blocks 
 // Teams and queues from a cost model: work(i, g) = estimated time of scene i's
 // solves on a team of g blocks.  Scene i starts in class first_class[i] (teams
 // of 2^c blocks).  Every non-empty class gets one team; then, while blocks are
-// left, the class with the latest estimated finish (its work over its teams,
-// or its largest scene) gets one more team or teams twice as large (up to
-// max_team blocks), whichever shortens that finish most per block spent, as
-// long as it improves.  Each queue is ordered by work, largest first.
+// left, the class with the latest estimated finish (its queue, largest scene
+// first, handed to whichever of its teams frees first) gets one more team or
+// teams twice as large (up to max_team blocks), whichever shortens that
+// finish most per block spent, as long as it improves.  Each queue is ordered by work, largest first.
 // teams[c] and tsize[c] give the teams of class c; returns the blocks in
 // teams, or -1 when the classes' first teams alone exceed the grid.
 int pcg_plan_teams_fn(int grid, int n, const int *first_class, const PlanWork &work, int *teams, int *tsize,
@@ -1589,61 +1590,70 @@ int pcg_plan_teams_fn(int grid, int n, const int *first_class, const PlanWork &w
         members[c].push_back(i);
     }
     int size[kMaxClasses];
-    double tot[kMaxClasses], big[kMaxClasses];
-    auto account = [&](int c, int g, double *t, double *b) {
-        *t = *b = 0.0;
+    // Finish time of a class: its queue (largest first) served by `nt` teams of
+    // g blocks, each job taken by the team that frees first.
+    std::vector<double> loads;  // min-heap of the teams' busy times
+    auto finish = [&](int c, int nt, int g) {
+        loads.assign(std::min<size_t>(nt, members[c].size()), 0.0);
+        double fin = 0.0;
         for (int i : members[c]) {
-            const double v = work(i, g);
-            *t += v;
-            *b = std::max(*b, v);
+            std::pop_heap(loads.begin(), loads.end(), std::greater<double>());
+            loads.back() += work(i, g);
+            fin = std::max(fin, loads.back());
+            std::push_heap(loads.begin(), loads.end(), std::greater<double>());
         }
+        return fin;
     };
+    double fin[kMaxClasses];
     for (int c = 0; c < kMaxClasses; c++) {
         size[c] = 1 << c;
         std::stable_sort(members[c].begin(), members[c].end(),
                          [&](int a, int b) { return work(a, 1 << c) > work(b, 1 << c); });
-        account(c, size[c], &tot[c], &big[c]);
     }
     int left = grid;
     for (int c = 0; c < kMaxClasses; c++) {
         teams[c] = members[c].empty() ? 0 : 1;
         left -= teams[c] << c;
+        fin[c] = members[c].empty() ? 0.0 : finish(c, 1, size[c]);
     }
     if (left < 0) return -1;
     for (;;) {
         int best = -1;
         double bt = -1.0;
         for (int c = 0; c < kMaxClasses; c++) {
-            if (members[c].empty()) continue;
-            const double fin = std::max(tot[c] / teams[c], big[c]);
-            if (fin > bt) {
-                bt = fin;
+            if (!members[c].empty() && fin[c] > bt) {
+                bt = fin[c];
                 best = c;
             }
         }
         if (best < 0) break;
         const int c = best, sz = size[c];
-        // one more team of the current size
-        const bool can_add = teams[c] < (int)members[c].size() && sz <= left;
-        const double fin_add = can_add ? std::max(tot[c] / (teams[c] + 1), big[c]) : bt;
+        // more teams of the current size: the fewest that shorten the finish
+        // (with jobs of equal size one more team may not)
+        int add = 0;
+        double fin_add = bt;
+        for (int k = 1; teams[c] + k <= (int)members[c].size() && k * sz <= left; k++) {
+            fin_add = finish(c, teams[c] + k, sz);
+            if (fin_add < bt) {
+                add = k;
+                break;
+            }
+        }
+        const bool can_add = add > 0;
         // every team of the class twice as large
         const bool can_grow = sz * 2 <= max_team && teams[c] * sz <= left;
-        double fin_grow = bt, tg = 0.0, bg = 0.0;
-        if (can_grow) {
-            account(c, 2 * sz, &tg, &bg);
-            fin_grow = std::max(tg / teams[c], bg);
-        }
+        const double fin_grow = can_grow ? finish(c, teams[c], 2 * sz) : bt;
         // the option that shortens the finish most per block spent
-        const double gain_add = can_add ? (bt - fin_add) / sz : 0.0;
+        const double gain_add = can_add ? (bt - fin_add) / ((double)add * sz) : 0.0;
         const double gain_grow = can_grow ? (bt - fin_grow) / ((double)teams[c] * sz) : 0.0;
         if (gain_add > 0.0 && gain_add >= gain_grow) {
-            teams[c]++;
-            left -= sz;
+            teams[c] += add;
+            left -= add * sz;
+            fin[c] = fin_add;
         } else if (gain_grow > 0.0) {
             left -= teams[c] * sz;
             size[c] = 2 * sz;
-            tot[c] = tg;
-            big[c] = bg;
+            fin[c] = fin_grow;
         } else {
             break;
         }
