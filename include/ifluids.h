@@ -404,6 +404,11 @@ typedef struct {
     int32_t active, queued;
     int64_t bytes_in_use, cell_steps, steps, rebuilds;
     int32_t threads, strips_per_block, stages, pad_;
+    int64_t peak_queued;  /* longest queue seen at a step (after admission)     */
+    int64_t admitted, completed;  /* requests admitted / finished so far         */
+    double rebuild_ms;    /* host time spent on new memberships: building the
+                             batch and what its first step costs beyond a
+                             steady step (plan, graph capture)               */
 } ifl_server_info;
 
 void ifl_server_default_params(ifl_server_params *p, int variant, int precision);

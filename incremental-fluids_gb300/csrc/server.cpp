@@ -95,15 +95,29 @@ class Server {
 
     int step(int *n_active, int *n_queued) {
         admit();
+        peak_queued_ = std::max<int64_t>(peak_queued_, (int64_t)queue_.size());
         int e = IFL_OK;
         if (!active_.empty()) {
             if (!p_.dry_run) {
+                const bool fresh = dirty_;
+                const auto t0 = std::chrono::steady_clock::now();
                 if (dirty_) {
                     if ((e = rebuild())) return e;
                 }
+                const auto t1 = std::chrono::steady_clock::now();
                 if ((e = batch_->update(p_.dt))) {
                     err_ = batch_->error();
                     return e;
+                }
+                if (fresh) {
+                    // a new membership: building the batch, plus what its first
+                    // step spends beyond a steady step (plan, graph capture)
+                    const auto t2 = std::chrono::steady_clock::now();
+                    const double build = std::chrono::duration<double, std::milli>(t1 - t0).count();
+                    const double first = std::chrono::duration<double, std::milli>(t2 - t1).count();
+                    rebuild_ms_ += build + std::max(0.0, first - last_steady_ms_);
+                } else {
+                    last_steady_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
                 }
             }
             const double t = now();
@@ -114,6 +128,7 @@ class Server {
                 cell_steps_ += (int64_t)q->prm.w * q->prm.h;
                 if (!p_.dry_run) q->solver->advance_bodies(p_.dt);  // SolidBody::update between steps
                 if (q->done >= q->steps) {
+                    completed_++;
                     q->state = Request::DONE;
                     q->finished = t;
                     finished_.push_back(q->id);
@@ -196,6 +211,10 @@ class Server {
         o->threads = opt_.threads;
         o->strips_per_block = opt_.strips_per_block;
         o->stages = opt_.stages;
+        o->peak_queued = peak_queued_;
+        o->admitted = admitted_;
+        o->completed = completed_;
+        o->rebuild_ms = rebuild_ms_;
     }
 
     const std::string &error() const { return err_; }
@@ -220,6 +239,7 @@ class Server {
                 if (!q->bodies.empty()) q->solver->set_bodies(q->bodies.data(), (int)q->bodies.size());
             }
             queue_.pop_front();
+            admitted_++;
             in_use_ += q->bytes;
             q->state = Request::ACTIVE;
             q->admitted = now();
@@ -274,7 +294,8 @@ class Server {
     std::unique_ptr<BatchBase> batch_;
     bool dirty_ = false, tune_pending_ = false;
     size_t in_use_ = 0;
-    int64_t cell_steps_ = 0, steps_run_ = 0, rebuilds_ = 0;
+    int64_t cell_steps_ = 0, steps_run_ = 0, rebuilds_ = 0, peak_queued_ = 0, admitted_ = 0, completed_ = 0;
+    double rebuild_ms_ = 0.0, last_steady_ms_ = 0.0;
     std::string err_;
 };
 

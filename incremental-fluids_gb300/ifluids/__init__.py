@@ -129,7 +129,9 @@ class Completion(C.Structure):
 class ServerInfo(C.Structure):
     _fields_ = [("active", C.c_int32), ("queued", C.c_int32), ("bytes_in_use", C.c_int64),
                 ("cell_steps", C.c_int64), ("steps", C.c_int64), ("rebuilds", C.c_int64), ("threads", C.c_int32),
-                ("strips_per_block", C.c_int32), ("stages", C.c_int32), ("pad_", C.c_int32)]
+                ("strips_per_block", C.c_int32), ("stages", C.c_int32), ("pad_", C.c_int32),
+                ("peak_queued", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
+                ("rebuild_ms", C.c_double)]
 
 
 class IflError(RuntimeError):
