@@ -449,45 +449,87 @@ __global__ void extrap_mask_kernel(Scene<F> S, unsigned qmask, int *counters) {
     extrap_mask_body(S, qmask, counters, blockIdx);
 }
 
-// Pass 2: one CTA per quantity relaxes its list until nothing changes.
+// Pass 2: one CTA per quantity solves the DAG by frontiers.  The first
+// frontier holds the listed cells whose upstream neighbours are all fluid
+// (mask 0).  A round computes its frontier (every value in it depends only on
+// cells that are final); after a barrier, which makes the round's values
+// visible to the whole CTA, each computed cell looks at its four neighbours: a
+// pending listed cell whose upstream neighbours are now all done joins the
+// next frontier, claimed once by an atomic compare-and-swap of its state
+// (0 pending, 2 queued, 1 done).  The work is proportional to the solid cells,
+// not to cells times the depth of the DAG, and each cell still gets the value
+// the reference's stack computes for it.  Cells on an upwind cycle are never
+// queued, as the reference never solves them.
+template <typename F>
+__device__ __forceinline__ bool extrap_claim(uint8_t *ready, long idx) {
+    unsigned *w = (unsigned *)((uintptr_t)(ready + idx) & ~(uintptr_t)3);
+    const unsigned sh = 8u * (unsigned)((uintptr_t)(ready + idx) & 3);
+    unsigned old = *(volatile unsigned *)w;
+    for (;;) {
+        if ((old >> sh) & 0xffu) return false;
+        const unsigned seen = atomicCAS(w, old, old | (2u << sh));
+        if (seen == old) return true;
+        old = seen;
+    }
+}
+
 template <typename F>
 __device__ __forceinline__ void extrap_solve_body(const Scene<F> &S, unsigned qmask, const int *counters, int qi) {
     if (!((qmask >> qi) & 1u)) return;
     Quant<F> Q = S.q[qi];
     const long P = S.P;
     const size_t cap = (size_t)P * (S.h + 2);
-    int *cur = Q.list, *nxt = Q.list + cap;
-    int cnt = counters[qi];
-    __shared__ int s_next;
-    const int max_rounds = Q.w + Q.h + 16;
-    for (int round = 0; round < max_rounds && cnt > 0; round++) {
-        if (threadIdx.x == 0) s_next = 0;
+    // the list is read once (first frontier); the frontiers then alternate
+    // between the second half and the first half of the list buffer
+    const int *lst = Q.list;
+    int *cur = Q.list + cap, *nxt = Q.list;
+    const int cnt = counters[qi];
+    __shared__ int s_n;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const int e = lst[i];
+        if ((e & 3) == 0) {
+            Q.ready[e >> 2] = 2;
+            cur[atomicAdd(&s_n, 1)] = e >> 2;
+        }
+    }
+    __syncthreads();
+    int n = s_n;
+    __syncthreads();
+    while (n > 0) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const long idx = cur[i];
+            const double nx = Q.nx[idx], ny = Q.ny[idx];
+            const long ix = idx + sgn(nx), iy = idx + (long)sgn(ny) * P;
+            const double sx = (double)Q.src[ix], sy = (double)Q.src[iy];
+            Q.src[idx] = (F)((fabs(nx) * sx + fabs(ny) * sy) / (fabs(nx) + fabs(ny)));
+            Q.ready[idx] = 1;
+        }
+        if (threadIdx.x == 0) s_n = 0;
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            int e = cur[i];
-            long idx = e >> 2;
-            int m = e & 3;
-            double nx = Q.nx[idx], ny = Q.ny[idx];
-            long ix = idx + sgn(nx), iy = idx + (long)sgn(ny) * P;
-            bool ok = (!(m & 1) || ldv(Q.ready + ix)) && (!(m & 2) || ldv(Q.ready + iy));
-            if (ok) {
-                double sx = (double)ldv(Q.src + ix), sy = (double)ldv(Q.src + iy);
-                double val = (fabs(nx) * sx + fabs(ny) * sy) / (fabs(nx) + fabs(ny));
-                stv(Q.src + idx, (F)val);
-                __threadfence_block();
-                stv(Q.ready + idx, (uint8_t)1);
-            } else {
-                nxt[atomicAdd(&s_next, 1)] = e;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const long idx = cur[i];
+            const long nbr[4] = {idx - 1, idx + 1, idx - P, idx + P};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const long j = nbr[k];
+                const int x = (int)(j % P), y = (int)(j / P);
+                if (x < 1 || y < 1 || x >= Q.w - 1 || y >= Q.h - 1) continue;  // the outer ring is never extrapolated
+                if (Q.cell[j] == CELL_FLUID || Q.ready[j] != 0) continue;
+                const double nx = Q.nx[j], ny = Q.ny[j];
+                const long jx = j + sgn(nx), jy = j + (long)sgn(ny) * P;
+                const bool wx = nx != 0.0 && Q.cell[jx] != CELL_FLUID, wy = ny != 0.0 && Q.cell[jy] != CELL_FLUID;
+                if ((wx && Q.ready[jx] != 1) || (wy && Q.ready[jy] != 1)) continue;
+                if (extrap_claim<F>(Q.ready, j)) nxt[atomicAdd(&s_n, 1)] = (int)j;
             }
         }
         __syncthreads();
-        int n2 = s_next;
-        __syncthreads();
-        if (n2 == cnt) break;  // upwind cycle: the reference never solves these cells either
+        n = s_n;
         int *t = cur;
         cur = nxt;
         nxt = t;
-        cnt = n2;
+        __syncthreads();
     }
 }
 template <typename F>
