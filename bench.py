@@ -77,11 +77,12 @@ def pcg_bytes_per_cell(F: int, iterations: int) -> float:
 
 # Bytes per cell the kernels of this library actually move for one solve (its
 # own layout: 1-byte neighbour bits, the 4-word MIC(0) record, an FP32 copy of
-# r, a separate z.r pass); reported beside the algorithmic figure.
+# r; the FP64 form's separate z.r pass, which the FP32 form folds into its
+# forward sweep as q.q); reported beside the algorithmic figure.
 def pcg_kernel_bytes_per_cell(F: int, iterations: int) -> float:
     copy = F if F == 4 else 0
     factor, setup = 7 * F + 9, 17 + copy
-    sweeps = 6 * F + 6 * F + F + 9
+    sweeps = 6 * F + 6 * F + (0 if F == 4 else F + 9)
     per_iter = (6 * F + 9) + (41 + F + copy)
     return factor + setup + sweeps + iterations * per_iter + max(iterations - 1, 0) * sweeps
 

@@ -411,6 +411,12 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
 
     V prev = V(0);                   // result of the previous cell in sweep order
     F prev_a = F(0), prev_b = F(0);  // forward: lx, ly of that cell; factor: ax, ay
+    // FP32 form, forward solve: this lane's sum of q*q over its cells (sigma,
+    // see pcg_job), fused FP32 products over one staged block of diagonals,
+    // then added in FP64 (keeps the FP64 pipe, 1/64 of the FP32 rate on this
+    // part, off the per-cell path).
+    constexpr bool kQQ = KIND == 1 && sizeof(F) == 4;
+    double qq = 0.0;
 
     // Halo prefetch: lane l < kHB holds the word of the column that the
     // waiting lane reaches at step t0 + l, and where needed the lower
@@ -458,6 +464,7 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
         const F *g1 = (const F *)(sbuf + S1);
         const F *g2 = (const F *)(sbuf + 2 * S1);
         const uint8_t *gnb = (const uint8_t *)(sbuf + 3 * S1);
+        float qq32 = 0.f;
         for (int sub = 0; sub < kB / kHB; sub++) {
             const int t0 = blk * kB + sub * kHB;
             // stage this sub-block's operands in registers
@@ -596,11 +603,21 @@ __device__ void sweep_strip(const PcgArgs<F> &A, int s, Ring<F> &R, const Chan i
                         st4(micp + 4 * i, self ? (F)((double)o1[jj] * pcv) : F(0),
                             self ? (F)((double)o2[jj] * pcv) : F(0), self ? (F)pcv : F(0), nb_word(b, F(0)));
                     } else {
-                        if (b & NB_SELF) zout[i] = res[jj];
+                        if (b & NB_SELF) {
+                            zout[i] = res[jj];
+                            if constexpr (kQQ) qq32 = fmaf((float)res[jj], (float)res[jj], qq32);
+                        }
                     }
                 }
             }
         }
+        if constexpr (kQQ) qq += (double)qq32;
+    }
+    if constexpr (kQQ) {
+        // the strip's partial: lanes by a fixed shuffle tree (independent of
+        // which warp of which team sweeps the strip)
+        qq = warp_sum(qq);
+        if (lane == 0) A.partials[2 * (size_t)((sd.S * D + kChunk - 1) / kChunk) + s] = qq;
     }
     __syncwarp();
 }
@@ -765,17 +782,18 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     // loads (from L2: other blocks wrote them before the team barrier) are
     // issued eight at a time, so a scene of thousands of chunks costs a few
     // memory latencies, not one per 32 chunks.
-    auto chunk_total = [&](int slot, bool is_max) -> double {
+    // n: the slot's number of partials (chunks; strips for sigma).
+    auto chunk_total = [&](int slot, bool is_max, int n) -> double {
         if (threadIdx.x < 32) {
             double acc = 0.0;
             const double *pt = A.partials + (size_t)slot * nchunk;
-            for (int c0 = lane; c0 < nchunk; c0 += 32 * 8) {
+            for (int c0 = lane; c0 < n; c0 += 32 * 8) {
                 double v[8];
 #pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = c0 + 32 * j < nchunk ? __ldcg(pt + c0 + 32 * j) : 0.0;
+                for (int j = 0; j < 8; j++) v[j] = c0 + 32 * j < n ? __ldcg(pt + c0 + 32 * j) : 0.0;
 #pragma unroll
                 for (int j = 0; j < 8; j++)
-                    if (c0 + 32 * j < nchunk) acc = is_max ? smax(acc, v[j]) : acc + v[j];
+                    if (c0 + 32 * j < n) acc = is_max ? smax(acc, v[j]) : acc + v[j];
             }
             acc = is_max ? warp_max(acc) : warp_sum(acc);
             if (lane == 0) sm[kMaxWarps] = acc;
@@ -805,9 +823,11 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
         return true;
     };
 
-    // sigma = z . r over the red cells (3-conjugate-gradients/Fluid.cpp:356, 376):
-    // a separate pass keeps the FP64 products off the backward sweep's chain.
-    // Staged: z, r and the neighbour bits of a unit.
+    // sigma = z . r over the red cells (3-conjugate-gradients/Fluid.cpp:356, 376).
+    // FP64 form: a separate pass after the backward solve, z_i * r_i as the
+    // reference forms them (FP64 products on the sweeping warp's chain would
+    // cost the wavefront more than the pass).  Staged: z, r and the neighbour
+    // bits of a unit.
     auto dot_zr = [&]() {
         constexpr unsigned kRow = 32u * (sizeof(F) + 8 + 1);
         const int U = unit_rows(R.sbytes, kRow);
@@ -828,11 +848,29 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 const uint8_t *snb = (const uint8_t *)(g_smem + onb);
                 for (int u = 0; u < U; u++) {
                     const int k = u * 32 + lane;
-                    // FP32 form: one rounding per product-add (fused)
-                    if (snb[k] & NB_RED) acc = kF32 ? fma((double)sz[k], sr[k], acc) : acc + (double)sz[k] * sr[k];
+                    if (snb[k] & NB_RED) acc = acc + (double)sz[k] * sr[k];
                 }
             }
             chunk_put(2, c, acc, false);
+        }
+    };
+    // FP32 form: sigma is taken as q . q, q = L^-1 r the forward solve's result.
+    // The MIC(0) apply is z = L^-T L^-1 r with L's diagonal 1/precon and its
+    // strictly lower part aPlus*precon of the column's cell (the forward solve's
+    // coefficients; the backward solve uses the same ones transposed, also after
+    // FP32 rounding), so z . r = (L^-1 r) . (L^-1 r) exactly, and in floating
+    // point within the rounding of the two triangular solves.  The forward sweep
+    // adds q*q up per strip (slot 2 holds one partial per strip): no pass over z
+    // and r and no team barrier for it.  Cells outside the masked MIC(0) work
+    // hold q = 0 (and r = 0: the right-hand side and A*s vanish there), so they
+    // add nothing to either form.
+    auto sigma_of_sweeps = [&]() -> double {
+        if constexpr (kF32) {
+            return chunk_total(2, false, sd.S);
+        } else {
+            dot_zr();
+            team_barrier(T, A.fl);
+            return chunk_total(2, false, nchunk);
         }
     };
 
@@ -1058,11 +1096,9 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     team_barrier(T, A.fl);
     sweep<2, F>(A, T, R, hsm_off, nstrips_blk);
     team_barrier(T, A.fl);
-    dot_zr();
-    team_barrier(T, A.fl);
 
-    double maxError = chunk_total(0, true);
-    double sigma = chunk_total(2, false);
+    double maxError = chunk_total(0, true, nchunk);
+    double sigma = sigma_of_sweeps();
     int iterations = 0, status;
     if (A.pinned >= 0 ? A.pinned == 0 : maxError < kTol) {
         status = 1;
@@ -1077,11 +1113,11 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
             matvec(iter, beta);
             team_barrier(T, A.fl);
-            const double alpha = sigma / chunk_total(1, false);
+            const double alpha = sigma / chunk_total(1, false, nchunk);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
             axpy(iter, alpha);
             team_barrier(T, A.fl);
-            maxError = chunk_total(0, true);
+            maxError = chunk_total(0, true, nchunk);
             iterations = iter + 1;
             if (A.pinned >= 0 ? iterations >= A.pinned : maxError < kTol) {
                 status = 0;
@@ -1092,9 +1128,7 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             team_barrier(T, A.fl);
             sweep<2, F>(A, T, R, hsm_off, nstrips_blk);
             team_barrier(T, A.fl);
-            dot_zr();
-            team_barrier(T, A.fl);
-            const double sigmaNew = chunk_total(2, false);
+            const double sigmaNew = sigma_of_sweeps();
             beta = sigmaNew / sigma;
             sigma = sigmaNew;
         }
