@@ -883,7 +883,7 @@ def run_batch(args, rank, world, local_rank):
             "gpu_launches": launches, "clocks": clk.summary(), "fp64_dropin": fp64, "cells": cells,
             "latency_ms": {"p50": round(pct(0.50), 1), "p99": round(pct(0.99), 1)},
             "batch": {k: info[k] for k in ("members", "threads", "strips_per_block", "stages", "grid", "graph",
-                                           "candidate_ms")}}
+                                           "candidate_ms", "tiles", "tile_ms")}}
 
 
 # ------------------------------------------------------------- serving

@@ -320,7 +320,30 @@ typedef struct {
     int32_t use_graph;        /* 1: replay each step as one CUDA graph (default) */
     int32_t tune_iterations;  /* PCG iterations per autotuning trial (default 8) */
     int32_t max_team_blocks;  /* largest team (blocks working on one scene); 0: 128 */
+    /* Tile shapes (threads x rows of one block) of the tiled phase kernels.
+     * 1 (default): at the first update every candidate shape runs each phase
+     * of IFL_TILE_FILL .. IFL_TILE_ADVECT twice on the real state (those
+     * phases are idempotent) and the fastest is kept per phase; 0: 32 x 8
+     * everywhere; 2: the shapes given in tile_w / tile_h.  A cell's results do
+     * not depend on the tile shape. */
+    int32_t tile_tune;
+    int32_t pad_;
+    int32_t tile_w[8], tile_h[8]; /* tile_tune 2: per IFL_TILE_* phase; one of the candidates */
 } ifl_batch_options;
+
+/* Tiled phases of a batch step (index into tile_w / tile_h). */
+enum {
+    IFL_TILE_FILL = 0,          /* fillSolidFields: phi, cell, volume, normals */
+    IFL_TILE_BC = 1,            /* setBoundaryCondition */
+    IFL_TILE_ASSEMBLE = 2,      /* buildRhs, buildPressureMatrix, densities */
+    IFL_TILE_HEAT_ASSEMBLE = 3, /* heat matrix and right-hand side */
+    IFL_TILE_ADVECT = 4,        /* advect of every quantity */
+    IFL_TILE_APPLY = 5,         /* applyPressure (32 x 8: not idempotent, not tuned) */
+    IFL_TILE_BUOYANCY = 6,      /* addBuoyancy (32 x 8, not tuned) */
+    IFL_TILE_MASK = 7,          /* extrapolation mask (32 x 8, not tuned) */
+    IFL_TILE_PHASES = 8
+};
+/* Candidate tile shapes (threads x rows): 32x8, 32x4, 64x4, 16x16, 128x2, 64x2. */
 
 typedef struct {
     int32_t members;
@@ -336,6 +359,8 @@ typedef struct {
     int64_t steps;
     int64_t h2d_bytes_last_step;                /* host -> device bytes of the last step */
     int64_t d2h_bytes_last_step;                /* device -> host bytes of the last step */
+    int32_t tile_w[8], tile_h[8];               /* tile shape of each IFL_TILE_* phase in use */
+    double tile_ms[8];                          /* tuned phases: trial time of the shape kept (ms) */
 } ifl_batch_info;
 
 void ifl_batch_default_options(ifl_batch_options *o);

@@ -78,7 +78,7 @@ class BatchImpl final : public BatchBase {
         const size_t o_bd = off;
         off = al256(off + (size_t)n_ * kMaxBodies * sizeof(DevBody));
         const size_t o_ts = off;
-        off = al256(off + (n_ + 1) * sizeof(int));
+        off = al256(off + (size_t)kTileShapes * (n_ + 1) * sizeof(int));
         const size_t o_is = off;
         off = al256(off + (n_ + 1) * sizeof(int));
         const size_t o_in = off;
@@ -125,29 +125,43 @@ class BatchImpl final : public BatchBase {
         std::memset(h_stats_, 0, 2 * n_ * sizeof(PcgOut));
         std::memset(h_sflags_, 0, n_ * sizeof(unsigned));
 
-        // static tables
-        std::vector<int> ts(n_ + 1, 0);
+        // static tables: the tile prefix sums of every candidate tile shape
+        std::vector<int> ts((size_t)kTileShapes * (n_ + 1), 0);
         std::vector<PcgOut *> outs(n_);
         std::vector<unsigned *> fls(n_);
-        for (int i = 0; i < n_; i++) {
-            const Scene<F> &S = scene(i);
-            ts[i + 1] = ts[i] + batch_tiles(S.w, S.h);
-            outs[i] = ((PcgScratch *)m_[i]->scratch_ptr())->out;
-            fls[i] = S.flags;
+        for (int k = 0; k < kTileShapes; k++) {
+            int *t = ts.data() + (size_t)k * (n_ + 1);
+            for (int i = 0; i < n_; i++) t[i + 1] = t[i] + batch_tiles(scene(i).w, scene(i).h, kTileW[k], kTileH[k]);
         }
-        tiles_ = ts[n_];
+        for (int i = 0; i < n_; i++) {
+            outs[i] = ((PcgScratch *)m_[i]->scratch_ptr())->out;
+            fls[i] = scene(i).flags;
+        }
         if (check(cudaMemcpy(d_tile_start_, ts.data(), ts.size() * sizeof(int), cudaMemcpyHostToDevice), "tables") ||
             check(cudaMemcpy(d_outs_, outs.data(), n_ * sizeof(PcgOut *), cudaMemcpyHostToDevice), "tables") ||
             check(cudaMemcpy(d_flags_, fls.data(), n_ * sizeof(unsigned *), cudaMemcpyHostToDevice), "tables"))
             return IFL_ERR_CUDA;
         inflows_.assign(n_, {});
         if (int e = upload_inflows()) return e;
-        B_.scenes = d_scenes_;
-        B_.tile_start = d_tile_start_;
-        B_.inflows = d_inflows_;
-        B_.inflow_start = d_inflow_start_;
-        B_.n = n_;
-        B_.tiles = tiles_;
+        for (int k = 0; k < kTileShapes; k++) {
+            SceneBatch<F> &b = tb_[k];
+            b.scenes = d_scenes_;
+            b.tile_start = d_tile_start_ + (size_t)k * (n_ + 1);
+            b.inflows = d_inflows_;
+            b.inflow_start = d_inflow_start_;
+            b.n = n_;
+            b.tiles = ts[(size_t)k * (n_ + 1) + n_];
+            b.tw = kTileW[k];
+            b.th = kTileH[k];
+        }
+        B_ = tb_[0];
+        for (int p = 0; p < IFL_TILE_PHASES; p++) tile_pick_[p] = 0;
+        if (opt_.tile_tune == 2) {
+            for (int p = 0; p < IFL_TILE_ADVECT + 1; p++) tile_pick_[p] = tile_index(opt_.tile_w[p], opt_.tile_h[p]);
+            tiles_tuned_ = true;
+        } else if (opt_.tile_tune == 0) {
+            tiles_tuned_ = true;
+        }
 
         iters_.assign(n_, 0.0);
         for (int i = 0; i < n_; i++) {
@@ -176,6 +190,10 @@ class BatchImpl final : public BatchBase {
                 check(cudaStreamWaitEvent(st_, member_ev_[i], 0), "member wait"))
                 return IFL_ERR_CUDA;
         if (int e = stage_tables()) return e;
+        if (!tiles_tuned_) {
+            if (int e = autotune_tiles(dt)) return e;
+            tiles_tuned_ = true;
+        }
         if (!tuned_) {
             if (int e = autotune(dt)) return e;
             tuned_ = true;
@@ -246,6 +264,11 @@ class BatchImpl final : public BatchBase {
         o->steps = steps_;
         o->h2d_bytes_last_step = h2d_bytes_;
         o->d2h_bytes_last_step = (int64_t)(2 * n_ * sizeof(PcgOut) + n_ * sizeof(unsigned));
+        for (int p = 0; p < IFL_TILE_PHASES; p++) {
+            o->tile_w[p] = kTileW[tile_pick_[p]];
+            o->tile_h[p] = kTileH[tile_pick_[p]];
+            o->tile_ms[p] = tile_ms_[p];
+        }
         return IFL_OK;
     }
 
@@ -341,16 +364,18 @@ class BatchImpl final : public BatchBase {
     // with its size.  Constants fitted to per-phase timers in the batched
     // kernel on GB300 (512-scene batch, FP32 form, 64-thread blocks, teams of
     // 1 to 64 blocks): tau = 0.11 us per wavefront step, lag = 6.4 us per
-    // strip, 27.4 ns per cell per two-warp block, barriers 15 + 6 log2(g) us
-    // per iteration.
+    // strip, 27.4 ns per cell per two-warp block for three elementwise passes,
+    // barriers 15 + 6 log2(g) us for five team barriers per iteration; the
+    // sigma pass (about an eighth of the elementwise time) and one barrier have
+    // since moved into the forward sweep, leaving 24 ns and 12 + 4.8 log2(g).
     double plan_cost(int i, int g) const {
-        constexpr double kTau = 0.11, kLag = 6.4, kElemNs = 27.4;
+        constexpr double kTau = 0.11, kLag = 6.4, kElemNs = 24.0;
         const Scene<F> &S = scene(i);
         const int P = g * shape_.K, Sn = S.sd.S;
         const double Dt = S.sd.D * kTau * (sizeof(F) == 8 ? 3.0 : 1.0);
         const double sweep = std::max((Sn - 1) * kLag + Dt, ((Sn - 1) / P) * Dt + ((Sn - 1) % P) * kLag + Dt);
         const double elem = 1e-3 * kElemNs * (double)S.w * S.h / g * (64.0 / shape_.threads);
-        const double bars = g == 1 ? 2.0 : 15.0 + 6.0 * std::log2((double)g);
+        const double bars = g == 1 ? 1.6 : 12.0 + 4.8 * std::log2((double)g);
         return iters_[i] * (2.0 * sweep + elem + bars);
     }
 
@@ -414,18 +439,18 @@ class BatchImpl final : public BatchBase {
         launch_batch_inflow<F>(B_, st_);
         launches_++;
         if (variant_ >= IFL_SOLID) {
-            launch_batch_fill_solid<F>(B_, variant_, nq_, st_);
+            launch_batch_fill_solid<F>(TB(IFL_TILE_FILL), variant_, nq_, st_);
             launches_ += variant_ >= IFL_CURVED ? 2 : 1;
         }
         if (variant_ >= IFL_HEAT) {
-            launch_batch_heat_assemble<F>(B_, dt, st_);
+            launch_batch_heat_assemble<F>(TB(IFL_TILE_HEAT_ASSEMBLE), dt, st_);
             launches_++;
         } else {
             if (variant_ >= IFL_SOLID) {
-                launch_batch_bc<F>(B_, st_);
+                launch_batch_bc<F>(TB(IFL_TILE_BC), st_);
                 launches_++;
             }
-            launch_batch_assemble<F>(B_, dt, ASM_RHS | ASM_MATRIX, st_);
+            launch_batch_assemble<F>(TB(IFL_TILE_ASSEMBLE), dt, ASM_RHS | ASM_MATRIX, st_);
             launches_++;
         }
     }
@@ -443,9 +468,9 @@ class BatchImpl final : public BatchBase {
             launch_batch_heat_to_rows<F>(B_, st_);
             launch_batch_extrapolate<F>(B_, 1u << 1, st_);
             launch_batch_buoyancy<F>(B_, dt, st_);
-            launch_batch_bc<F>(B_, st_);
-            launch_batch_assemble<F>(B_, dt, ASM_RHS | ASM_MATRIX | (variant_ >= IFL_VARDENS ? ASM_DENS : 0),
-                                     st_);
+            launch_batch_bc<F>(TB(IFL_TILE_BC), st_);
+            launch_batch_assemble<F>(TB(IFL_TILE_ASSEMBLE), dt,
+                                     ASM_RHS | ASM_MATRIX | (variant_ >= IFL_VARDENS ? ASM_DENS : 0), st_);
             launches_ += 1 + 3 + 1 + 1 + 1;
         }
         if (timed) cudaEventRecordWithFlags(ev_pcg0_, st_, ext);
@@ -455,10 +480,10 @@ class BatchImpl final : public BatchBase {
         launches_++;
         if (variant_ >= IFL_SOLID) {
             launch_batch_extrapolate<F>(B_, (1u << 0) | (1u << 2) | (1u << 3), st_);
-            launch_batch_bc<F>(B_, st_);
+            launch_batch_bc<F>(TB(IFL_TILE_BC), st_);
             launches_ += 4;
         }
-        launch_batch_advect<F>(B_, dt, st_);
+        launch_batch_advect<F>(TB(IFL_TILE_ADVECT), dt, st_);
         gather_stats_kernel<<<(n_ + 127) / 128, 128, 0, st_>>>(d_outs_, d_flags_, d_stats_, d_sflags_, n_);
         launches_ += 2;
         if (check(cudaMemcpyAsync(h_stats_, d_stats_, 2 * n_ * sizeof(PcgOut), cudaMemcpyDeviceToHost, st_),
@@ -501,6 +526,75 @@ class BatchImpl final : public BatchBase {
         cudaGraphDestroy(g);
         graph_dt_ = dt;
         return IFL_OK;
+    }
+
+    const SceneBatch<F> &TB(int phase) const { return tb_[tile_pick_[phase]]; }
+
+    static int tile_index(int w, int h) {
+        for (int k = 0; k < kTileShapes; k++)
+            if (kTileW[k] == w && kTileH[k] == h) return k;
+        return -1;
+    }
+
+    // One launch of a tuned phase with tile shape k (the phase's arguments of
+    // this variant's step); false if the variant has no such phase.
+    bool tile_trial(int phase, int k, double dt) {
+        const SceneBatch<F> &b = tb_[k];
+        switch (phase) {
+        case IFL_TILE_FILL:
+            if (variant_ < IFL_SOLID) return false;
+            launch_batch_fill_solid<F>(b, variant_, nq_, st_);
+            launches_ += variant_ >= IFL_CURVED ? 2 : 1;
+            return true;
+        case IFL_TILE_BC:
+            if (variant_ < IFL_SOLID) return false;
+            launch_batch_bc<F>(b, st_);
+            break;
+        case IFL_TILE_ASSEMBLE:
+            launch_batch_assemble<F>(b, dt, ASM_RHS | ASM_MATRIX | (variant_ >= IFL_VARDENS ? ASM_DENS : 0), st_);
+            break;
+        case IFL_TILE_HEAT_ASSEMBLE:
+            if (variant_ < IFL_HEAT) return false;
+            launch_batch_heat_assemble<F>(b, dt, st_);
+            break;
+        case IFL_TILE_ADVECT:
+            launch_batch_advect<F>(b, dt, st_);
+            break;
+        default:
+            return false;
+        }
+        launches_++;
+        return true;
+    }
+
+    // Tile shapes of the tuned phases: each candidate runs each phase twice on
+    // the current state (the faster run counts).  These phases are idempotent:
+    // they write only what the step rewrites before reading it (solid fields,
+    // boundary velocities, the systems and right-hand sides, the advected
+    // copies), and the step that follows runs every one of them again.
+    int autotune_tiles(double dt) {
+        for (int p = 0; p <= IFL_TILE_ADVECT; p++) {
+            double best = std::numeric_limits<double>::infinity();
+            for (int k = 0; k < kTileShapes; k++) {
+                double t = std::numeric_limits<double>::infinity();
+                for (int rep = 0; rep < 2; rep++) {
+                    if (check(cudaEventRecord(ev_trial0_, st_), "event")) return IFL_ERR_CUDA;
+                    if (!tile_trial(p, k, dt)) break;
+                    if (check(cudaEventRecord(ev_trial1_, st_), "event") ||
+                        check(cudaEventSynchronize(ev_trial1_), "tile autotune"))
+                        return IFL_ERR_CUDA;
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ev_trial0_, ev_trial1_);
+                    t = std::min(t, (double)ms);
+                }
+                if (t < best) {
+                    best = t;
+                    tile_pick_[p] = k;
+                }
+            }
+            tile_ms_[p] = best < std::numeric_limits<double>::infinity() ? best : 0.0;
+        }
+        return check(cudaGetLastError(), "tile autotune") ? IFL_ERR_CUDA : IFL_OK;
     }
 
     // Each candidate shape solves the first step's real system with a pinned
@@ -567,7 +661,7 @@ class BatchImpl final : public BatchBase {
 
     std::vector<SolverBase *> m_;
     ifl_batch_options opt_;
-    int n_ = 0, variant_ = 0, nq_ = 3, dev_ = 0, tiles_ = 0;
+    int n_ = 0, variant_ = 0, nq_ = 3, dev_ = 0;
     cudaStream_t st_ = nullptr;
     std::vector<cudaEvent_t> member_ev_;
     cudaEvent_t ev_step0_ = nullptr, ev_step1_ = nullptr, ev_pcg0_ = nullptr, ev_pcg1_ = nullptr;
@@ -590,7 +684,11 @@ class BatchImpl final : public BatchBase {
     PcgOut *h_stats_ = nullptr;
     unsigned *h_sflags_ = nullptr;
     std::vector<std::vector<ifl_inflow>> inflows_;
-    SceneBatch<F> B_{};
+    SceneBatch<F> B_{};                 // 32 x 8 tiles (the phases that are not tuned)
+    SceneBatch<F> tb_[kTileShapes]{};   // the same tables for every candidate tile shape
+    int tile_pick_[IFL_TILE_PHASES]{};  // candidate in use per IFL_TILE_* phase
+    double tile_ms_[IFL_TILE_PHASES]{};
+    bool tiles_tuned_ = false;
     PcgBatchPlan *plan_ = nullptr;
     PcgShape shape_{};
     bool tuned_ = false;
@@ -629,6 +727,17 @@ int make_batch(SolverBase *const *members, int n, const ifl_batch_options &opt, 
     if (opt.threads != 0 && opt.threads != 32 && opt.threads != 64 && opt.threads != 128 && opt.threads != 256)
         return IFL_ERR_ARG;
     if (opt.max_team_blocks < 0) return IFL_ERR_ARG;
+    if (opt.tile_tune < 0 || opt.tile_tune > 2) return IFL_ERR_ARG;
+    if (opt.tile_tune == 2)
+        for (int p = 0; p <= IFL_TILE_ADVECT; p++) {
+            bool ok = false;
+            for (int k = 0; k < kTileShapes; k++) ok = ok || (opt.tile_w[p] == kTileW[k] && opt.tile_h[p] == kTileH[k]);
+            if (!ok) {
+                if (err) *err = "tile shape " + std::to_string(opt.tile_w[p]) + "x" + std::to_string(opt.tile_h[p]) +
+                                " is not a candidate";
+                return IFL_ERR_ARG;
+            }
+        }
     std::vector<SolverBase *> m(members, members + n);
     int e;
     if (p0.precision == IFL_FP32) {

@@ -377,6 +377,11 @@ void ifl_batch_default_options(ifl_batch_options *o) {
     std::memset(o, 0, sizeof *o);
     o->use_graph = 1;
     o->tune_iterations = 8;
+    o->tile_tune = 1;
+    for (int p = 0; p < 8; p++) {
+        o->tile_w[p] = 32;
+        o->tile_h[p] = 8;
+    }
 }
 
 int ifl_batch_create(ifl_solver *const *members, int n, const ifl_batch_options *opt, ifl_batch **out) {

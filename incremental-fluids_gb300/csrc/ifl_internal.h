@@ -210,16 +210,24 @@ struct BatchInflow {
 };
 
 // Tiles of 32x8 threads that cover every grid of a w x h scene.
-inline int batch_tiles(int w, int h) { return ((w + 2 + 31) / 32) * ((h + 2 + 7) / 8); }
+inline int batch_tiles(int w, int h, int tw = 32, int th = 8) {
+    return ((w + 2 + tw - 1) / tw) * ((h + 2 + th - 1) / th);
+}
+// Candidate tile shapes (threads x rows) of the batched tiled phases; the
+// first is the default.
+constexpr int kTileShapes = 6;
+constexpr int kTileW[kTileShapes] = {32, 32, 64, 16, 128, 64};
+constexpr int kTileH[kTileShapes] = {8, 4, 4, 16, 2, 2};
 
 // Device view of a batch of scenes for the batched phase launches.
 template <typename F>
 struct SceneBatch {
     const Scene<F> *scenes;        // n scenes
-    const int *tile_start;         // n + 1 prefix sums of batch_tiles
+    const int *tile_start;         // n + 1 prefix sums of batch_tiles for tiles of tw x th
     const BatchInflow *inflows;    // inflows of all scenes, scene by scene
     const int *inflow_start;       // n + 1 prefix sums
     int n, tiles;
+    int tw, th;                    // tile shape (threads x rows of one block)
 };
 
 template <typename F> void launch_batch_inflow(const SceneBatch<F> &B, cudaStream_t st);

@@ -951,10 +951,11 @@ void launch_sd_to_rows(const Scene<F> &S, F *rows, const double *sd_arr, cudaStr
 
 // ------------------------------------------------------------ batched phases
 // One launch runs a phase for every scene of a batch.  A scene covers
-// batch_tiles(w, h) tiles of 32x8 threads, enough for every grid of the scene
-// (the bodies bound-check their own grid); blockIdx.x enumerates the tiles of
-// all scenes through the prefix table tile_start, blockIdx.y is the phase's
-// third grid dimension (quantity or face kind).
+// batch_tiles(w, h, tw, th) tiles of tw x th threads (the batch's shape for the
+// phase), enough for every grid of the scene (the bodies bound-check their own
+// grid and index by blockDim); blockIdx.x enumerates the tiles of all scenes
+// through the prefix table tile_start, blockIdx.y is the phase's third grid
+// dimension (quantity or face kind).
 namespace {
 
 template <typename F>
@@ -972,7 +973,7 @@ template <typename F, typename Op>
 __global__ void __launch_bounds__(256) batch_tiles_kernel(SceneBatch<F> B, Op op) {
     const int i = scene_of_tile(B, blockIdx.x);
     const Scene<F> &S = B.scenes[i];
-    const int tx = (S.w + 2 + 31) / 32;
+    const int tx = (S.w + 2 + (int)blockDim.x - 1) / (int)blockDim.x;
     const int local = blockIdx.x - B.tile_start[i];
     op(S, make_uint3(local % tx, local / tx, blockIdx.y));
 }
@@ -1054,7 +1055,7 @@ __global__ void __launch_bounds__(1024) batch_extrap_solve_kernel(SceneBatch<F> 
 
 template <typename F, typename Op>
 void tiles(const SceneBatch<F> &B, int nz, Op op, cudaStream_t st) {
-    if (B.tiles > 0) batch_tiles_kernel<F, Op><<<dim3(B.tiles, nz), dim3(32, 8), 0, st>>>(B, op);
+    if (B.tiles > 0) batch_tiles_kernel<F, Op><<<dim3(B.tiles, nz), dim3(B.tw, B.th), 0, st>>>(B, op);
 }
 
 }  // namespace

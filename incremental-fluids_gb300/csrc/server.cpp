@@ -264,7 +264,7 @@ class Server {
         }
         rebuilds_++;
         dirty_ = false;
-        if (opt_.threads == 0) tune_pending_ = true;
+        if (opt_.threads == 0 || opt_.tile_tune == 1) tune_pending_ = true;
         return IFL_OK;
     }
 
@@ -277,6 +277,12 @@ class Server {
             opt_.threads = bi.threads;
             opt_.strips_per_block = bi.strips_per_block;
             opt_.stages = bi.stages;
+            // and its tile shapes: a rebuilt batch times no candidates again
+            opt_.tile_tune = 2;
+            for (int p = 0; p < 8; p++) {
+                opt_.tile_w[p] = bi.tile_w[p];
+                opt_.tile_h[p] = bi.tile_h[p];
+            }
             tune_pending_ = false;
         }
     }

@@ -97,7 +97,13 @@ class Inflow(C.Structure):
 
 class BatchOptions(C.Structure):
     _fields_ = [("threads", C.c_int32), ("strips_per_block", C.c_int32), ("stages", C.c_int32),
-                ("use_graph", C.c_int32), ("tune_iterations", C.c_int32), ("max_team_blocks", C.c_int32)]
+                ("use_graph", C.c_int32), ("tune_iterations", C.c_int32), ("max_team_blocks", C.c_int32),
+                ("tile_tune", C.c_int32), ("pad_", C.c_int32), ("tile_w", C.c_int32 * 8), ("tile_h", C.c_int32 * 8)]
+
+
+# Tiled phases of a batch step (ifl_batch_options.tile_w / tile_h, ifl_batch_info)
+TILE_PHASES = ("fill", "bc", "assemble", "heat_assemble", "advect", "apply", "buoyancy", "mask")
+TILE_SHAPES = ((32, 8), (32, 4), (64, 4), (16, 16), (128, 2), (64, 2))
 
 
 class BatchInfo(C.Structure):
@@ -105,7 +111,8 @@ class BatchInfo(C.Structure):
                 ("stages", C.c_int32), ("grid", C.c_int32), ("graph", C.c_int32), ("candidates", C.c_int32),
                 ("pad_", C.c_int32), ("candidate_ms", C.c_double * 8), ("last_step_ms", C.c_double),
                 ("last_pcg_ms", C.c_double), ("launches", C.c_int64), ("steps", C.c_int64),
-                ("h2d_bytes_last_step", C.c_int64), ("d2h_bytes_last_step", C.c_int64)]
+                ("h2d_bytes_last_step", C.c_int64), ("d2h_bytes_last_step", C.c_int64),
+                ("tile_w", C.c_int32 * 8), ("tile_h", C.c_int32 * 8), ("tile_ms", C.c_double * 8)]
 
 
 class ServerParams(C.Structure):
@@ -539,7 +546,8 @@ class Batch:
     """
 
     def __init__(self, solvers: Sequence[FluidSolver], threads: int = 0, strips_per_block: int = 0,
-                 stages: int = 0, use_graph: bool = True, tune_iterations: int = 8, max_team_blocks: int = 0):
+                 stages: int = 0, use_graph: bool = True, tune_iterations: int = 8, max_team_blocks: int = 0,
+                 tiles=None):
         self._L = load_library()
         self.solvers = list(solvers)
         o = BatchOptions()
@@ -548,6 +556,16 @@ class Batch:
         o.use_graph = 1 if use_graph else 0
         o.tune_iterations = int(tune_iterations)
         o.max_team_blocks = int(max_team_blocks)
+        # tiles: None = tune at the first update; "default" = 32 x 8; or a
+        # {phase name: (threads, rows)} dict (phases not named: 32 x 8)
+        if tiles is None:
+            o.tile_tune = 1
+        elif tiles == "default":
+            o.tile_tune = 0
+        else:
+            o.tile_tune = 2
+            for k, name in enumerate(TILE_PHASES):
+                o.tile_w[k], o.tile_h[k] = tiles.get(name, (32, 8))
         arr = (C.c_void_p * len(self.solvers))(*[s._h for s in self.solvers])
         h_ = C.c_void_p()
         rc = self._L.ifl_batch_create(arr, len(self.solvers), C.byref(o), C.byref(h_))
@@ -605,7 +623,9 @@ class Batch:
                 "last_step_ms": o.last_step_ms, "last_pcg_ms": o.last_pcg_ms,
                 "launches": int(o.launches), "steps": int(o.steps),
                 "h2d_bytes_last_step": int(o.h2d_bytes_last_step),
-                "d2h_bytes_last_step": int(o.d2h_bytes_last_step)}
+                "d2h_bytes_last_step": int(o.d2h_bytes_last_step),
+                "tiles": {name: (o.tile_w[k], o.tile_h[k]) for k, name in enumerate(TILE_PHASES)},
+                "tile_ms": {name: o.tile_ms[k] for k, name in enumerate(TILE_PHASES[:5]) if o.tile_ms[k] > 0}}
 
     @property
     def stream(self) -> int:

@@ -72,6 +72,8 @@ def test_batch_options_defaults(ifl):
     o = ifl.BatchOptions()
     ifl.load_library().ifl_batch_default_options(C.byref(o))
     assert (o.threads, o.use_graph, o.tune_iterations) == (0, 1, 8)
+    assert o.tile_tune == 1 and list(o.tile_w) == [32] * 8 and list(o.tile_h) == [8] * 8
+    assert C.sizeof(o) == 8 * 4 + 2 * 8 * 4  # the C struct: 6 ints, tile_tune, pad, two int[8]
 
 
 def test_batch_create_rejects_empty(ifl):

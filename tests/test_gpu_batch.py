@@ -208,6 +208,37 @@ def test_autotuner_tries_shapes_and_keeps_one(ifl):
     assert info["grid"] > 0 and info["steps"] == 2 and info["launches"] > 0
 
 
+def test_tile_autotuner_keeps_a_candidate_per_phase(ifl):
+    b, _ = _run(ifl, ifl.FP32, 2)
+    info = b.info()
+    assert set(info["tile_ms"]) == {"fill", "bc", "assemble", "advect"}  # variant 4: no heat assembly
+    for name, shape in info["tiles"].items():
+        assert tuple(shape) in ifl.TILE_SHAPES, (name, shape)
+    for name in ("apply", "buoyancy", "mask"):
+        assert tuple(info["tiles"][name]) == (32, 8)
+
+
+@pytest.mark.parametrize("variant", [5, 7])
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+def test_tile_shapes_do_not_change_results(ifl, variant, precision):
+    """Every tuned phase on another tile shape than 32 x 8 gives bit-identical
+    fields (each cell's arithmetic is independent of the tiling)."""
+    forced = {"fill": (16, 16), "bc": (128, 2), "assemble": (64, 4), "heat_assemble": (32, 4),
+              "advect": (64, 2)}
+    out = []
+    for tiles in ("default", forced):
+        ms, oracles, gpus, b = build(ifl, variant, precision=precision, tiles=tiles)
+        for _ in range(3):
+            b.update(DT)
+        names = ("d", "u", "v", "p") + (("t",) if variant >= 6 else ())
+        out.append([[g.read_field(n) for n in names] for g in gpus])
+        if tiles != "default":
+            assert {k: tuple(v) for k, v in b.info()["tiles"].items() if k in forced} == forced
+    for x, y in zip(*out):
+        for u, v in zip(x, y):
+            assert np.array_equal(u, v)
+
+
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
 def test_batch_equals_single_handles_bit_for_bit(ifl, precision):
     """Ragged generated scenes (sides 64..320, 0-4 bodies, 1-3 inflows): every
