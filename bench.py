@@ -257,12 +257,13 @@ def cpu_baseline(n: int, steps: int, warmup: int, procs: int, seed: int):
 
 
 # ----------------------------------------------------------------- GPU arm
-def make_solver(ifl, sc, precision, device, bodies):
+def make_solver(ifl, sc, precision, device, bodies, pcg_cap=0):
+    cap = {"max_iter_pressure": pcg_cap} if pcg_cap > 0 else {}
     if sc.variant >= 6:
         return ifl.FluidSolver(sc.w, sc.h, sc.density, sc.density_soot, sc.diffusion, bodies, variant=sc.variant,
-                               precision=precision, device=device)
+                               precision=precision, device=device, **cap)
     return ifl.FluidSolver(sc.w, sc.h, sc.density, bodies, variant=sc.variant, precision=precision,
-                           device=device)
+                           device=device, **cap)
 
 
 def body_objs(ifl, sc):
@@ -298,9 +299,9 @@ def run_gpu(args, rank, world, local_rank):
     # pass, so that both time the same steps (the PCG iteration count varies with
     # the state of the flow)
     bodies = body_objs(ifl, sc)
-    g = make_solver(ifl, sc, prec, local_rank, bodies)
+    g = make_solver(ifl, sc, prec, local_rank, bodies, args.pcg_cap)
     bodies_e = body_objs(ifl, sc)
-    ge = make_solver(ifl, sc, prec, local_rank, bodies_e)
+    ge = make_solver(ifl, sc, prec, local_rank, bodies_e, args.pcg_cap)
     stream = torch.cuda.ExternalStream(g.stream, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -823,13 +824,13 @@ def run_batch(args, rank, world, local_rank):
     achieved = pcg_bytes / (sum(pcg_ms) / 1e3) / 1e9 if sum(pcg_ms) > 0 else 0.0
     # DRAM traffic of one launch: the full batch is too large to capture under
     # the profiler's size rule, so it is scaled from a DRAM-only capture of 32
-    # tall scenes (6.9 M cells, working set ~4x the L2), where the kernel moved
-    # 1.08x its algorithmic bytes (profiles/pcg_batch_kernel_dram_scaling.md)
-    traffic_ratio = 1.08
+    # tall scenes (6.9 M cells, working set ~4x the L2, 20 pinned iterations),
+    # where the kernel moved 1.05x its algorithmic bytes
+    traffic_ratio = 1.05
     roof = {"bound": "hbm", "kernel": "pcg_batch_kernel", "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": f"of {peak_kind}",
             "traffic": round(traffic_ratio * pcg_bytes / args.steps),
-            "traffic_source": "scaled from a 32-scene DRAM capture: 1.08 x algorithmic bytes",
+            "traffic_source": "scaled from a 32-scene DRAM capture: 1.05 x algorithmic bytes",
             "algorithmic_bytes_per_step": round(pcg_bytes / args.steps),
             "kernel_bytes_per_step": round(kernel_bytes / args.steps),
             "kernel_bytes_gbs": round(kernel_bytes / (sum(pcg_ms) / 1e3) / 1e9, 1) if sum(pcg_ms) > 0 else 0.0,
@@ -1021,6 +1022,9 @@ def main():
     ap.add_argument("--max-team-blocks", type=int, default=0, help="batch: largest PCG team in blocks (0 = library default)")
     ap.add_argument("--shape", default="", help="batch: fixed PCG shape threads,strips_per_block,stages (default: autotuned)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--pcg-cap", type=int, default=0,
+                    help="single / c3: cap the pressure PCG at this many iterations (a short launch for profiler "
+                         "captures; the line then names the cap and is not the benchmark)")
     ap.add_argument("--field-check", type=int, default=-1,
                     help="scenes whose next update is compared with the FP64 reference after the timed region "
                          "(default: 8 for the batch, 1 for the 1024^2 scene, 0 otherwise)")
@@ -1084,6 +1088,8 @@ def main():
                   "variant": "4-solid-boundaries", "grid": [args.size, args.size], "bodies": 3, "seed": args.seed,
                   "precision_form": args.precision, "l2": "flushed between timed steps (512 MiB write)",
                   "scene_data": "seeded synthetic scene"}
+    if args.pcg_cap > 0 and args.workload in ("single", "c3"):
+        config["pcg_cap"] = f"pressure PCG capped at {args.pcg_cap} iterations (profiling case, not the benchmark)"
 
     if args.impl == "reference":
         if rank != 0:
