@@ -980,29 +980,35 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                     for (int q = 0; q < 5; q++)
                         sv[q] = iter == 0 ? vz[q] : ((vn[q] & NB_RED) ? F(vz[q] + vs[q] * fbeta) : vs[q]);
                     // FP64 form: FP64 accumulation in the reference's order.  FP32
-                    // form: an error-free float-float sum on the FP32 pipes (GB300
-                    // runs FP64 at 1/64 of the FP32 rate), and for the pressure
-                    // matrices, whose rows sum to zero in the reference
-                    // (aDiag = sum of the face factors, each off-diagonal = -factor),
-                    // the form sum_j a_ij (s_j - s_i), which keeps that property
-                    // exactly: the FP32-rounded aDiag no longer matches its
-                    // off-diagonals, and the resulting tiny, non-zero eigenvalue made
-                    // CG stagnate on some scenes (up to the 2000-iteration cap).
+                    // form, pressure matrices (rows sum to zero in the reference:
+                    // aDiag = sum of the face factors, each off-diagonal = -factor):
+                    // the form sum_j a_ij (s_j - s_i), in FP32 fused multiply-adds.
+                    // It keeps the zero row sums exactly (with the FP32-rounded aDiag
+                    // the plain form left a tiny, non-zero eigenvalue that made CG
+                    // stagnate on some scenes, up to the 2000-iteration cap), and its
+                    // terms carry no cancellation between the diagonal and the
+                    // neighbours, so FP32 accumulation suffices: against a
+                    // float-float sum, the 512-scene batch ran the same iteration
+                    // counts (to 3 of 639 on the longest solve) with a pressure error
+                    // against the FP64 reference of 1.5e-6 (8e-7), 7 % faster.
+                    // Other FP32-form matrices (heat): a float-float sum of the
+                    // exact products on the FP32 pipes (GB300 runs FP64 at 1/64 of
+                    // the FP32 rate).
                     double t;
                     if constexpr (kF32) {
-                        FF acc;
                         if (A.rowsum_zero) {
-                            acc = FF{0.f, 0.f};
+                            float tf = 0.f;
 #pragma unroll
                             for (int q = 1; q < 5; q++)
-                                if (fl & (2u << q)) acc = ff_add(acc, ff_prod(va[q], sv[q] - sv[0]));
+                                if (fl & (2u << q)) tf = fmaf(va[q], sv[q] - sv[0], tf);
+                            t = (double)tf;
                         } else {
-                            acc = ff_prod(va[0], sv[0]);
+                            FF acc = ff_prod(va[0], sv[0]);
 #pragma unroll
                             for (int q = 1; q < 5; q++)
                                 if (fl & (2u << q)) acc = ff_add(acc, ff_prod(va[q], sv[q]));
+                            t = (double)acc.hi + (double)acc.lo;
                         }
-                        t = (double)acc.hi + (double)acc.lo;
                     } else {
                         t = (double)va[0] * (double)sv[0];
 #pragma unroll
