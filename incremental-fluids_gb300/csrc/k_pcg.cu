@@ -107,6 +107,7 @@ struct PcgArgs {
     int mode, limit, pinned;
     int K, stages;
     int rowsum_zero;  // 1: pressure matrix (rows sum to zero), 0: heat matrix
+    int all_red;      // 1: every cell takes part in the dot products and AXPYs (unmasked solves)
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -881,15 +882,19 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
     // aPlusY of r0-1 .. r0+U-1, aDiag of the unit.  The lower neighbour of lane
     // 0 and the upper neighbour of lane 31 live in the adjacent strips; lanes
     // 0..U-1 and 16..16+U-1 load them and hand them over by shuffle.
-    auto matvec = [&](int iter, double beta) -> void {
+    // kAllRed (the unmasked pressure solves of steps 3-5, whose every cell is
+    // red): the neighbour bits are neither staged nor read, as every in-grid
+    // neighbour takes the s-update.
+    auto matvec = [&](int iter, double beta, auto all_red_tag) -> void {
+        constexpr bool kAllRed = decltype(all_red_tag)::value;
         const F fbeta = (F)beta;
         auto need = [](int v) {
-            return (unsigned)(v + 2) * 32u * (2u * sizeof(F) + 1u) + (unsigned)v * 32u * sizeof(F) +
+            return (unsigned)(v + 2) * 32u * (2u * sizeof(F) + (kAllRed ? 0u : 1u)) + (unsigned)v * 32u * sizeof(F) +
                    2u * (unsigned)(v + 1) * 32u * sizeof(F);
         };
         int U = kChunk;
         while (U > 1 && need(U) > R.sbytes) U >>= 1;
-        const unsigned rz = (unsigned)(U + 2) * 32u * sizeof(F), rn = (unsigned)(U + 2) * 32u,
+        const unsigned rz = (unsigned)(U + 2) * 32u * sizeof(F), rn = kAllRed ? 0u : (unsigned)(U + 2) * 32u,
                        ra = (unsigned)U * 32u * sizeof(F), rxy = (unsigned)(U + 1) * 32u * sizeof(F);
         const unsigned oz = R.sbuf, os = oz + rz, onb = os + rz, oad = onb + rn, oax = oad + ra, oay = oax + rxy;
         const F *__restrict__ zp = A.z;
@@ -905,12 +910,12 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 if (unit_begin()) {
                     uint64_t *bar = R.stage_bar();
                     const unsigned tx = 2u * clipped_bytes<F>(r0 - 1, r0 + U + 1, rows) +
-                                        clipped_bytes<uint8_t>(r0 - 1, r0 + U + 1, rows) +
+                                        (kAllRed ? 0u : clipped_bytes<uint8_t>(r0 - 1, r0 + U + 1, rows)) +
                                         clipped_bytes<F>(r0, r0 + U, rows) + 2u * clipped_bytes<F>(r0 - 1, r0 + U, rows);
                     mbar_expect_tx(bar, tx);
                     stage_rows(oz, zp, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
                     stage_rows(os, so, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
-                    stage_rows(onb, A.nb, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
+                    if (!kAllRed) stage_rows(onb, A.nb, r0 - 1, r0 - 1, r0 + U + 1, rows, bar);
                     stage_rows(oad, A.adiag, r0, r0, r0 + U, rows, bar);
                     stage_rows(oax, A.ax, r0 - 1, r0 - 1, r0 + U, rows, bar);
                     stage_rows(oay, A.ay, r0 - 1, r0 - 1, r0 + U, rows, bar);
@@ -924,13 +929,13 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                         const size_t k = sd.slot(d, 32 * s - 1);
                         xz = zp[k];
                         xs = so[k];
-                        xn = A.nb[k];
+                        if (!kAllRed) xn = A.nb[k];
                         xa = A.ay[k];
                     } else if (j < U && lane >= 16 && d - 31 >= 0 && d - 31 < W && 32 * s + 32 < H) {  // above lane 31
                         const size_t k = sd.slot(d - 31, 32 * s + 32);
                         xz = zp[k];
                         xs = so[k];
-                        xn = A.nb[k];
+                        if (!kAllRed) xn = A.nb[k];
                     }
                 }
                 stage_wait(R, A.fl);
@@ -942,9 +947,9 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 const F *say = (const F *)(g_smem + oay);
                 for (int u = 0; u < U; u++) {
                     const F dz = __shfl_sync(FULL, xz, u), ds = __shfl_sync(FULL, xs, u), da = __shfl_sync(FULL, xa, u);
-                    const unsigned dn = __shfl_sync(FULL, xn, u);
+                    const unsigned dn = kAllRed ? 0u : __shfl_sync(FULL, xn, u);
                     const F uz = __shfl_sync(FULL, xz, 16 + u), us = __shfl_sync(FULL, xs, 16 + u);
-                    const unsigned un = __shfl_sync(FULL, xn, 16 + u);
+                    const unsigned un = kAllRed ? 0u : __shfl_sync(FULL, xn, 16 + u);
                     const int x = d0 + u - lane, y = s * 32 + lane;
                     const bool in = x >= 0 && x < W && y < H;
                     const bool hl = in && x > 0, hd = in && y > 0, hr = in && x < W - 1, hu = in && y < H - 1;
@@ -954,20 +959,25 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                     // a missing neighbour takes the cell's own values and is not used
                     F vz[5], vs[5], va[5];
                     unsigned vn[5];
-                    vz[0] = szv[k0]; vs[0] = ssv[k0]; vn[0] = snb[k0];
-                    vz[1] = hl ? szv[kl] : vz[0]; vs[1] = hl ? ssv[kl] : vs[0]; vn[1] = hl ? snb[kl] : vn[0];
+                    // neighbour bits (kAllRed: every cell red, no load)
+                    auto nbits = [&](bool h, int k, unsigned other) -> unsigned {
+                        if constexpr (kAllRed) return NB_RED;
+                        else return h ? (unsigned)snb[k] : other;
+                    };
+                    vz[0] = szv[k0]; vs[0] = ssv[k0]; vn[0] = nbits(true, k0, 0u);
+                    vz[1] = hl ? szv[kl] : vz[0]; vs[1] = hl ? ssv[kl] : vs[0]; vn[1] = nbits(hl, kl, vn[0]);
                     if (lane > 0) {
-                        vz[2] = hd ? szv[kd] : vz[0]; vs[2] = hd ? ssv[kd] : vs[0]; vn[2] = hd ? snb[kd] : vn[0];
+                        vz[2] = hd ? szv[kd] : vz[0]; vs[2] = hd ? ssv[kd] : vs[0]; vn[2] = nbits(hd, kd, vn[0]);
                         va[2] = hd ? say[u * 32 + lane - 1] : F(0);
                     } else {
-                        vz[2] = hd ? dz : vz[0]; vs[2] = hd ? ds : vs[0]; vn[2] = hd ? dn : vn[0];
+                        vz[2] = hd ? dz : vz[0]; vs[2] = hd ? ds : vs[0]; vn[2] = kAllRed ? NB_RED : (hd ? dn : vn[0]);
                         va[2] = hd ? da : F(0);
                     }
-                    vz[3] = hr ? szv[kr] : vz[0]; vs[3] = hr ? ssv[kr] : vs[0]; vn[3] = hr ? snb[kr] : vn[0];
+                    vz[3] = hr ? szv[kr] : vz[0]; vs[3] = hr ? ssv[kr] : vs[0]; vn[3] = nbits(hr, kr, vn[0]);
                     if (lane < 31) {
-                        vz[4] = hu ? szv[ku] : vz[0]; vs[4] = hu ? ssv[ku] : vs[0]; vn[4] = hu ? snb[ku] : vn[0];
+                        vz[4] = hu ? szv[ku] : vz[0]; vs[4] = hu ? ssv[ku] : vs[0]; vn[4] = nbits(hu, ku, vn[0]);
                     } else {
-                        vz[4] = hu ? uz : vz[0]; vs[4] = hu ? us : vs[0]; vn[4] = hu ? un : vn[0];
+                        vz[4] = hu ? uz : vz[0]; vs[4] = hu ? us : vs[0]; vn[4] = kAllRed ? NB_RED : (hu ? un : vn[0]);
                     }
                     va[0] = sad[u * 32 + lane];
                     va[1] = sax[u * 32 + lane];        // aPlusX of the left neighbour (row r0+u-1)
@@ -1117,7 +1127,8 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             // block-uniform: every thread of the block leaves together
             if (__syncthreads_or(threadIdx.x == 0 && timed_out(A.fl))) break;
             // s = z + beta*s (first iteration: s = z), then z' = A s and z'.s  (:361-362, 375)
-            matvec(iter, beta);
+            if (A.all_red) matvec(iter, beta, std::true_type{});
+            else matvec(iter, beta, std::false_type{});
             team_barrier(T, A.fl);
             const double alpha = sigma / chunk_total(1, false, nchunk);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
@@ -1316,6 +1327,7 @@ PcgArgs<F> make_args(const Scene<F> &S, const PcgScratch &X, int heat) {
     A.out = X.out + (heat ? 1 : 0);
     A.iter_total = X.iter_total;
     A.rowsum_zero = heat ? 0 : 1;
+    A.all_red = (!heat && S.variant < 6) ? 1 : 0;
     return A;
 }
 }  // namespace
@@ -1346,6 +1358,7 @@ PcgArgs<float> make_args_f32(const Scene<double> &S, const PcgF32 &M, const PcgS
     A.out = X.out + (heat ? 1 : 0);
     A.iter_total = X.iter_total;
     A.rowsum_zero = heat ? 0 : 1;
+    A.all_red = (!heat && S.variant < 6) ? 1 : 0;
     return A;
 }
 __global__ void matrix_to_f32_kernel(const double *a, const double *b, const double *c, float *fa, float *fb,
