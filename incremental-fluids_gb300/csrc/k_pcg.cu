@@ -1038,8 +1038,10 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
 
     // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366), staged
     // p, r, A*s, s and the neighbour bits of a unit.
-    auto axpy = [&](int iter, double alpha) -> void {
-        constexpr unsigned kRow = 32u * (8u + 8u + 8u + sizeof(F) + 1u);
+    // kAllRed: the red cells are the grid's own cells (no neighbour bits staged).
+    auto axpy = [&](int iter, double alpha, auto all_red_tag) -> void {
+        constexpr bool kAllRed = decltype(all_red_tag)::value;
+        constexpr unsigned kRow = 32u * (8u + 8u + 8u + sizeof(F) + (kAllRed ? 0u : 1u));
         const int U = unit_rows(R.sbytes, kRow);
         const unsigned op = R.sbuf, orr = op + U * 256u, oas = orr + U * 256u, osn = oas + U * 256u,
                        onb = osn + U * 32u * sizeof(F);
@@ -1050,6 +1052,7 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
         if (lane == 0) fence_proxy_async_global();
         for (int c = c_begin; c < c_end; c++) {
             unsigned long long mx = 0ull;  // bits of the largest |r| so far
+            const int s = (c * kChunk) / D, y = s * 32 + lane;  // the chunk's strip, this lane's row
             for (int r0 = c * kChunk; r0 < (c + 1) * kChunk; r0 += U) {
                 if (unit_begin()) {
                     uint64_t *bar = R.stage_bar();
@@ -1058,7 +1061,7 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                     stage_rows(orr, A.r, r0, r0, r0 + U, rows, bar);
                     stage_rows(oas, A.as, r0, r0, r0 + U, rows, bar);
                     stage_rows(osn, snp, r0, r0, r0 + U, rows, bar);
-                    stage_rows(onb, A.nb, r0, r0, r0 + U, rows, bar);
+                    if (!kAllRed) stage_rows(onb, A.nb, r0, r0, r0 + U, rows, bar);
                 }
                 stage_wait(R, A.fl);
                 const double *sp = (const double *)(g_smem + op);
@@ -1068,7 +1071,14 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 const uint8_t *snb = (const uint8_t *)(g_smem + onb);
                 for (int u = 0; u < U; u++) {
                     const int k = u * 32 + lane;
-                    if (snb[k] & NB_RED) {
+                    bool red;
+                    if constexpr (kAllRed) {
+                        const int x = r0 + u - s * D - lane;
+                        red = x >= 0 && x < W && y < H;
+                    } else {
+                        red = snb[k] & NB_RED;
+                    }
+                    if (red) {
                         const size_t i = (size_t)(r0 + u) * 32 + lane;
                         // FP32 form: one rounding per update (fused); FP64 form: the
                         // reference's two
@@ -1132,7 +1142,8 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
             team_barrier(T, A.fl);
             const double alpha = sigma / chunk_total(1, false, nchunk);
             // p += alpha s; r -= alpha z'; maxError = |r|_inf  (:363-366)
-            axpy(iter, alpha);
+            if (A.all_red) axpy(iter, alpha, std::true_type{});
+            else axpy(iter, alpha, std::false_type{});
             team_barrier(T, A.fl);
             maxError = chunk_total(0, true, nchunk);
             iterations = iter + 1;
