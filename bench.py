@@ -929,6 +929,9 @@ def run_serve(args, local_rank):
     lat64, work = [], 0
     t64 = time.perf_counter()
     for k, sc in enumerate(scs):
+        if args.serve_no_fp64:
+            work += sc.cells * steps[k]
+            continue
         wait = offsets[k] - (time.perf_counter() - t64)
         if wait > 0:
             time.sleep(wait)
@@ -964,11 +967,10 @@ def run_serve(args, local_rank):
             "batch_rebuilds": info["rebuilds"], "rebuild_ms_total": round(info["rebuild_ms"], 1),
             "rebuild_ms_per_membership_change": round(info["rebuild_ms"] / max(1, info["rebuilds"]), 2),
             "hbm_budget_gb": args.serve_budget_gb,
-            "fp64_one_at_a_time": {"p50_latency_s": round(pct(lat64, 0.5), 3),
-                                   "p99_latency_s": round(pct(lat64, 0.99), 3),
-                                   "cell_steps_per_s": round(work / wall64, 1), "wall_s": round(wall64, 2),
-                                   "how": "run: FP64 drop-in (ifl_update), one request at a time in arrival "
-                                          "order on the same arrivals"}}
+            "fp64_one_at_a_time": None if args.serve_no_fp64 else
+            {"p50_latency_s": round(pct(lat64, 0.5), 3), "p99_latency_s": round(pct(lat64, 0.99), 3),
+             "cell_steps_per_s": round(work / wall64, 1), "wall_s": round(wall64, 2),
+             "how": "run: FP64 drop-in (ifl_update), one request at a time in arrival order on the same arrivals"}}
 
 
 # ------------------------------------------------------- profiler case
@@ -1017,6 +1019,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-steps-scale", type=float, default=0.1, help="scale of the U[50,500] steps per request")
     ap.add_argument("--serve-budget-gb", type=float, default=64.0, help="HBM budget of the serving run")
+    ap.add_argument("--serve-no-fp64", action="store_true",
+                    help="skip the FP64 one-at-a-time serving leg (it takes about 10x the batched leg's time)")
     ap.add_argument("--cpu-procs", type=int, default=0, help="host processes for the CPU legs (0 = auto)")
     ap.add_argument("--cpu-sample", type=int, default=32, help="batch: scenes of the CPU sample (size-stratified)")
     ap.add_argument("--max-team-blocks", type=int, default=0, help="batch: largest PCG team in blocks (0 = library default)")
