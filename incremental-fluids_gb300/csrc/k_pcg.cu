@@ -945,6 +945,20 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                 const F *sad = (const F *)(g_smem + oad);
                 const F *sax = (const F *)(g_smem + oax);
                 const F *say = (const F *)(g_smem + oay);
+                // A register window slides along the unit's diagonals: row r0+u-1
+                // (L: the left neighbour), r0+u (C: the cell) and r0+u+1 (R: the
+                // right neighbour) of this lane; the lower neighbour is lane-1's L
+                // and the upper one lane+1's R (shuffles), lanes 0 and 31 take
+                // theirs from the adjacent strips.  Per diagonal a lane loads only
+                // row R and the cell's coefficients.  A neighbour outside the grid
+                // holds whatever its slot holds and is not used (fl).
+                F zL = szv[lane], sL = ssv[lane], zC = szv[32 + lane], sC = ssv[32 + lane];
+                F axL = sax[lane], ayL = say[lane];
+                unsigned nL = 0u, nC = 0u;
+                if constexpr (!kAllRed) {
+                    nL = snb[lane];
+                    nC = snb[32 + lane];
+                }
                 for (int u = 0; u < U; u++) {
                     const F dz = __shfl_sync(FULL, xz, u), ds = __shfl_sync(FULL, xs, u), da = __shfl_sync(FULL, xa, u);
                     const unsigned dn = kAllRed ? 0u : __shfl_sync(FULL, xn, u);
@@ -953,36 +967,41 @@ __device__ void pcg_job(const PcgArgs<F> &A, const Team &T, Ring<F> &R, double *
                     const int x = d0 + u - lane, y = s * 32 + lane;
                     const bool in = x >= 0 && x < W && y < H;
                     const bool hl = in && x > 0, hd = in && y > 0, hr = in && x < W - 1, hu = in && y < H - 1;
-                    const int k0 = (u + 1) * 32 + lane;  // the cell (z, s, bits)
-                    const int kl = u * 32 + lane, kr = (u + 2) * 32 + lane;
-                    const int kd = u * 32 + lane - 1, ku = (u + 2) * 32 + lane + 1;
-                    // a missing neighbour takes the cell's own values and is not used
-                    F vz[5], vs[5], va[5];
-                    unsigned vn[5];
-                    // neighbour bits (kAllRed: every cell red, no load)
-                    auto nbits = [&](bool h, int k, unsigned other) -> unsigned {
-                        if constexpr (kAllRed) return NB_RED;
-                        else return h ? (unsigned)snb[k] : other;
-                    };
-                    vz[0] = szv[k0]; vs[0] = ssv[k0]; vn[0] = nbits(true, k0, 0u);
-                    vz[1] = hl ? szv[kl] : vz[0]; vs[1] = hl ? ssv[kl] : vs[0]; vn[1] = nbits(hl, kl, vn[0]);
-                    if (lane > 0) {
-                        vz[2] = hd ? szv[kd] : vz[0]; vs[2] = hd ? ssv[kd] : vs[0]; vn[2] = nbits(hd, kd, vn[0]);
-                        va[2] = hd ? say[u * 32 + lane - 1] : F(0);
-                    } else {
-                        vz[2] = hd ? dz : vz[0]; vs[2] = hd ? ds : vs[0]; vn[2] = kAllRed ? NB_RED : (hd ? dn : vn[0]);
-                        va[2] = hd ? da : F(0);
+                    const int kr = (u + 2) * 32 + lane;
+                    const F zR = szv[kr], sR = ssv[kr];
+                    const unsigned nR = kAllRed ? (unsigned)NB_RED : (unsigned)snb[kr];
+                    F zD = __shfl_up_sync(FULL, zL, 1), sD = __shfl_up_sync(FULL, sL, 1);
+                    F aD = __shfl_up_sync(FULL, ayL, 1);
+                    F zU = __shfl_down_sync(FULL, zR, 1), sU = __shfl_down_sync(FULL, sR, 1);
+                    unsigned nD = kAllRed ? (unsigned)NB_RED : __shfl_up_sync(FULL, nL, 1);
+                    unsigned nU = kAllRed ? (unsigned)NB_RED : __shfl_down_sync(FULL, nR, 1);
+                    if (lane == 0) {
+                        zD = dz;
+                        sD = ds;
+                        aD = da;
+                        if constexpr (!kAllRed) nD = dn;
                     }
-                    vz[3] = hr ? szv[kr] : vz[0]; vs[3] = hr ? ssv[kr] : vs[0]; vn[3] = nbits(hr, kr, vn[0]);
-                    if (lane < 31) {
-                        vz[4] = hu ? szv[ku] : vz[0]; vs[4] = hu ? ssv[ku] : vs[0]; vn[4] = nbits(hu, ku, vn[0]);
-                    } else {
-                        vz[4] = hu ? uz : vz[0]; vs[4] = hu ? us : vs[0]; vn[4] = kAllRed ? NB_RED : (hu ? un : vn[0]);
+                    if (lane == 31) {
+                        zU = uz;
+                        sU = us;
+                        if constexpr (!kAllRed) nU = un;
                     }
-                    va[0] = sad[u * 32 + lane];
-                    va[1] = sax[u * 32 + lane];        // aPlusX of the left neighbour (row r0+u-1)
-                    va[3] = sax[(u + 1) * 32 + lane];  // aPlusX of the cell
-                    va[4] = say[(u + 1) * 32 + lane];  // aPlusY of the cell
+                    const F axC = sax[(u + 1) * 32 + lane], ayC = say[(u + 1) * 32 + lane];
+                    F vz[5] = {zC, zL, zD, zR, zU}, vs[5] = {sC, sL, sD, sR, sU};
+                    // aDiag of the cell, aPlusX of the left neighbour, aPlusY of the
+                    // lower one, aPlusX and aPlusY of the cell
+                    F va[5] = {sad[u * 32 + lane], axL, hd ? aD : F(0), axC, ayC};
+                    unsigned vn[5] = {kAllRed ? (unsigned)NB_RED : nC, kAllRed ? (unsigned)NB_RED : nL, nD, nR, nU};
+                    zL = zC;
+                    sL = sC;
+                    zC = zR;
+                    sC = sR;
+                    axL = axC;
+                    ayL = ayC;
+                    if constexpr (!kAllRed) {
+                        nL = nC;
+                        nC = nR;
+                    }
                     const unsigned fl = (in ? 2u : 0u) | (hl ? 4u : 0u) | (hd ? 8u : 0u) | (hr ? 16u : 0u) |
                                         (hu ? 32u : 0u);
                     F sv[5];
