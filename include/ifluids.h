@@ -315,7 +315,9 @@ typedef struct {
     /* Shape of the batched PCG launch: threads per block (32, 64, 128 or 256),
      * strips per block, bulk-copy ring stages.  threads = 0: autotune at the
      * first update (each candidate shape runs a few pinned PCG iterations of
-     * the real system; the fastest is kept). */
+     * the real system; the fastest is kept, unless the home shape, the first
+     * candidate, is within 5 % of it: such a short trial cannot separate
+     * closer shapes). */
     int32_t threads, strips_per_block, stages;
     int32_t use_graph;        /* 1: replay each step as one CUDA graph (default) */
     int32_t tune_iterations;  /* PCG iterations per autotuning trial (default 8) */

@@ -42,11 +42,18 @@ int pow2ceil(int v) {
     return p;
 }
 
+// The home shape (the first candidate) is kept unless another one is more than
+// kHomeMargin faster in the trial: a trial of a few pinned iterations of the
+// first system cannot separate shapes within a few percent (on GB300 the
+// 512-scene batch ran its steps 19 % faster on 64 x 1 x 2 than on 32 x 1 x 2,
+// which had won such a trial by 1.4 %).
+constexpr double kHomeMargin = 0.05;
+
 template <typename F>
 std::vector<PcgShape> candidate_shapes() {
     if (sizeof(F) == 4)
-        return {{256, 4, 3}, {128, 2, 2}, {128, 1, 2}, {64, 2, 2}, {64, 1, 3}, {64, 1, 2}, {32, 1, 2}, {32, 1, 3}};
-    return {{256, 2, 3}, {128, 2, 2}, {128, 1, 2}, {64, 1, 3}, {64, 1, 2}, {32, 1, 2}, {32, 1, 3}};
+        return {{64, 1, 2}, {256, 4, 3}, {128, 2, 2}, {128, 1, 2}, {64, 2, 2}, {64, 1, 3}, {32, 1, 2}, {32, 1, 3}};
+    return {{128, 1, 2}, {256, 2, 3}, {128, 2, 2}, {64, 1, 3}, {64, 1, 2}, {32, 1, 2}, {32, 1, 3}};
 }
 
 template <typename F>
@@ -637,6 +644,8 @@ class BatchImpl final : public BatchBase {
             err_ = "no batched PCG shape fits this batch";
             return IFL_ERR_UNSUPPORTED;
         }
+        const double home = trial_ms_.empty() ? -1.0 : trial_ms_[0];
+        if (home > 0.0 && home <= best * (1.0 + kHomeMargin)) best_sh = candidate_shapes<F>()[0];
         return make_plan(best_sh);
     }
 
