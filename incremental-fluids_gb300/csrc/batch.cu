@@ -375,6 +375,9 @@ class BatchImpl final : public BatchBase {
     // barriers 15 + 6 log2(g) us for five team barriers per iteration; the
     // sigma pass (about an eighth of the elementwise time) and one barrier have
     // since moved into the forward sweep, leaving 24 ns and 12 + 4.8 log2(g).
+    // The step time is flat around these values: with the faster matvec that
+    // followed, 17, 20 or 30 ns per cell and a lag of 8 us changed the
+    // 512-scene step by less than its step-to-step spread.
     double plan_cost(int i, int g) const {
         constexpr double kTau = 0.11, kLag = 6.4, kElemNs = 24.0;
         const Scene<F> &S = scene(i);
